@@ -1,0 +1,118 @@
+/*
+ * nwgpu.h -- C ABI of the GB300 (sm_103a) all-pairs Needleman-Wunsch,
+ * cherry-traceback and neighbor-joining library (libnwgpu.so).
+ *
+ * Drop-in boundary for the ptersnow/mestrado hot path.  Every entry point is
+ * plain C: POD arguments, caller-owned host buffers (or caller-owned device
+ * pointers for the *_dev forms), an int status return (0 == NWG_OK) instead of
+ * the reference's print-and-exit (AlignmentScore.cu:3-8, :119-122).  The C++
+ * classes with the reference's signatures (AlignmentScore, AlignmentMatch) sit
+ * on top of this ABI in nwgpu_compat.hpp.
+ *
+ * Threading: one nwg_ctx per host thread; calls on one context are not
+ * re-entrant.  A context owns its CUDA stream (or borrows the caller's, see
+ * nwg_set_stream) and all device buffers it needs for its lifetime -- no
+ * per-window malloc/free as in AlignmentScore.cu:286-312.
+ */
+#ifndef NWGPU_H
+#define NWGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define NWG_OK 0
+#define NWG_ERR_NO_DEVICE 1     /* no CUDA device (reference: exit(0), AlignmentScore.cu:119-122) */
+#define NWG_ERR_OOM 2           /* device allocation failed                                      */
+#define NWG_ERR_BAD_RESIDUE 3   /* byte outside the 24-letter alphabet (AlignmentScore.cu:10-27)  */
+#define NWG_ERR_TIMEOUT 4       /* a bounded device wait gave up                                  */
+#define NWG_ERR_OVERFLOW 5      /* a score left the int32 range                                   */
+#define NWG_ERR_INVALID 6       /* bad argument                                                   */
+#define NWG_ERR_CUDA 7          /* CUDA runtime error                                             */
+#define NWG_ERR_EMPTY_SEQ 8     /* zero-length sequence (FastaFile.cpp:55 rejects these too)      */
+#define NWG_ERR_NJ_AMBIGUOUS 9  /* informational: see nwg_nj_stats.ambiguous_steps               */
+
+/* ---- scoring modes ------------------------------------------------------ */
+#define NWG_MODE_BATCHED 0      /* persistent length-bucketed wavefront kernels, int16x2 + int32 */
+#define NWG_MODE_PLAIN 1        /* one thread per pair, int32, one launch per length group       */
+#define NWG_MODE_BATCHED_INT32 2/* batched kernels with every pair on the int32 lanes            */
+
+typedef struct nwg_ctx nwg_ctx;
+
+typedef struct {
+  int64_t pairs;        /* pairs computed, diagonal self-pairs included              */
+  int64_t cells;        /* sum over i<j of L_i*L_j: the GCUPS work unit              */
+  int64_t pairs_int16;  /* pairs that ran on int16x2 lanes                           */
+  int64_t pairs_int32;  /* pairs that ran on int32 lanes                             */
+  int32_t launches;     /* kernels launched by the call                              */
+  int32_t buckets;      /* length buckets                                            */
+  double kernel_ms;     /* device time of the scoring launches (events on the stream)*/
+  double h2d_ms;        /* host->device copies (host-buffer entry points only)       */
+  double d2h_ms;        /* device->host copies (host-buffer entry points only)       */
+  double total_ms;      /* host wall time of the call                                */
+} nwg_stats;
+
+/* Create a context on the current CUDA device.  gap_open/gap_ext are the
+ * penalties of AlignmentScore(gapOpen, gapExt, ...) (AlignmentScore.cu:
+ * 110-136; the aligner passes 10 and 2, SpeciesBlock.cpp:361).  sub is the
+ * 24x24 substitution matrix in the reference's letter order, or NULL for the
+ * built-in blosum64.txt matrix (definitions.cuh:96-121). */
+int nwg_ctx_create(int gap_open, int gap_ext, const int8_t* sub, nwg_ctx** out);
+int nwg_ctx_destroy(nwg_ctx* ctx);
+
+/* Launch on the caller's cudaStream_t (passed as void*) instead of the
+ * context's own stream; NULL restores the context's stream. */
+int nwg_set_stream(nwg_ctx* ctx, void* stream);
+
+const char* nwg_status_str(int status);
+
+/* Last CUDA or argument error seen by the context, as text. */
+const char* nwg_last_error(const nwg_ctx* ctx);
+
+/* ---- host-side encoding (AlignmentScore::parse, AlignmentScore.cu:142-178) */
+
+/* Decode the wire buffer of SpeciesBlock.cpp:309-322
+ * ([int rank][{int seqNo, int len, char[len], '\0'} x n]) into reversed
+ * 8-bit codes.  offsets must hold n+1 entries; codes must hold the residue
+ * total (pass codes == NULL to only fill offsets). */
+int nwg_parse_wire(const char* wire, int n, int8_t* codes, int64_t* offsets);
+
+/* Encode and reverse n ASCII sequences laid end to end (offsets[n+1]). */
+int nwg_encode(const char* ascii, const int64_t* offsets, int n, int8_t* codes);
+
+/* ---- all-pairs distance matrix ----------------------------------------- */
+
+/* Replaces AlignmentScore::loadDB + computeDistanceMtx on one rank
+ * (AlignmentScore.cu:180-277, SpeciesBlock.cpp:361-363): fills the full
+ * n x n row-major float matrix D (leading dimension ld >= n) with
+ * D[i][j] = D[j][i] = (float)score(i, j), diagonal included.  codes/offsets
+ * are reversed codes as produced by nwg_parse_wire/nwg_encode.  Host buffers:
+ * the call copies the codes in and D out. */
+int nwg_score_all(nwg_ctx* ctx, const int8_t* codes, const int64_t* offsets, int n,
+                  float* D, int64_t ld, int mode, nwg_stats* stats);
+
+/* Same with device-resident codes (d_codes) and matrix (d_D); offsets stay on
+ * the host.  Work is queued on the context stream; the call returns once the
+ * kernels are queued unless stats != NULL (then it synchronizes to time). */
+int nwg_score_all_dev(nwg_ctx* ctx, const int8_t* d_codes, const int64_t* offsets, int n,
+                      float* d_D, int64_t ld, int mode, nwg_stats* stats);
+
+/* Rectangular block: D[x][r0 + y] = score(X_x, Y_y) for nx rows of the
+ * loaded set X and ny sequences of block Y -- the computeDistanceMtx(rbuf,
+ * rSz, distances, r0) shape (AlignmentScore.cu:187-277).  Host buffers. */
+int nwg_score_block(nwg_ctx* ctx, const int8_t* xcodes, const int64_t* xoffsets, int nx,
+                    const int8_t* ycodes, const int64_t* yoffsets, int ny,
+                    float* D, int64_t ld, int64_t r0, int mode, nwg_stats* stats);
+
+/* Score an explicit pair list (pi[k], pj[k]) -> out[k]; host buffers. */
+int nwg_score_pairs(nwg_ctx* ctx, const int8_t* codes, const int64_t* offsets, int n,
+                    const int32_t* pi, const int32_t* pj, int64_t npairs, int32_t* out,
+                    nwg_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,70 @@
+// nwg_ctx.h -- the context behind the opaque nwg_ctx handle (not installed).
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "nwg_internal.h"
+
+namespace nwg {
+
+// Grow-only device buffer owned by a context.
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  int ensure(size_t bytes);
+  void release();
+};
+
+// One sequence set as the kernels see it: sorted by length (descending).
+struct SetView {
+  int n = 0;
+  int maxlen = 0;
+  std::vector<int32_t> len, orig, bound;
+  std::vector<int64_t> start;
+  const int8_t* d_codes = nullptr;
+  const int64_t* d_start = nullptr;
+  const int32_t* d_len = nullptr;
+  const int32_t* d_orig = nullptr;
+};
+
+const int8_t* builtin_matrix();
+const char* letter_order();
+int choose_rows_per_lane(int rows, const int* table);
+
+struct Ctx {
+  int go = 10, ge = 2;
+  int8_t sub[kLetters * kLetters];
+  int device = 0, sms = 1;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::string last_err;
+  int launches = 0;
+  const int* tune_table = nullptr;   // rows-per-lane per length class (6 entries) or null
+  int tune_storage[6] = {4, 8, 12, 16, 24, 24};
+
+  DevBuf b_codes, b_start, b_len, b_orig, b_bound, b_bad;
+  DevBuf b_start2, b_len2, b_orig2;
+  DevBuf b_gy, b_gy2, b_gx, b_jobs, b_counter, b_wscratch, b_pscratch, b_yprefix;
+  DevBuf b_D, b_sub, b_rowmax;
+  DevBuf b_pi, b_pj, b_out;
+  // traceback / neighbor joining state (trace.cu, nj.cu)
+  void* trace_state = nullptr;
+  void* nj_state = nullptr;
+  void extra_release();
+
+  ~Ctx();
+  int fail(int status, const char* what, cudaError_t e = cudaSuccess);
+  int cuda(cudaError_t e, const char* what);
+  int prepare_set(const int8_t* d_codes, const int64_t* offsets, int n, SetView& v, DevBuf& bstart,
+                  DevBuf& blen, DevBuf& borig, bool want_bounds);
+  int run_batched(const SetView& X, const SetView& Y, bool triangle, float* d_D, int64_t ld,
+                  int64_t col0, bool force32, nwg_stats* st);
+  int run_plain(const SetView& X, const SetView& Y, bool triangle, float* d_D, int64_t ld,
+                int64_t col0, nwg_stats* st);
+  int score_all_dev(const int8_t* d_codes, const int64_t* offsets, int n, float* d_D, int64_t ld,
+                    int mode, nwg_stats* st);
+};
+
+}  // namespace nwg

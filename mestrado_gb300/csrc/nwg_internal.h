@@ -1,0 +1,111 @@
+// nwg_internal.h -- shared declarations of libnwgpu (not installed).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/nwgpu.h"
+
+namespace nwg {
+
+constexpr int kLetters = 24;              // alphabet of AlignmentScore.cu:10-27
+constexpr int kShortMin = -32768;         // SHORT_MIN of NeedlemanWunsch.cu:12
+constexpr int kWaveWarps = 8;             // warps per CTA of the wavefront kernels
+constexpr int kWaveThreads = 32 * kWaveWarps;
+constexpr int kPlainThreads = 128;
+constexpr int kPlainRows = 16;            // rows per thread strip in the plain kernel
+constexpr int kInt16MaxLen = 8000;        // int16 lanes: |H| lower bound 4*L+16 < 32768
+
+// Per-sequence upper bound of any H value of a pair containing it:
+// sum over its residues of the best score of that residue's matrix row.
+// A pair goes to int16 lanes only when min(bound_x, bound_y) <= kInt16MaxH
+// and both lengths <= kInt16MaxLen (see DESIGN: overflow guard).
+constexpr int kInt16MaxH = 32767 - 16;
+
+// Sequence set laid out on the device for one call: sorted by length
+// (descending), each start 16-byte aligned.
+struct DevSet {
+  int n = 0;
+  std::vector<int32_t> h_len;     // sorted lengths
+  std::vector<int32_t> h_orig;    // sorted -> original index
+  std::vector<int64_t> h_start;   // sorted -> start in d_codes
+  std::vector<int32_t> h_bound;   // sorted -> H upper bound
+  int8_t* d_codes = nullptr;      // aligned, packed codes (owned by ctx arena)
+  int64_t* d_start = nullptr;
+  int32_t* d_len = nullptr;
+  int32_t* d_orig = nullptr;
+  int64_t bytes = 0;
+};
+
+struct WaveArgs {
+  const int8_t* codes;
+  const int64_t* xstart;
+  const int32_t* xlen;
+  const int32_t* xorig;
+  const int64_t* ystart;
+  const int32_t* ylen;
+  const int32_t* yorig;
+  const int32_t* group_y;     // per Y group: first Y (sorted index)
+  const int32_t* group_y2;    // per Y group: second Y for int16x2 lanes, or -1
+  const int32_t* group_x;     // per Y group: number of X rows (triangle: up to the group's last Y)
+  const int64_t* job_prefix;  // per Y group of this bucket: first CTA job; ngroups+1 entries
+  unsigned long long* counter;
+  float* D;
+  int32_t* scratch;           // per warp: 2 buffers x 2 words x scratch_cols
+  int64_t ld;
+  int64_t col0;
+  int64_t njobs;
+  int nx, ny;
+  int g_begin, ngroups;
+  int triangle;
+  int go, ge;
+  int scratch_cols;
+  const int8_t* sub;          // 24*24 on device
+};
+
+struct PlainArgs {
+  const int8_t* codes;
+  const int64_t* xstart;
+  const int32_t* xlen;
+  const int32_t* xorig;
+  const int64_t* ystart;
+  const int32_t* ylen;
+  const int32_t* yorig;
+  const int64_t* y_prefix;    // per Y in this launch: first thread; ny_launch+1 entries
+  int2* scratch;              // [column][thread]
+  float* D;
+  int64_t ld;
+  int64_t col0;
+  int64_t nthreads;
+  int y_begin, ny_launch;
+  int triangle;
+  int go, ge;
+  const int8_t* sub;
+};
+
+struct PairListArgs {
+  const int8_t* codes;
+  const int64_t* start;
+  const int32_t* len;
+  const int32_t* pi;
+  const int32_t* pj;
+  int32_t* out;
+  int2* scratch;              // [column][thread]
+  int64_t npairs;
+  int64_t base;               // first pair of this launch
+  int go, ge;
+  const int8_t* sub;
+};
+
+// Launchers (score_kernels.cu).  R is the rows per lane; P = 2 for int16x2
+// lanes (two pairs per warp), 1 for int32 lanes.
+cudaError_t launch_wave(int R, int P, const WaveArgs& a, int grid, cudaStream_t s);
+int wave_max_ctas_per_sm(int R, int P);
+size_t wave_smem_bytes(int R);
+cudaError_t launch_plain(const PlainArgs& a, cudaStream_t s);
+cudaError_t launch_pairlist(const PairListArgs& a, int64_t count, cudaStream_t s);
+
+}  // namespace nwg

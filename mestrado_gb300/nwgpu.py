@@ -1,0 +1,201 @@
+"""Python host side of libnwgpu: contexts and the reference's AlignmentScore.
+
+Every compute call goes through the C ABI (include/nwgpu.h).  Arrays are
+numpy on the host; the ``*_dev`` forms take raw device pointers (for example
+``torch.Tensor.data_ptr()``) and optionally a CUDA stream handle.
+"""
+from __future__ import annotations
+
+import ctypes
+import struct
+
+import numpy as np
+
+from ._native import (MODE_BATCHED, MODE_BATCHED_INT32, MODE_PLAIN, NWGError, Stats, c_f32p,
+                      c_i8p, c_i32p, c_i64p, check, lib)
+
+__all__ = ["Context", "AlignmentScore", "encode", "make_wire", "parse_wire"]
+
+
+def _p(a: np.ndarray, ct):
+    return a.ctypes.data_as(ct)
+
+
+def _as_seq_list(seqs):
+    if hasattr(seqs, "residues") and hasattr(seqs, "offsets"):
+        return seqs.residues, np.asarray(seqs.offsets, dtype=np.int64)
+    parts = [s.encode() if isinstance(s, str) else bytes(s) for s in seqs]
+    off = np.zeros(len(parts) + 1, dtype=np.int64)
+    np.cumsum([len(p) for p in parts], out=off[1:])
+    return b"".join(parts), off
+
+
+def encode(seqs):
+    """Reversed 8-bit codes + offsets for ASCII sequences (AlignmentScore.cu:142-178)."""
+    res, off = _as_seq_list(seqs)
+    codes = np.zeros(max(int(off[-1]), 1), dtype=np.int8)
+    st = lib().nwg_encode(res, _p(off, c_i64p), len(off) - 1, _p(codes, c_i8p))
+    check(st)
+    return codes, off
+
+
+def make_wire(seqs, rank: int = 0) -> bytes:
+    """The sequence block rank 0 sends in SpeciesBlock.cpp:309-322:
+    [int rank][{int seqNo, int len, char[len], '\\0'} x n]."""
+    res, off = _as_seq_list(seqs)
+    out = [struct.pack("<i", rank)]
+    for k in range(len(off) - 1):
+        s = res[off[k]:off[k + 1]]
+        out.append(struct.pack("<ii", k, len(s)) + s + b"\0")
+    return b"".join(out)
+
+
+def parse_wire(buf: bytes, n: int):
+    """Decode a wire block into reversed codes + offsets (AlignmentScore::parse)."""
+    off = np.zeros(n + 1, dtype=np.int64)
+    check(lib().nwg_parse_wire(buf, n, None, _p(off, c_i64p)))
+    codes = np.zeros(max(int(off[-1]), 1), dtype=np.int8)
+    check(lib().nwg_parse_wire(buf, n, _p(codes, c_i8p), _p(off, c_i64p)))
+    return codes, off
+
+
+class Context:
+    """One libnwgpu context: gap penalties, substitution matrix, CUDA stream."""
+
+    def __init__(self, gap_open: int = 10, gap_ext: int = 2, sub=None):
+        self._lib = lib()
+        h = ctypes.c_void_p()
+        subp = None
+        if sub is not None:
+            self._sub = np.ascontiguousarray(sub, dtype=np.int8).reshape(576)
+            subp = _p(self._sub, c_i8p)
+        check(self._lib.nwg_ctx_create(gap_open, gap_ext, subp, ctypes.byref(h)))
+        self.h = h
+        self.gap_open, self.gap_ext = gap_open, gap_ext
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.nwg_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, st):
+        check(st, self.h)
+
+    def set_stream(self, stream_handle: int | None):
+        self._check(self._lib.nwg_set_stream(self.h, ctypes.c_void_p(stream_handle or 0)))
+
+    # ---- scoring ---------------------------------------------------------
+    def score_all(self, seqs=None, *, codes=None, offsets=None, mode: int = MODE_BATCHED,
+                  out: np.ndarray | None = None, stats: bool = False):
+        """Full n x n distance matrix (float32) of ASCII ``seqs`` or of
+        pre-encoded ``codes``/``offsets``.  Host buffers in and out."""
+        if codes is None:
+            codes, offsets = encode(seqs)
+        codes = np.ascontiguousarray(codes, dtype=np.int8)
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        n = len(offsets) - 1
+        D = out if out is not None else np.empty((n, n), dtype=np.float32)
+        st = Stats()
+        self._check(self._lib.nwg_score_all(self.h, _p(codes, c_i8p), _p(offsets, c_i64p), n,
+                                            _p(D, c_f32p), D.strides[0] // 4, mode, ctypes.byref(st)))
+        return (D, st.as_dict()) if stats else D
+
+    def score_all_dev(self, d_codes: int, offsets: np.ndarray, d_D: int, ld: int,
+                      mode: int = MODE_BATCHED, stats: bool = False):
+        """Device-resident form: ``d_codes``/``d_D`` are device pointers."""
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        st = Stats()
+        self._check(self._lib.nwg_score_all_dev(self.h, ctypes.c_void_p(d_codes), _p(offsets, c_i64p),
+                                                len(offsets) - 1, ctypes.c_void_p(d_D), ld, mode,
+                                                ctypes.byref(st) if stats else None))
+        return st.as_dict() if stats else None
+
+    def score_block(self, xseqs=None, yseqs=None, *, D=None, r0: int = 0, mode: int = MODE_BATCHED,
+                    xcodes=None, xoffsets=None, ycodes=None, yoffsets=None, stats: bool = False):
+        """D[x][r0 + y] = score(X_x, Y_y): the computeDistanceMtx block shape."""
+        if xcodes is None:
+            xcodes, xoffsets = encode(xseqs)
+        if ycodes is None:
+            ycodes, yoffsets = encode(yseqs)
+        nx, ny = len(xoffsets) - 1, len(yoffsets) - 1
+        if D is None:
+            D = np.zeros((nx, r0 + ny), dtype=np.float32)
+        xoffsets = np.ascontiguousarray(xoffsets, dtype=np.int64)
+        yoffsets = np.ascontiguousarray(yoffsets, dtype=np.int64)
+        st = Stats()
+        self._check(self._lib.nwg_score_block(self.h, _p(xcodes, c_i8p), _p(xoffsets, c_i64p), nx,
+                                              _p(ycodes, c_i8p), _p(yoffsets, c_i64p), ny, _p(D, c_f32p),
+                                              D.strides[0] // 4, r0, mode, ctypes.byref(st)))
+        return (D, st.as_dict()) if stats else D
+
+    def score_pairs(self, codes, offsets, pi, pj):
+        """Scores of explicit pairs (int32 lanes, one thread per pair)."""
+        pi = np.ascontiguousarray(pi, dtype=np.int32)
+        pj = np.ascontiguousarray(pj, dtype=np.int32)
+        out = np.zeros(len(pi), dtype=np.int32)
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        self._check(self._lib.nwg_score_pairs(self.h, _p(codes, c_i8p), _p(offsets, c_i64p),
+                                              len(offsets) - 1, _p(pi, c_i32p), _p(pj, c_i32p), len(pi),
+                                              _p(out, c_i32p), None))
+        return out
+
+
+class AlignmentScore:
+    """The reference class AlignmentScore (AlignmentScore.cuh:10-38) on libnwgpu.
+
+    ``AlignmentScore(10, 2, 16, maxSeqLen)`` then ``loadDB(lbuf, lSz)`` and
+    ``computeDistanceMtx(rbuf, rSz, distances, r0)`` as SpeciesBlock.cpp:361-363
+    calls them.  ``distances`` is an (lSz x N) float32 array (or a list of
+    per-row lists, as the C++ vector<vector<float>>); row x, column r0+y gets
+    score(X_x, Y_y).  The window size is accepted and ignored: the GPU path
+    has no windows.  Errors raise NWGError instead of exiting.
+    """
+
+    def __init__(self, gapOpen: int, gapExt: int, wSize: int, maxSeqLen: int):
+        self.ctx = Context(gapOpen, gapExt)
+        self.windowSize = wSize
+        self.maxSeqLength = maxSeqLen
+        self.xSize = 0
+        self._x = None
+        self._xbuf = None
+
+    def parse(self, input: bytes, size: int):
+        """Returns (codes, starts, lengths) -- AlignmentScore::parse's outputs."""
+        codes, off = parse_wire(input, size)
+        return codes, off[:-1].copy(), np.diff(off)
+
+    def loadDB(self, lbuf: bytes, lSz: int):
+        self.xSize = lSz
+        self._xbuf = bytes(lbuf)
+        self._x = parse_wire(lbuf, lSz)
+
+    def computeDistanceMtx(self, rbuf: bytes, rSz: int, distances, r0: int):
+        if self._x is None:
+            raise NWGError(6, "loadDB must come first")
+        ycodes, yoff = parse_wire(rbuf, rSz)
+        xcodes, xoff = self._x
+        as_list = not isinstance(distances, np.ndarray)
+        same = (bytes(rbuf) == self._xbuf and rSz == self.xSize)
+        if same:
+            # the square, symmetric block of one rank: all pairs once
+            D = self.ctx.score_all(codes=xcodes, offsets=xoff)
+            block = D
+        else:
+            block = self.ctx.score_block(xcodes=xcodes, xoffsets=xoff, ycodes=ycodes, yoffsets=yoff)
+        if as_list:
+            for x in range(self.xSize):
+                distances[x][r0:r0 + rSz] = block[x, :rSz].tolist()
+        else:
+            distances[:self.xSize, r0:r0 + rSz] = block[:, :rSz]

@@ -1,0 +1,128 @@
+"""Parity of the sm_103a scoring kernels with the oracle (bit-exact: integer
+scores stored as float32).  Every call goes through the C ABI."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle_py as O
+from mestrado_gb300 import (MODE_BATCHED, MODE_BATCHED_INT32, MODE_PLAIN, AlignmentScore, NWGError,
+                            encode, make_wire, synth)
+from mestrado_gb300 import _native
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+MODES = [MODE_BATCHED, MODE_PLAIN, MODE_BATCHED_INT32]
+
+
+def _rand_set(seed, n, lo, hi, alphabet=b"ARNDCQEGHILKMFPSTWYV"):
+    rng = np.random.default_rng(seed)
+    letters = np.frombuffer(alphabet, dtype=np.uint8)
+    lens = rng.integers(lo, hi + 1, size=n)
+    return [letters[rng.integers(0, len(letters), L)].tobytes() for L in lens]
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_cfg0_matrix_equals_golden(ctx, mode):
+    D0 = np.load(os.path.join(GOLD, "cfg0", "D.npy"))
+    S = synth.config(0)
+    D, st = ctx.score_all(S, mode=mode, stats=True)
+    assert np.array_equal(D, D0)
+    assert st["pairs"] == 64 * 65 // 2
+    assert st["cells"] == S.cells()
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("seed,n,lo,hi", [(1, 40, 1, 60), (2, 33, 100, 420), (3, 21, 300, 900),
+                                          (4, 12, 700, 2100)])
+def test_random_lengths_match_oracle(ctx, mode, seed, n, lo, hi):
+    seqs = _rand_set(seed, n, lo, hi)
+    D = ctx.score_all(seqs, mode=mode)
+    assert np.array_equal(D, O.score_all(seqs, threads=os.cpu_count()))
+
+
+def test_full_alphabet_and_identical_and_single_residue(ctx):
+    seqs = _rand_set(7, 10, 1, 50, alphabet=b"ARNDCQEGHILKMFPSTWYVBZX*")
+    seqs += [b"A", b"W", seqs[3], seqs[3], b"*"]
+    Dref = O.score_all(seqs)
+    for mode in MODES:
+        assert np.array_equal(ctx.score_all(seqs, mode=mode), Dref)
+
+
+def test_one_and_two_sequences(ctx):
+    for seqs in ([b"MKV"], [b"MKV", b"MKVL"]):
+        assert np.array_equal(ctx.score_all(seqs), O.score_all(seqs))
+
+
+def test_overflow_guard_routes_to_int32(ctx):
+    # W scores 11 against itself: a 3200-residue W run bounds H at 35200 > int16
+    seqs = [b"W" * 3200, b"W" * 3100 + b"A" * 50, b"MKV" * 300, b"W" * 3000]
+    D, st = ctx.score_all(seqs, mode=MODE_BATCHED, stats=True)
+    assert st["pairs_int32"] > 0
+    assert np.array_equal(D, O.score_all(seqs, threads=os.cpu_count()))
+    assert D[0, 0] == 3200 * 11
+
+
+def test_block_shape_with_column_offset(ctx):
+    X = _rand_set(9, 17, 20, 400)
+    Y = _rand_set(10, 13, 5, 300)
+    for mode in MODES:
+        D = np.full((17, 40), -1.0, dtype=np.float32)
+        ctx.score_block(X, Y, D=D, r0=20, mode=mode)
+        ref = np.array([[O.score_pair(x, y) for y in Y] for x in X], dtype=np.float32)
+        assert np.array_equal(D[:, 20:33], ref)
+        assert (D[:, :20] == -1).all() and (D[:, 33:] == -1).all()
+
+
+def test_pair_list(ctx):
+    seqs = _rand_set(11, 30, 1, 500)
+    codes, off = encode(seqs)
+    rng = np.random.default_rng(0)
+    pi, pj = rng.integers(0, 30, 200), rng.integers(0, 30, 200)
+    out = ctx.score_pairs(codes, off, pi, pj)
+    ref = O.score_list(codes, off, pi, pj)
+    assert np.array_equal(out, ref)
+
+
+def test_reference_class_mirror(ctx):
+    S = synth.family(40, 200, seed=21)
+    wire = make_wire(S)
+    al = AlignmentScore(10, 2, 16, int(S.lengths.max()))
+    al.loadDB(wire, len(S))
+    D = [[0.0] * len(S) for _ in range(len(S))]
+    al.computeDistanceMtx(wire, len(S), D, 0)
+    assert np.array_equal(np.array(D, dtype=np.float32), O.score_all(S))
+    # a second block at a column offset (two-rank ring step shape)
+    half = S.subset(range(20))
+    other = S.subset(range(20, 40))
+    al2 = AlignmentScore(10, 2, 16, 400)
+    al2.loadDB(make_wire(half), 20)
+    D2 = np.zeros((20, 40), dtype=np.float32)
+    al2.computeDistanceMtx(make_wire(other, rank=1), 20, D2, 20)
+    assert np.array_equal(D2[:, 20:], O.score_all(S)[:20, 20:])
+
+
+def test_errors_are_status_codes(ctx):
+    with pytest.raises(NWGError) as e:
+        ctx.score_all(codes=np.array([0, 1, 30], dtype=np.int8), offsets=np.array([0, 3], dtype=np.int64))
+    assert e.value.status == _native.NWG_ERR_BAD_RESIDUE
+    with pytest.raises(NWGError) as e:
+        ctx.score_all(codes=np.array([0, 1], dtype=np.int8), offsets=np.array([0, 2, 2], dtype=np.int64))
+    assert e.value.status == _native.NWG_ERR_EMPTY_SEQ
+
+
+def test_config1_full_size_properties_and_sample(ctx):
+    S = synth.config(1)
+    n = len(S)
+    codes, off = encode(S)
+    Db, st = ctx.score_all(codes=codes, offsets=off, mode=MODE_BATCHED, stats=True)
+    assert st["pairs"] == n * (n + 1) // 2
+    assert np.array_equal(Db, Db.T)
+    Dp = ctx.score_all(codes=codes, offsets=off, mode=MODE_PLAIN)
+    assert np.array_equal(Db, Dp)
+    rng = np.random.default_rng(1)
+    pi, pj = rng.integers(0, n, 3000), rng.integers(0, n, 3000)
+    ref = O.score_list(codes, off, pi, pj, threads=os.cpu_count())
+    assert np.array_equal(Db[pi, pj], ref.astype(np.float32))
+    diag = O.score_list(codes, off, np.arange(0, n, 37), np.arange(0, n, 37), threads=os.cpu_count())
+    assert np.array_equal(np.diag(Db)[::37], diag.astype(np.float32))
