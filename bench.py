@@ -1,0 +1,397 @@
+"""Benchmark: all-pairs Needleman-Wunsch distance matrix on one GB300.
+
+Workload (default): benchmark configuration 2 -- 10,000 synthetic protein
+sequences in 50 families of 200, lognormal root lengths (median 350, sigma
+0.6, clipped 30-4000), ~5e7 pairs, scored by the batched persistent
+length-bucketed kernels (int16x2 DPX lanes with int32 for pairs the overflow
+guard routes there).  One step = the full 10,000 x 10,000 distance matrix.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  value = GCUPS (sum over i<j of L_i*L_j per
+second) with codes and matrix resident in HBM; e2e = the same metric through
+the host-buffer C ABI call (nwg_score_all: codes host->device, matrix
+device->host inside the timed region).  --impl reference times the
+reference's recurrence restated on the CPU (its CUDA does not build on CUDA
+13) on every host core, on a bounded sample of the same pairs.
+
+Multi-GPU (torchrun, N>1): every rank scores its own replica of the workload
+(families drawn with a rank-dependent seed); no data-path collective; the
+result is weak scaling, value = all ranks' cells / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIG = 2
+METRIC = "nw_gcups_batched"
+UNIT = "GCUPS"
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+    return world, rank, local
+
+
+def _barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def _max_over_ranks(world, v: float) -> float:
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _sum_over_ranks(world, v: float) -> float:
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm), "power_w_max": float(max(power)) if power else None}
+
+
+def cpu_baseline(S, target_s: float, threads: int, seed: int = 7):
+    """Oracle (the reference's recurrence restated in C, OpenMP over pairs) on a
+    seeded random sample of the workload's pairs sized to ~target_s seconds."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_py as O
+    O.build()
+    codes, off = O.encode(S)
+    n = len(S)
+    rng = np.random.default_rng(seed)
+    L = S.lengths.astype(np.float64)
+
+    def sample(k):
+        i = rng.integers(0, n, k)
+        j = rng.integers(0, n, k)
+        m = i != j
+        return i[m].astype(np.int32), j[m].astype(np.int32)
+
+    pi, pj = sample(64 * threads)
+    t0 = time.perf_counter()
+    O.score_list(codes, off, pi, pj, threads=threads)
+    dt = max(time.perf_counter() - t0, 1e-3)
+    rate = float((L[pi] * L[pj]).sum()) / dt
+    want_cells = rate * target_s
+    mean_cells = float((L[pi] * L[pj]).mean())
+    k = int(max(64, want_cells / mean_cells))
+    pi, pj = sample(k)
+    cells = float((L[pi] * L[pj]).sum())
+    t0 = time.perf_counter()
+    O.score_list(codes, off, pi, pj, threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": cells / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{len(pi)} seeded random pairs of configuration {CONFIG} ({cells:.3g} cells, "
+                      f"{dt:.1f} s), GCUPS = cells / time"}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    from mestrado_gb300 import synth
+    S = synth.config(CONFIG)
+    threads = os.cpu_count() or 1
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_py as O
+    O.build()
+    codes, off = O.encode(S)
+    n = len(S)
+    rng = np.random.default_rng(3)
+    L = S.lengths.astype(np.float64)
+    # size one step to ~4 s on this host
+    pi = rng.integers(0, n, 32 * threads).astype(np.int32)
+    pj = rng.integers(0, n, 32 * threads).astype(np.int32)
+    t0 = time.perf_counter()
+    O.score_list(codes, off, pi, pj, threads=threads)
+    rate = float((L[pi] * L[pj]).sum()) / max(time.perf_counter() - t0, 1e-3)
+    k = int(max(64, rate * 4.0 / float((L[pi] * L[pj]).mean())))
+    pi = rng.integers(0, n, k).astype(np.int32)
+    pj = rng.integers(0, n, k).astype(np.int32)
+    cells = float((L[pi] * L[pj]).sum())
+    for _ in range(args.warmup):
+        O.score_list(codes, off, pi[: max(1, k // 8)], pj[: max(1, k // 8)], threads=threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.score_list(codes, off, pi, pj, threads=threads)
+        times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    v = cells * args.steps / tot / 1e9
+    line = {
+        "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": tot / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": f"configuration {CONFIG}: 10000 seqs, 50 families x 200, lognormal "
+                               "lengths (median 350, sigma 0.6, 30-4000)",
+                   "sample_pairs": int(k), "l2": "host run"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{k} seeded random pairs per step ({cells:.3g} cells); the reference's "
+                                   "recurrence (NeedlemanWunsch.cu:22-161) restated in C, OpenMP over pairs; "
+                                   "its own CUDA kernel does not build on CUDA 13"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison run")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--subset", type=int, default=0,
+                    help="score only the first N sequences (whole families first); for profiling runs")
+    ap.add_argument("--quick", action="store_true",
+                    help="device-resident timing only (no e2e, plain, CPU or parity legs); for profiling runs")
+    args = ap.parse_args()
+    world, rank, local = _dist()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    from mestrado_gb300 import MODE_BATCHED, MODE_PLAIN, Context, encode, synth
+
+    spec = synth.config_spec(CONFIG)
+    seed = synth.config_seed(CONFIG) + 1000003 * rank
+    S = synth.generate(spec, seed)
+    if args.subset:
+        S = S.subset(range(min(args.subset, len(S))))
+    n = len(S)
+    cells = S.cells()
+    codes, off = encode(S)
+    ctx = Context(10, 2)
+    # a dedicated stream: the library launches on it and the CUDA events below
+    # are recorded on it (torch's default stream has handle 0, which the C ABI
+    # reads as "use the context's own stream")
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+
+    d_codes = torch.from_numpy(codes).to("cuda")
+    d_D = torch.empty((n, n), dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 256 MB > L2
+
+    # roofline denominator: the bare DPX cell update on every SM
+    peak16 = ctx.dpx_peak(True)
+    peak32 = ctx.dpx_peak(False)
+
+    for _ in range(args.warmup):
+        ctx.score_all_dev(d_codes.data_ptr(), off, d_D.data_ptr(), n, MODE_BATCHED)
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    _barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    launches = 0
+    wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.zero_()                      # L2 flushed between timed steps
+        ev[k][0].record(stream)
+        st = ctx.score_all_dev(d_codes.data_ptr(), off, d_D.data_ptr(), n, MODE_BATCHED, stats=False)
+        ev[k][1].record(stream)
+        launches += 0 if st is None else st["launches"]
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    _barrier(world)
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    tot_s = sum(step_ms) / 1e3
+    tot_s_max = _max_over_ranks(world, tot_s)
+    all_cells = _sum_over_ranks(world, float(cells) * args.steps)
+    value = all_cells / tot_s_max / 1e9
+
+    # launches of one step and the dominant launch, timed alone (events around each launch)
+    ctx.set_launch_timing(True)
+    flush.zero_()
+    st = ctx.score_all_dev(d_codes.data_ptr(), off, d_D.data_ptr(), n, MODE_BATCHED, stats=True)
+    recs = ctx.launch_records()
+    ctx.set_launch_timing(False)
+    timed_sum_ms = sum(r["ms"] for r in recs)
+    per_step_launches = st["launches"]
+    launches = per_step_launches * args.steps
+    dom = max(recs, key=lambda r: r["ms"]) if recs else None
+
+    if args.quick:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                              "quick": True, "n": n, "cells_per_step": cells,
+                              "launch_records": recs, "peak16_gcups": peak16 / 1e9}), flush=True)
+        return
+
+    # parity spot check of this run's matrix against the oracle (small sample)
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_py as O
+    O.build()
+    rng = np.random.default_rng(17)
+    pi = rng.integers(0, n, 64)
+    pj = rng.integers(0, n, 64)
+    Dh = d_D.cpu().numpy()
+    ref = O.score_list(codes, off, pi, pj, threads=os.cpu_count() or 1)
+    parity = bool(np.array_equal(Dh[pi, pj], ref.astype(np.float32))) and bool(np.array_equal(Dh, Dh.T))
+
+    # end to end through the host-buffer C ABI call: pinned codes in, matrix out
+    h_codes = torch.from_numpy(codes).pin_memory()
+    h_D = torch.empty((n, n), dtype=torch.float32).pin_memory()
+    ctx.set_stream(None)
+    torch.cuda.synchronize()
+    e2e_times = []
+    for k in range(max(1, args.steps)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.score_all(codes=h_codes.numpy(), offsets=off, out=h_D.numpy(), mode=MODE_BATCHED)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = _max_over_ranks(world, sum(e2e_times))
+    e2e = {"value": _sum_over_ranks(world, float(cells) * len(e2e_times)) / e2e_s / 1e9, "unit": UNIT,
+           "h2d_bytes_per_step": int(codes.nbytes + off.nbytes), "d2h_bytes_per_step": int(n * n * 4)}
+    parity = parity and bool(np.array_equal(h_D.numpy(), Dh))
+    ctx.set_stream(stream.cuda_stream)
+
+    # plain form (one thread per pair, int32, launch per length group) once, for the batched/plain ratio
+    plain = None
+    if not args.no_plain:
+        flush.zero_()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ctx.score_all_dev(d_codes.data_ptr(), off, d_D.data_ptr(), n, MODE_PLAIN)
+        b.record(stream)
+        torch.cuda.synchronize()
+        pms = a.elapsed_time(b)
+        plain = {"gcups": cells / (pms / 1e3) / 1e9, "ms": pms,
+                 "matrix_equal": bool(np.array_equal(d_D.cpu().numpy(), Dh))}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(S, args.cpu_seconds, os.cpu_count() or 1)
+
+    if rank != 0:
+        return
+    roof = None
+    if dom is not None:
+        peak = peak16 if dom["lanes16"] else peak32
+        ach = dom["cells"] / (dom["ms"] / 1e3)
+        roof = {"bound": "int", "achieved": ach / 1e9, "peak": peak / 1e9, "unit": "GCUPS",
+                "frac": ach / peak, "traffic": None,
+                "kernel": f"wave_kernel<R={dom['rows_per_lane']},{'int16x2' if dom['lanes16'] else 'int32'}>",
+                "launch_ms": dom["ms"], "launch_cells": dom["cells"],
+                "peak_source": "nwg_dpx_peak: 5-instruction DPX cell update on every SM, registers only, "
+                               "measured in this run",
+                "peak_int32_gcups": peak32 / 1e9}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": tot_s_max / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int16x2+int32", "data": "synthetic",
+        "config": {"workload": f"configuration {CONFIG}: {n} seqs, 50 families x 200, lognormal lengths "
+                               "(median 350, sigma 0.6, clipped 30-4000), all pairs incl. diagonal",
+                   "pairs": n * (n + 1) // 2, "cells_per_step": cells, "l2": "flushed (256 MB write) between steps",
+                   "parallelism": f"{world} replica(s)"},
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "launches_per_step": per_step_launches,
+        "launch_records": [{k: r[k] for k in ("rows_per_lane", "lanes16", "grid", "cells", "ms")} for r in recs],
+        "sequential_launch_sum_ms": timed_sum_ms,
+        "reruns": st["reruns"],
+        "plain": plain,
+        "batched_over_plain": (value / world) / plain["gcups"] if plain else None,
+        "parity_sample_ok": parity,
+        "pairs_int16": st["pairs_int16"], "pairs_int32": st["pairs_int32"],
+        "wall_s": wall,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

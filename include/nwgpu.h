@@ -47,6 +47,7 @@ typedef struct {
   int64_t cells;        /* sum over i<j of L_i*L_j: the GCUPS work unit              */
   int64_t pairs_int16;  /* pairs that ran on int16x2 lanes                           */
   int64_t pairs_int32;  /* pairs that ran on int32 lanes                             */
+  int64_t reruns;       /* int16 pairs re-run on int32 lanes by the overflow guard   */
   int32_t launches;     /* kernels launched by the call                              */
   int32_t buckets;      /* length buckets                                            */
   double kernel_ms;     /* device time of the scoring launches (events on the stream)*/
@@ -111,6 +112,35 @@ int nwg_score_block(nwg_ctx* ctx, const int8_t* xcodes, const int64_t* xoffsets,
 int nwg_score_pairs(nwg_ctx* ctx, const int8_t* codes, const int64_t* offsets, int n,
                     const int32_t* pi, const int32_t* pj, int64_t npairs, int32_t* out,
                     nwg_stats* stats);
+
+/* ---- measurement ---------------------------------------------------------
+ * Not part of the reference's interface (the reference times nothing on the
+ * device; timer.h falls back to clock()).  These give the bench its roofline
+ * denominator and per-launch device times. */
+
+/* Peak of the cell update alone: every SM runs the 5-instruction DPX cell
+ * update (viaddmax x3, vimax3, one add) on register-resident strips, no
+ * memory, no shuffles.  lanes16 != 0: int16x2 words (2 cells per word), else
+ * int32.  Returns cells per second. */
+int nwg_dpx_peak(nwg_ctx* ctx, int lanes16, double* cells_per_s);
+
+typedef struct {
+  int32_t kind;         /* 0 wave (batched), 1 plain, 2 pair list, 3 other    */
+  int32_t rows_per_lane;/* R of the wave kernel                                */
+  int32_t lanes16;      /* 1: int16x2 lanes, 0: int32                          */
+  int32_t grid;         /* CTAs launched                                       */
+  int64_t pairs;        /* pairs (i<j) this launch computes                    */
+  int64_t cells;        /* their L_i*L_j sum                                   */
+  double ms;            /* device time (events around this launch alone)       */
+} nwg_launch_rec;
+
+/* Per-launch event timing for the next calls (0 = off, the default: timing
+ * inserts events between launches). */
+int nwg_set_launch_timing(nwg_ctx* ctx, int on);
+
+/* Records of the launches of the last scoring call; returns how many exist
+ * (copies at most cap). */
+int nwg_launch_records(nwg_ctx* ctx, nwg_launch_rec* out, int cap);
 
 #ifdef __cplusplus
 }

@@ -41,6 +41,7 @@ class Stats(ctypes.Structure):
         ("cells", ctypes.c_int64),
         ("pairs_int16", ctypes.c_int64),
         ("pairs_int32", ctypes.c_int64),
+        ("reruns", ctypes.c_int64),
         ("launches", ctypes.c_int32),
         ("buckets", ctypes.c_int32),
         ("kernel_ms", ctypes.c_double),
@@ -101,7 +102,26 @@ def lib():
     return _lib
 
 
-EXTRA_SIGS: dict = {}
+class LaunchRec(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int32),
+        ("rows_per_lane", ctypes.c_int32),
+        ("lanes16", ctypes.c_int32),
+        ("grid", ctypes.c_int32),
+        ("pairs", ctypes.c_int64),
+        ("cells", ctypes.c_int64),
+        ("ms", ctypes.c_double),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+EXTRA_SIGS: dict = {
+    "nwg_dpx_peak": ([ctypes.c_void_p, ctypes.c_int, P(ctypes.c_double)], ctypes.c_int),
+    "nwg_set_launch_timing": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "nwg_launch_records": ([ctypes.c_void_p, P(LaunchRec), ctypes.c_int], ctypes.c_int),
+}
 
 
 def exported_symbols():

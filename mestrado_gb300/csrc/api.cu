@@ -53,47 +53,21 @@ double now_ms() {
   return std::chrono::duration<double, std::milli>(clk::now().time_since_epoch()).count();
 }
 
-// Per-sequence sum of row maxima: an upper bound on every H value of any pair
-// containing the sequence (each residue is aligned at most once, gaps score
-// below zero).
-__global__ void seq_bound_kernel(const int8_t* __restrict__ codes, const int64_t* __restrict__ start,
-                                 const int32_t* __restrict__ len, const int8_t* __restrict__ rowmax,
-                                 int n, int32_t* __restrict__ bound, int32_t* __restrict__ bad) {
-  const int s = blockIdx.x;
-  if (s >= n) return;
-  const int8_t* p = codes + start[s];
-  const int L = len[s];
-  int acc = 0, nbad = 0;
-  for (int k = threadIdx.x; k < L; k += blockDim.x) {
-    const int c = p[k];
-    if (c < 0 || c >= kLetters) ++nbad;
-    else acc += rowmax[c];
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    acc += __shfl_down_sync(0xffffffffu, acc, o);
-    nbad += __shfl_down_sync(0xffffffffu, nbad, o);
-  }
-  __shared__ int wa[32], wb[32];
-  if ((threadIdx.x & 31) == 0) { wa[threadIdx.x >> 5] = acc; wb[threadIdx.x >> 5] = nbad; }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int A = 0, B = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { A += wa[w]; B += wb[w]; }
-    bound[s] = A;
-    if (B) atomicAdd(bad, B);
-  }
-}
-
 }  // namespace
 
 // ---- context ---------------------------------------------------------------
 
 Ctx::~Ctx() {
+  destroy_plans(this);
+  for (cudaStream_t b : branch) cudaStreamDestroy(b);
+  for (cudaEvent_t e : join_ev) cudaEventDestroy(e);
+  if (fork_ev) cudaEventDestroy(fork_ev);
   for (DevBuf* b : {&b_codes, &b_start, &b_len, &b_orig, &b_bound, &b_bad, &b_start2, &b_len2,
                     &b_orig2, &b_gy, &b_gy2, &b_gx, &b_jobs, &b_counter, &b_wscratch, &b_pscratch,
                     &b_yprefix, &b_D, &b_sub, &b_rowmax, &b_pi, &b_pj, &b_out})
     b->release();
   extra_release();
+  for (cudaEvent_t e : evpool) cudaEventDestroy(e);
   if (ev0) cudaEventDestroy(ev0);
   if (ev1) cudaEventDestroy(ev1);
   if (own_stream) cudaStreamDestroy(own_stream);
@@ -170,22 +144,7 @@ int Ctx::prepare_set(const int8_t* d_codes, const int64_t* offsets, int n, SetVi
   v.d_len = (int32_t*)blen.p;
   v.d_orig = (int32_t*)borig.p;
   v.bound.assign(n, 0);
-  if (want_bounds) {
-    if ((rc = b_bound.ensure(sizeof(int32_t) * n)) || (rc = b_bad.ensure(sizeof(int32_t))))
-      return fail(rc, "bound allocation");
-    if ((rc = cuda(cudaMemsetAsync(b_bad.p, 0, sizeof(int32_t), stream), "bound")))
-      return rc;
-    seq_bound_kernel<<<n, 128, 0, stream>>>(d_codes, v.d_start, v.d_len, (const int8_t*)b_rowmax.p, n,
-                                             (int32_t*)b_bound.p, (int32_t*)b_bad.p);
-    ++launches;
-    if ((rc = cuda(cudaGetLastError(), "bound kernel"))) return rc;
-    int32_t bad = 0;
-    if ((rc = cuda(cudaMemcpyAsync(v.bound.data(), b_bound.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, stream), "bound copy")) ||
-        (rc = cuda(cudaMemcpyAsync(&bad, b_bad.p, sizeof(int32_t), cudaMemcpyDeviceToHost, stream), "bound copy")) ||
-        (rc = cuda(cudaStreamSynchronize(stream), "bound sync")))
-      return rc;
-    if (bad) return fail(NWG_ERR_BAD_RESIDUE, "residue code outside 0..23");
-  }
+  (void)want_bounds;
   return NWG_OK;
 }
 
@@ -199,119 +158,6 @@ int choose_rows_per_lane(int rows, const int* table) {
 }
 
 // Build and launch the batched (wavefront) plan for X rows against Y groups.
-int Ctx::run_batched(const SetView& X, const SetView& Y, bool triangle, float* d_D, int64_t ld,
-                     int64_t col0, bool force32, nwg_stats* st) {
-  // 1. Y groups: consecutive sorted Ys pair up on int16x2 lanes when every
-  //    pair they can form is provably inside int16 (overflow guard).
-  const bool x_short = X.maxlen <= kInt16MaxLen;
-  struct Group { int y, y2, nx, R, P; };
-  std::vector<Group> groups;
-  groups.reserve((size_t)Y.n / 2 + 1);
-  auto safe = [&](int y) {
-    return !force32 && x_short && Y.len[y] <= kInt16MaxLen && Y.bound[y] <= kInt16MaxH;
-  };
-  int64_t p16 = 0, p32 = 0;
-  for (int y = 0; y < Y.n;) {
-    const int R = choose_rows_per_lane(Y.len[y], tune_table);
-    if (safe(y)) {
-      const int y2 = (y + 1 < Y.n && safe(y + 1)) ? y + 1 : -1;
-      const int last = y2 >= 0 ? y2 : y;
-      const int nx = triangle ? last + 1 : X.n;
-      groups.push_back({y, y2, nx, R, 2});
-      p16 += triangle ? (y + 1) + (y2 >= 0 ? y2 + 1 : 0) : (int64_t)X.n * (y2 >= 0 ? 2 : 1);
-      y = last + 1;
-    } else {
-      const int nx = triangle ? y + 1 : X.n;
-      groups.push_back({y, -1, nx, R, 1});
-      p32 += nx;
-      ++y;
-    }
-  }
-  // 2. buckets by (R, P), longest rows first.
-  std::stable_sort(groups.begin(), groups.end(), [](const Group& a, const Group& b) {
-    if (a.R != b.R) return a.R > b.R;
-    return a.P > b.P;
-  });
-  const int ng = (int)groups.size();
-  std::vector<int32_t> gy(ng), gy2(ng), gx(ng);
-  for (int k = 0; k < ng; ++k) { gy[k] = groups[k].y; gy2[k] = groups[k].y2; gx[k] = groups[k].nx; }
-  struct Bucket { int R, P, g0, ng; int64_t j0, njobs; int maxlx; };
-  std::vector<Bucket> buckets;
-  std::vector<int64_t> prefix;
-  prefix.reserve(ng + 16);
-  for (int k = 0; k < ng;) {
-    int e = k;
-    while (e < ng && groups[e].R == groups[k].R && groups[e].P == groups[k].P) ++e;
-    Bucket b{groups[k].R, groups[k].P, k, e - k, (int64_t)prefix.size(), 0, 0};
-    int64_t acc = 0;
-    for (int g = k; g < e; ++g) {
-      prefix.push_back(acc);
-      acc += (groups[g].nx + kWaveWarps - 1) / kWaveWarps;
-      b.maxlx = std::max(b.maxlx, X.len[0]);
-    }
-    prefix.push_back(acc);
-    b.njobs = acc;
-    buckets.push_back(b);
-    k = e;
-  }
-  int rc;
-  if ((rc = b_gy.ensure(sizeof(int32_t) * ng)) || (rc = b_gy2.ensure(sizeof(int32_t) * ng)) ||
-      (rc = b_gx.ensure(sizeof(int32_t) * ng)) || (rc = b_jobs.ensure(sizeof(int64_t) * prefix.size())) ||
-      (rc = b_counter.ensure(sizeof(unsigned long long) * (buckets.size() + 1))))
-    return fail(rc, "plan allocation");
-  if ((rc = cuda(cudaMemcpyAsync(b_gy.p, gy.data(), sizeof(int32_t) * ng, cudaMemcpyHostToDevice, stream), "plan upload")) ||
-      (rc = cuda(cudaMemcpyAsync(b_gy2.p, gy2.data(), sizeof(int32_t) * ng, cudaMemcpyHostToDevice, stream), "plan upload")) ||
-      (rc = cuda(cudaMemcpyAsync(b_gx.p, gx.data(), sizeof(int32_t) * ng, cudaMemcpyHostToDevice, stream), "plan upload")) ||
-      (rc = cuda(cudaMemcpyAsync(b_jobs.p, prefix.data(), sizeof(int64_t) * prefix.size(), cudaMemcpyHostToDevice, stream), "plan upload")) ||
-      (rc = cuda(cudaMemsetAsync(b_counter.p, 0, sizeof(unsigned long long) * (buckets.size() + 1), stream), "plan upload")))
-    return rc;
-  // 3. scratch for bands after the first (rows > 32*R)
-  int grid_max = 0;
-  size_t scratch_words = 0;
-  std::vector<int> grids(buckets.size());
-  for (size_t k = 0; k < buckets.size(); ++k) {
-    const Bucket& b = buckets[k];
-    const int occ = wave_max_ctas_per_sm(b.R, b.P);
-    grids[k] = (int)std::min<int64_t>(b.njobs, (int64_t)sms * occ);
-    grid_max = std::max(grid_max, grids[k]);
-  }
-  const int scols = std::max(X.maxlen, 1);
-  scratch_words = (size_t)grid_max * kWaveWarps * 4 * (size_t)scols;
-  if ((rc = b_wscratch.ensure(sizeof(int32_t) * scratch_words))) return fail(rc, "wave scratch");
-
-  WaveArgs a{};
-  a.codes = X.d_codes;
-  a.xstart = X.d_start; a.xlen = X.d_len; a.xorig = X.d_orig;
-  a.ystart = Y.d_start; a.ylen = Y.d_len; a.yorig = Y.d_orig;
-  a.group_y = (const int32_t*)b_gy.p;
-  a.group_y2 = (const int32_t*)b_gy2.p;
-  a.group_x = (const int32_t*)b_gx.p;
-  a.D = d_D; a.ld = ld; a.col0 = col0;
-  a.scratch = (int32_t*)b_wscratch.p;
-  a.scratch_cols = scols;
-  a.nx = X.n; a.ny = Y.n;
-  a.triangle = triangle ? 1 : 0;
-  a.go = go; a.ge = ge;
-  a.sub = (const int8_t*)b_sub.p;
-  for (size_t k = 0; k < buckets.size(); ++k) {
-    const Bucket& b = buckets[k];
-    if (b.njobs == 0) continue;
-    a.job_prefix = (const int64_t*)b_jobs.p + b.j0;
-    a.counter = (unsigned long long*)b_counter.p + k;
-    a.njobs = b.njobs;
-    a.g_begin = b.g0;
-    a.ngroups = b.ng;
-    if ((rc = cuda(launch_wave(b.R, b.P, a, grids[k], stream), "wave launch"))) return rc;
-    ++launches;
-  }
-  if (st) {
-    st->pairs_int16 += p16;
-    st->pairs_int32 += p32;
-    st->buckets += (int32_t)buckets.size();
-  }
-  return NWG_OK;
-}
-
 int Ctx::run_plain(const SetView& X, const SetView& Y, bool triangle, float* d_D, int64_t ld,
                    int64_t col0, nwg_stats* st) {
   // one launch per group of consecutive (similar-length) Ys, <= kMaxThreads pairs each
@@ -351,15 +197,58 @@ int Ctx::run_plain(const SetView& X, const SetView& Y, bool triangle, float* d_D
   if ((rc = b_yprefix.ensure(sizeof(int64_t) * pre.size()))) return fail(rc, "plain plan");
   if ((rc = cuda(cudaMemcpyAsync(b_yprefix.p, pre.data(), sizeof(int64_t) * pre.size(), cudaMemcpyHostToDevice, stream), "plain plan")))
     return rc;
+  std::vector<double> sx((size_t)X.n + 1, 0.0);
+  for (int i = 0; i < X.n; ++i) sx[i + 1] = sx[i] + X.len[i];
   for (const L& l : ls) {
     a.y_begin = l.y0;
     a.ny_launch = l.ny;
     a.y_prefix = (const int64_t*)b_yprefix.p + l.off;
     a.nthreads = l.threads;
+    int ri = -1;
+    if (launch_timing) {
+      nwg_launch_rec r{1, 0, 0, (int32_t)((l.threads + kPlainThreads - 1) / kPlainThreads), 0, 0, 0.0};
+      double cells = 0;
+      for (int y = l.y0; y < l.y0 + l.ny; ++y) {
+        const int cnt = triangle ? y : X.n;
+        r.pairs += cnt;
+        cells += (double)Y.len[y] * sx[cnt];
+      }
+      r.cells = (int64_t)cells;
+      if ((ri = rec_begin(r)) < 0) return fail(NWG_ERR_CUDA, "launch timing");
+    }
     if ((rc = cuda(launch_plain(a, stream), "plain launch"))) return rc;
+    if (ri >= 0 && (rc = rec_end(ri))) return rc;
     ++launches;
   }
   if (st) st->pairs_int32 += triangle ? (int64_t)Y.n * (Y.n + 1) / 2 : (int64_t)X.n * Y.n;
+  return NWG_OK;
+}
+
+int Ctx::rec_begin(const nwg_launch_rec& r) {
+  const size_t k = recs.size();
+  while (evpool.size() < 2 * (k + 1)) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return -1;
+    evpool.push_back(e);
+  }
+  recs.push_back(r);
+  if (cudaEventRecord(evpool[2 * k], stream) != cudaSuccess) return -1;
+  return (int)k;
+}
+
+int Ctx::rec_end(int idx) {
+  return cuda(cudaEventRecord(evpool[2 * (size_t)idx + 1], stream), "launch timing");
+}
+
+int Ctx::rec_finalize() {
+  for (size_t k = 0; k < recs.size(); ++k) {
+    if (recs[k].ms > 0) continue;
+    int rc;
+    if ((rc = cuda(cudaEventSynchronize(evpool[2 * k + 1]), "launch timing"))) return rc;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, evpool[2 * k], evpool[2 * k + 1]);
+    recs[k].ms = ms;
+  }
   return NWG_OK;
 }
 
@@ -368,18 +257,25 @@ int Ctx::score_all_dev(const int8_t* d_codes, const int64_t* offsets, int n, flo
   if (n < 1 || !offsets || !d_codes || !d_D || ld < n) return fail(NWG_ERR_INVALID, "score_all arguments");
   if (mode < 0 || mode > 2) return fail(NWG_ERR_INVALID, "mode");
   int rc;
-  SetView S;
-  if ((rc = prepare_set(d_codes, offsets, n, S, b_start, b_len, b_orig, true))) return rc;
   if (st) {
     double L = 0, L2 = 0;
-    for (int i = 0; i < n; ++i) { L += S.len[i]; L2 += (double)S.len[i] * S.len[i]; }
+    for (int i = 0; i < n; ++i) {
+      const double l = (double)(offsets[i + 1] - offsets[i]);
+      L += l;
+      L2 += l * l;
+    }
     st->cells += (int64_t)((L * L - L2) / 2);
     st->pairs += (int64_t)n * (n + 1) / 2;
   }
-  if (st && (rc = cuda(cudaEventRecord(ev0, stream), "event"))) return rc;
-  if (mode == NWG_MODE_PLAIN) rc = run_plain(S, S, true, d_D, ld, 0, st);
-  else rc = run_batched(S, S, true, d_D, ld, 0, mode == NWG_MODE_BATCHED_INT32, st);
-  if (rc) return rc;
+  if (mode == NWG_MODE_PLAIN) {
+    SetView S;
+    if ((rc = prepare_set(d_codes, offsets, n, S, b_start, b_len, b_orig, false))) return rc;
+    if (st && (rc = cuda(cudaEventRecord(ev0, stream), "event"))) return rc;
+    if ((rc = run_plain(S, S, true, d_D, ld, 0, st))) return rc;
+  } else {
+    if (st && (rc = cuda(cudaEventRecord(ev0, stream), "event"))) return rc;
+    if ((rc = batched(d_codes, offsets, n, offsets, n, true, d_D, ld, 0, mode, st))) return rc;
+  }
   if (st) {
     if ((rc = cuda(cudaEventRecord(ev1, stream), "event")) ||
         (rc = cuda(cudaEventSynchronize(ev1), "kernel sync")))
@@ -437,6 +333,21 @@ int nwg_ctx_create(int gap_open, int gap_ext, const int8_t* sub, nwg_ctx** out) 
     return rc;
   }
   c->stream = c->own_stream;
+  for (int k = 0; k < 2; ++k) {
+    cudaStream_t b;
+    cudaEvent_t e;
+    if ((rc = c->cuda(cudaStreamCreateWithFlags(&b, cudaStreamNonBlocking), "stream")) ||
+        (rc = c->cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event"))) {
+      delete c;
+      return rc;
+    }
+    c->branch.push_back(b);
+    c->join_ev.push_back(e);
+  }
+  if ((rc = c->cuda(cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming), "event"))) {
+    delete c;
+    return rc;
+  }
   int8_t rowmax[nwg::kLetters];
   for (int a = 0; a < nwg::kLetters; ++a) {
     int m = -128;
@@ -530,6 +441,7 @@ int nwg_score_all_dev(nwg_ctx* ctx, const int8_t* d_codes, const int64_t* offset
   const double t0 = nwg::now_ms();
   if (stats) std::memset(stats, 0, sizeof(*stats));
   c->launches = 0;
+  c->recs.clear();
   int rc = c->score_all_dev(d_codes, offsets, n, d_D, ld, mode, stats);
   if (stats) {
     stats->launches = c->launches;
@@ -545,8 +457,13 @@ int nwg_score_all(nwg_ctx* ctx, const int8_t* codes, const int64_t* offsets, int
   const double t0 = nwg::now_ms();
   if (stats) std::memset(stats, 0, sizeof(*stats));
   c->launches = 0;
+  c->recs.clear();
   const int64_t total = offsets[n];
   int rc;
+  for (int s = 0; s < n; ++s)
+    if (offsets[s + 1] <= offsets[s]) return c->fail(NWG_ERR_EMPTY_SEQ, "zero-length sequence");
+  for (int64_t k = 0; k < total; ++k)
+    if ((unsigned)codes[k] >= (unsigned)nwg::kLetters) return c->fail(NWG_ERR_BAD_RESIDUE, "residue code outside 0..23");
   if ((rc = c->b_codes.ensure((size_t)std::max<int64_t>(total, 1))) ||
       (rc = c->b_D.ensure(sizeof(float) * (size_t)n * (size_t)n)))
     return c->fail(rc, "score_all allocation");
@@ -585,6 +502,7 @@ int nwg_score_block(nwg_ctx* ctx, const int8_t* xcodes, const int64_t* xoff, int
   const double t0 = nwg::now_ms();
   if (stats) std::memset(stats, 0, sizeof(*stats));
   c->launches = 0;
+  c->recs.clear();
   const int64_t tx = xoff[nx], ty = yoff[ny];
   int rc;
   if ((rc = c->b_codes.ensure((size_t)(tx + ty))) || (rc = c->b_D.ensure(sizeof(float) * (size_t)nx * ny)))
@@ -593,24 +511,30 @@ int nwg_score_block(nwg_ctx* ctx, const int8_t* xcodes, const int64_t* xoff, int
   if ((rc = c->cuda(cudaMemcpyAsync(dc, xcodes, (size_t)tx, cudaMemcpyHostToDevice, c->stream), "upload")) ||
       (rc = c->cuda(cudaMemcpyAsync(dc + tx, ycodes, (size_t)ty, cudaMemcpyHostToDevice, c->stream), "upload")))
     return rc;
+  for (int64_t k = 0; k < tx; ++k)
+    if ((unsigned)xcodes[k] >= (unsigned)nwg::kLetters) return c->fail(NWG_ERR_BAD_RESIDUE, "residue code");
+  for (int64_t k = 0; k < ty; ++k)
+    if ((unsigned)ycodes[k] >= (unsigned)nwg::kLetters) return c->fail(NWG_ERR_BAD_RESIDUE, "residue code");
   std::vector<int64_t> yo2(ny + 1);
   for (int k = 0; k <= ny; ++k) yo2[k] = yoff[k] + tx;
-  nwg::SetView X, Y;
-  if ((rc = c->prepare_set(dc, xoff, nx, X, c->b_start, c->b_len, c->b_orig, true))) return rc;
-  std::vector<int32_t> xb = X.bound;
-  if ((rc = c->prepare_set(dc, yo2.data(), ny, Y, c->b_start2, c->b_len2, c->b_orig2, true))) return rc;
   if (stats) {
     double sx = 0, sy = 0;
-    for (int k = 0; k < nx; ++k) sx += X.len[k];
-    for (int k = 0; k < ny; ++k) sy += Y.len[k];
+    for (int k = 0; k < nx; ++k) sx += (double)(xoff[k + 1] - xoff[k]);
+    for (int k = 0; k < ny; ++k) sy += (double)(yoff[k + 1] - yoff[k]);
     stats->cells = (int64_t)(sx * sy);
     stats->pairs = (int64_t)nx * ny;
     cudaEventRecord(c->ev0, c->stream);
   }
   // block result in a dense nx x ny device matrix, then one 2D copy into D[:, r0:]
   float* dD = (float*)c->b_D.p;
-  if (mode == NWG_MODE_PLAIN) rc = c->run_plain(X, Y, false, dD, ny, 0, stats);
-  else rc = c->run_batched(X, Y, false, dD, ny, 0, mode == NWG_MODE_BATCHED_INT32, stats);
+  if (mode == NWG_MODE_PLAIN) {
+    nwg::SetView X, Y;
+    if ((rc = c->prepare_set(dc, xoff, nx, X, c->b_start, c->b_len, c->b_orig, false))) return rc;
+    if ((rc = c->prepare_set(dc, yo2.data(), ny, Y, c->b_start2, c->b_len2, c->b_orig2, false))) return rc;
+    rc = c->run_plain(X, Y, false, dD, ny, 0, stats);
+  } else {
+    rc = c->batched(dc, xoff, nx, yo2.data(), ny, false, dD, ny, 0, mode, stats);
+  }
   if (rc) return rc;
   if (stats) {
     cudaEventRecord(c->ev1, c->stream);
@@ -637,6 +561,7 @@ int nwg_score_pairs(nwg_ctx* ctx, const int8_t* codes, const int64_t* offsets, i
   const double t0 = nwg::now_ms();
   if (stats) std::memset(stats, 0, sizeof(*stats));
   c->launches = 0;
+  c->recs.clear();
   for (int64_t k = 0; k < npairs; ++k)
     if (pi[k] < 0 || pi[k] >= n || pj[k] < 0 || pj[k] >= n) return c->fail(NWG_ERR_INVALID, "pair index");
   int maxlen = 0;
@@ -693,6 +618,43 @@ int nwg_score_pairs(nwg_ctx* ctx, const int8_t* codes, const int64_t* offsets, i
     stats->total_ms = nwg::now_ms() - t0;
   }
   return NWG_OK;
+}
+
+int nwg_dpx_peak(nwg_ctx* ctx, int lanes16, double* cells_per_s) {
+  if (!ctx || !cells_per_s) return NWG_ERR_INVALID;
+  Ctx* c = reinterpret_cast<Ctx*>(ctx);
+  const int P = lanes16 ? 2 : 1;
+  const int grid = c->sms * nwg::dpx_peak_ctas_per_sm(P);
+  const int cols = 4096;
+  int rc;
+  if ((rc = c->b_out.ensure(sizeof(uint32_t) * grid))) return c->fail(rc, "dpx peak");
+  for (int rep = 0; rep < 2; ++rep) {      // first launch warms up clocks and caches
+    if ((rc = c->cuda(cudaEventRecord(c->ev0, c->stream), "event")) ||
+        (rc = c->cuda(nwg::launch_dpx_peak(P, cols, grid, (uint32_t*)c->b_out.p, c->go, c->ge, c->stream), "dpx peak")) ||
+        (rc = c->cuda(cudaEventRecord(c->ev1, c->stream), "event")) ||
+        (rc = c->cuda(cudaEventSynchronize(c->ev1), "dpx peak sync")))
+      return rc;
+  }
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  const double cells = (double)grid * 256.0 * cols * 16 * P;
+  *cells_per_s = cells / (ms * 1e-3);
+  return NWG_OK;
+}
+
+int nwg_set_launch_timing(nwg_ctx* ctx, int on) {
+  if (!ctx) return NWG_ERR_INVALID;
+  reinterpret_cast<Ctx*>(ctx)->launch_timing = on != 0;
+  return NWG_OK;
+}
+
+int nwg_launch_records(nwg_ctx* ctx, nwg_launch_rec* out, int cap) {
+  if (!ctx) return NWG_ERR_INVALID;
+  Ctx* c = reinterpret_cast<Ctx*>(ctx);
+  if (c->rec_finalize() != NWG_OK) return -NWG_ERR_CUDA;
+  const int n = (int)c->recs.size();
+  for (int k = 0; k < n && k < cap && out; ++k) out[k] = c->recs[k];
+  return n;
 }
 
 }  // extern "C"

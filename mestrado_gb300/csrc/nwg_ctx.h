@@ -32,6 +32,10 @@ const int8_t* builtin_matrix();
 const char* letter_order();
 int choose_rows_per_lane(int rows, const int* table);
 
+struct BatchPlan;
+struct Ctx;
+void destroy_plans(Ctx* c);
+
 struct Ctx {
   int go = 10, ge = 2;
   int8_t sub[kLetters * kLetters];
@@ -49,6 +53,21 @@ struct Ctx {
   DevBuf b_gy, b_gy2, b_gx, b_jobs, b_counter, b_wscratch, b_pscratch, b_yprefix;
   DevBuf b_D, b_sub, b_rowmax;
   DevBuf b_pi, b_pj, b_out;
+  // per-launch event timing (nwg_set_launch_timing)
+  bool launch_timing = false;
+  std::vector<nwg_launch_rec> recs;
+  std::vector<cudaEvent_t> evpool;
+  int rec_begin(const nwg_launch_rec& r);   // records the start event; returns record index
+  int rec_end(int idx);
+  int rec_finalize();
+  // batched-form plans (batched.cu): [0] all-pairs triangle, [1] block
+  BatchPlan* plans[2] = {nullptr, nullptr};
+  bool use_graphs = true;
+  std::vector<cudaStream_t> branch;     // parallel branches for bucket launches
+  cudaEvent_t fork_ev = nullptr;
+  std::vector<cudaEvent_t> join_ev;
+  int batched(const int8_t* d_codes, const int64_t* xoff, int nx, const int64_t* yoff, int ny, bool triangle,
+              float* d_D, int64_t ld, int64_t col0, int mode, nwg_stats* st);
   // traceback / neighbor joining state (trace.cu, nj.cu)
   void* trace_state = nullptr;
   void* nj_state = nullptr;
@@ -59,8 +78,6 @@ struct Ctx {
   int cuda(cudaError_t e, const char* what);
   int prepare_set(const int8_t* d_codes, const int64_t* offsets, int n, SetView& v, DevBuf& bstart,
                   DevBuf& blen, DevBuf& borig, bool want_bounds);
-  int run_batched(const SetView& X, const SetView& Y, bool triangle, float* d_D, int64_t ld,
-                  int64_t col0, bool force32, nwg_stats* st);
   int run_plain(const SetView& X, const SetView& Y, bool triangle, float* d_D, int64_t ld,
                 int64_t col0, nwg_stats* st);
   int score_all_dev(const int8_t* d_codes, const int64_t* offsets, int n, float* d_D, int64_t ld,

@@ -17,13 +17,18 @@ constexpr int kWaveWarps = 8;             // warps per CTA of the wavefront kern
 constexpr int kWaveThreads = 32 * kWaveWarps;
 constexpr int kPlainThreads = 128;
 constexpr int kPlainRows = 16;            // rows per thread strip in the plain kernel
-constexpr int kInt16MaxLen = 8000;        // int16 lanes: |H| lower bound 4*L+16 < 32768
-
-// Per-sequence upper bound of any H value of a pair containing it:
-// sum over its residues of the best score of that residue's matrix row.
-// A pair goes to int16 lanes only when min(bound_x, bound_y) <= kInt16MaxH
-// and both lengths <= kInt16MaxLen (see DESIGN: overflow guard).
-constexpr int kInt16MaxH = 32767 - 16;
+// Overflow guard of the int16x2 lanes (offset binary, halves in [4, 65524]):
+//  * lower side: every value of a pair is >= -4*(max(Lx, rows)+1) - 16, rows
+//    including the band padding (< 32*32 rows), so lengths <= kInt16MaxLen
+//    keep values >= -32764;
+//  * upper side: every H of a pair is <= min(bound_x, bound_y), bound = sum of
+//    the residues' best matrix scores; <= kInt16MaxH keeps values <= 32756.
+//    With the built-in matrix (best score 11) a pair whose shorter sequence
+//    has <= kCertainLen residues is always inside; longer pairs run on int16
+//    lanes optimistically, are checked against the device-side bounds and
+//    re-run on int32 lanes when the check fails.
+constexpr int kInt16MaxLen = 6900;
+constexpr int kInt16MaxH = 32756 - 11;
 
 // Sequence set laid out on the device for one call: sorted by length
 // (descending), each start 16-byte aligned.
@@ -64,6 +69,13 @@ struct WaveArgs {
   int go, ge;
   int scratch_cols;
   const int8_t* sub;          // 24*24 on device
+  // overflow guard (optimistic int16 buckets)
+  int check_bound;
+  const int32_t* xbound;      // per sorted X: composition bound
+  const int32_t* ybound;
+  int2* rerun;                // (sorted x, sorted y) pairs to re-run on int32 lanes
+  unsigned long long* rerun_count;
+  int64_t rerun_cap;
 };
 
 struct PlainArgs {
@@ -104,8 +116,12 @@ struct PairListArgs {
 // lanes (two pairs per warp), 1 for int32 lanes.
 cudaError_t launch_wave(int R, int P, const WaveArgs& a, int grid, cudaStream_t s);
 int wave_max_ctas_per_sm(int R, int P);
+void prepare_wave(int R, int P);   // sets the dynamic shared memory limit (outside graph capture)
 size_t wave_smem_bytes(int R);
 cudaError_t launch_plain(const PlainArgs& a, cudaStream_t s);
+cudaError_t launch_rerun(const WaveArgs& a, int2* scratch, int64_t nthreads, cudaStream_t s);
+cudaError_t launch_dpx_peak(int P, int cols, int grid, uint32_t* sink, int go, int ge, cudaStream_t s);
+int dpx_peak_ctas_per_sm(int P);
 cudaError_t launch_pairlist(const PairListArgs& a, int64_t count, cudaStream_t s);
 
 }  // namespace nwg

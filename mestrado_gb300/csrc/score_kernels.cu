@@ -36,28 +36,40 @@ __device__ __forceinline__ uint32_t splat16(int v) {
 template <int P>
 struct Lanes;
 
-// Two independent pairs in the halves of each 32-bit word.  Every operation
-// is a DPX instruction; the int16 bound check of the host (overflow guard)
-// guarantees no half ever leaves [-32768, 32767].
+// Two independent pairs in the halves of every 32-bit word, each half in
+// offset binary (value + 32768).  The max operations are unsigned DPX
+// (__viaddmax_u16x2 adds per half modulo 2^16, then takes the unsigned max;
+// __vimax3_u16x2), and offset-binary order is numeric order.  The two plain
+// additions of a cell (H - go, diag + S) are ordinary 32-bit adds of a word
+// holding hi*65536 + lo: with every half inside [4, 65524] no carry crosses
+// from the low half, which the host's overflow guard guarantees (values stay
+// within [-32764, 32756]).  Per word: 2 full-rate adds + 3 DPX.
 template <>
 struct Lanes<2> {
-  static __device__ __forceinline__ uint32_t splat(int v) { return splat16(v); }
-  static __device__ __forceinline__ uint32_t add(uint32_t a, uint32_t b) {
-    return __viaddmax_s16x2(a, b, 0x80008000u);
+  static constexpr uint32_t kBias = 0x80008000u;
+  static __device__ __forceinline__ uint32_t splat(int v) { return splat16(v + 32768); }
+  // word to ADD (32-bit arithmetic) that adds lo to the low half and hi to the high half
+  static __device__ __forceinline__ uint32_t arith(int lo, int hi) {
+    return (uint32_t)(hi * 65536 + lo);
   }
+  // per-half operand for addmax (modulo 2^16 in each half)
+  static __device__ __forceinline__ uint32_t packed(int v) { return splat16(v); }
+  static __device__ __forceinline__ uint32_t add(uint32_t a, uint32_t b) { return a + b; }
   static __device__ __forceinline__ uint32_t addmax(uint32_t a, uint32_t b, uint32_t c) {
-    return __viaddmax_s16x2(a, b, c);
+    return __viaddmax_u16x2(a, b, c);
   }
   static __device__ __forceinline__ uint32_t max3(uint32_t a, uint32_t b, uint32_t c) {
-    return __vimax3_s16x2(a, b, c);
+    return __vimax3_u16x2(a, b, c);
   }
-  static __device__ __forceinline__ int lo(uint32_t w) { return (int)(int16_t)(w & 0xFFFFu); }
-  static __device__ __forceinline__ int hi(uint32_t w) { return (int)(int16_t)(w >> 16); }
+  static __device__ __forceinline__ int lo(uint32_t w) { return (int)(w & 0xFFFFu) - 32768; }
+  static __device__ __forceinline__ int hi(uint32_t w) { return (int)(w >> 16) - 32768; }
 };
 
 template <>
 struct Lanes<1> {
   static __device__ __forceinline__ uint32_t splat(int v) { return (uint32_t)v; }
+  static __device__ __forceinline__ uint32_t arith(int lo, int) { return (uint32_t)lo; }
+  static __device__ __forceinline__ uint32_t packed(int v) { return (uint32_t)v; }
   static __device__ __forceinline__ uint32_t add(uint32_t a, uint32_t b) {
     return (uint32_t)((int)a + (int)b);
   }
@@ -106,8 +118,8 @@ __device__ __forceinline__ void wave_band(const WaveArgs& a, int lane, int b, in
   using L = Lanes<P>;
   constexpr int BAND = 32 * R;
   constexpr int Q = R / 4;
-  const uint32_t NGE = L::splat(-a.ge);
-  const uint32_t NGO = L::splat(-a.go);
+  const uint32_t NGE = L::packed(-a.ge);        // per-half operand of addmax
+  const uint32_t NGO = L::arith(-a.go, -a.go);   // word added to H to get H - go
   const uint32_t SENT = L::splat(kShortMin + a.ge);
 
   uint32_t H[R], T[R], E[R];
@@ -184,6 +196,18 @@ __device__ __forceinline__ void wave_band(const WaveArgs& a, int lane, int b, in
   }
 }
 
+// Optimistic int16 groups: a pair whose composition bound could exceed the
+// int16 range is not reported from the int16 lanes; it goes to the int32
+// re-run queue instead.
+__device__ __forceinline__ bool int16_safe(const WaveArgs& a, int i, int y) {
+  return !a.check_bound || min(a.xbound[i], a.ybound[y]) <= kInt16MaxH;
+}
+
+__device__ __forceinline__ void queue_rerun(const WaveArgs& a, int i, int y) {
+  const unsigned long long k = atomicAdd(a.rerun_count, 1ull);
+  if (k < (unsigned long long)a.rerun_cap) a.rerun[k] = make_int2(i, y);
+}
+
 template <int R, int P>
 __global__ void __launch_bounds__(kWaveThreads) wave_kernel(const WaveArgs a) {
   constexpr int BAND = 32 * R;
@@ -223,8 +247,22 @@ __global__ void __launch_bounds__(kWaveThreads) wave_kernel(const WaveArgs a) {
     const bool active = i < nX;
     const int Lx = active ? a.xlen[i] : 0;
     const int8_t* X = a.codes + (active ? a.xstart[i] : 0);
-    const bool wantA = active && (!a.triangle || i <= y0);
-    const bool wantB = active && has_b && (!a.triangle || i <= y1);
+    bool wantA = active && (!a.triangle || i <= y0);
+    bool wantB = active && has_b && (!a.triangle || i <= y1);
+    if (P == 2 && a.check_bound && active) {
+      // A carry out of an overflowing low half would reach the high half of
+      // the same word, so an unsafe A pair also sends B to the re-run queue.
+      const bool safeA = int16_safe(a, i, y0);
+      const bool safeB = !has_b || int16_safe(a, i, y1);
+      if (wantA && !safeA) {
+        if (lane == 0) queue_rerun(a, i, y0);
+        wantA = false;
+      }
+      if (wantB && !(safeA && safeB)) {
+        if (lane == 0) queue_rerun(a, i, y1);
+        wantB = false;
+      }
+    }
     const int rows = LyA > LyB ? LyA : LyB;
     const int nb = (rows + BAND - 1) / BAND;
     const int xo = active ? a.xorig[i] : 0;
@@ -242,7 +280,7 @@ __global__ void __launch_bounds__(kWaveThreads) wave_kernel(const WaveArgs a) {
         uint32_t w;
         if (P == 2) {
           const int sb = grow < LyB ? (int)s_sub[clamp_code(YB[grow]) * kLetters + x] : 0;
-          w = (uint32_t)(sa & 0xFFFF) | ((uint32_t)(sb & 0xFFFF) << 16);
+          w = Lanes<2>::arith(sa, sb);
         } else {
           w = (uint32_t)sa;
         }
@@ -326,6 +364,24 @@ __global__ void __launch_bounds__(kPlainThreads) plain_kernel(const PlainArgs a)
   }
 }
 
+// int32 re-run of the pairs the optimistic int16 groups queued.  The count is
+// read on the device, so the launch needs no host round trip.
+__global__ void __launch_bounds__(kPlainThreads) rerun_kernel(const WaveArgs a, int2* scratch,
+                                                               int64_t nthreads) {
+  __shared__ int8_t s_sub[kLetters * kLetters];
+  for (int e = threadIdx.x; e < kLetters * kLetters; e += blockDim.x) s_sub[e] = a.sub[e];
+  __syncthreads();
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long cnt = *a.rerun_count;
+  if (cnt > (unsigned long long)a.rerun_cap) cnt = (unsigned long long)a.rerun_cap;
+  for (int64_t k = t; k < (int64_t)cnt; k += nthreads) {
+    const int2 q = a.rerun[k];
+    const int v = score_thread(a.codes + a.xstart[q.x], a.xlen[q.x], a.codes + a.ystart[q.y], a.ylen[q.y],
+                               a.go, a.ge, s_sub, scratch + t, nthreads);
+    put_score(a, a.xorig[q.x], a.yorig[q.y], v);
+  }
+}
+
 __global__ void __launch_bounds__(kPlainThreads) pairlist_kernel(const PairListArgs a, int64_t count) {
   __shared__ int8_t s_sub[kLetters * kLetters];
   for (int e = threadIdx.x; e < kLetters * kLetters; e += blockDim.x) s_sub[e] = a.sub[e];
@@ -338,16 +394,60 @@ __global__ void __launch_bounds__(kPlainThreads) pairlist_kernel(const PairListA
                           a.ge, s_sub, a.scratch + t, count);
 }
 
+// Peak of the cell update alone (roofline denominator): the inner loop of
+// wave_band on a 16-row register strip, with the profile words and the
+// incoming boundary taken from registers -- no memory, no shuffles.
+template <int P>
+__global__ void __launch_bounds__(256) dpx_peak_kernel(uint32_t p0, uint32_t p1, uint32_t p2,
+                                                       uint32_t p3, int go, int ge, int cols,
+                                                       uint32_t* sink) {
+  using L = Lanes<P>;
+  constexpr int R = 16;
+  const uint32_t NGE = L::packed(-ge), NGO = L::arith(-go, -go);
+  uint32_t H[R], T[R], E[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    H[r] = L::splat(-ge * (r + 1 + (int)(threadIdx.x & 7)));
+    T[r] = L::add(H[r], NGO);
+    E[r] = L::splat(kShortMin + ge);
+  }
+  uint32_t hprev = 0, hin = L::splat(-ge), fin = L::splat(kShortMin + ge);
+  const uint32_t pv[4] = {p0, p1, p2, p3};
+  for (int c = 0; c < cols; ++c) {
+    uint32_t diag = hprev;
+    hprev = hin;
+    uint32_t f = fin;
+    uint32_t tup = L::add(hin, NGO);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      f = L::addmax(f, NGE, tup);
+      const uint32_t e = L::addmax(E[r], NGE, T[r]);
+      const uint32_t hd = L::add(diag, pv[r & 3]);
+      const uint32_t h = L::max3(e, f, hd);
+      diag = H[r];
+      H[r] = h;
+      E[r] = e;
+      T[r] = L::add(h, NGO);
+      tup = T[r];
+    }
+    hin = T[3];
+    fin = f;
+  }
+  uint32_t acc = 0;
+#pragma unroll
+  for (int r = 0; r < R; ++r) acc ^= H[r] ^ E[r];
+  if (acc == 0x9E3779B9u) sink[blockIdx.x] = acc;   // keeps the chain live
+}
+
+template <int R, int P>
+void prepare_one() {
+  const size_t smem = (size_t)kLetters * 32 * R * sizeof(uint32_t);
+  cudaFuncSetAttribute(wave_kernel<R, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
 template <int R, int P>
 cudaError_t launch_one(const WaveArgs& a, int grid, cudaStream_t s) {
   const size_t smem = (size_t)kLetters * 32 * R * sizeof(uint32_t);
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(wave_kernel<R, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
   wave_kernel<R, P><<<grid, kWaveThreads, smem, s>>>(a);
   return cudaGetLastError();
 }
@@ -375,6 +475,16 @@ cudaError_t launch_wave(int R, int P, const WaveArgs& a, int grid, cudaStream_t 
   return cudaErrorInvalidValue;
 }
 
+void prepare_wave(int R, int P) {
+#define NWG_CASE(r)                                 \
+  if (R == r) {                                      \
+    if (P == 2) prepare_one<r, 2>(); else prepare_one<r, 1>(); \
+    return;                                          \
+  }
+  NWG_WAVE_CASES(NWG_CASE)
+#undef NWG_CASE
+}
+
 int wave_max_ctas_per_sm(int R, int P) {
 #define NWG_CASE(r) \
   if (R == r) return P == 2 ? occupancy_one<r, 2>() : occupancy_one<r, 1>();
@@ -384,6 +494,27 @@ int wave_max_ctas_per_sm(int R, int P) {
 }
 
 size_t wave_smem_bytes(int R) { return (size_t)kLetters * 32 * R * sizeof(uint32_t); }
+
+cudaError_t launch_dpx_peak(int P, int cols, int grid, uint32_t* sink, int go, int ge, cudaStream_t s) {
+  const uint32_t p0 = 4u * 65536u + 3u, p1 = (uint32_t)(-2 * 65536 + 1), p2 = (uint32_t)(2 * 65536 - 1),
+                 p3 = 5u * 65536u;
+  if (P == 2) dpx_peak_kernel<2><<<grid, 256, 0, s>>>(p0, p1, p2, p3, go, ge, cols, sink);
+  else dpx_peak_kernel<1><<<grid, 256, 0, s>>>(p0, 1u, 0xFFFFFFFEu, 3u, go, ge, cols, sink);
+  return cudaGetLastError();
+}
+
+int dpx_peak_ctas_per_sm(int P) {
+  int n = 0;
+  if (P == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dpx_peak_kernel<2>, 256, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dpx_peak_kernel<1>, 256, 0);
+  return n > 0 ? n : 1;
+}
+
+cudaError_t launch_rerun(const WaveArgs& a, int2* scratch, int64_t nthreads, cudaStream_t s) {
+  const int64_t blocks = (nthreads + kPlainThreads - 1) / kPlainThreads;
+  rerun_kernel<<<(unsigned)blocks, kPlainThreads, 0, s>>>(a, scratch, blocks * kPlainThreads);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_plain(const PlainArgs& a, cudaStream_t s) {
   const int64_t blocks = (a.nthreads + kPlainThreads - 1) / kPlainThreads;

@@ -96,6 +96,25 @@ class Context:
     def set_stream(self, stream_handle: int | None):
         self._check(self._lib.nwg_set_stream(self.h, ctypes.c_void_p(stream_handle or 0)))
 
+    # ---- measurement -----------------------------------------------------
+    def dpx_peak(self, lanes16: bool = True) -> float:
+        """Cells/s of the bare DPX cell update on every SM (roofline)."""
+        v = ctypes.c_double()
+        self._check(self._lib.nwg_dpx_peak(self.h, 1 if lanes16 else 0, ctypes.byref(v)))
+        return v.value
+
+    def set_launch_timing(self, on: bool):
+        self._check(self._lib.nwg_set_launch_timing(self.h, 1 if on else 0))
+
+    def launch_records(self):
+        from ._native import LaunchRec
+        n = self._lib.nwg_launch_records(self.h, None, 0)
+        if n < 0:
+            raise NWGError(-n, "launch records")
+        arr = (LaunchRec * max(n, 1))()
+        self._lib.nwg_launch_records(self.h, arr, n)
+        return [arr[k].as_dict() for k in range(n)]
+
     # ---- scoring ---------------------------------------------------------
     def score_all(self, seqs=None, *, codes=None, offsets=None, mode: int = MODE_BATCHED,
                   out: np.ndarray | None = None, stats: bool = False):

@@ -56,11 +56,29 @@ def test_one_and_two_sequences(ctx):
 
 def test_overflow_guard_routes_to_int32(ctx):
     # W scores 11 against itself: a 3200-residue W run bounds H at 35200 > int16
-    seqs = [b"W" * 3200, b"W" * 3100 + b"A" * 50, b"MKV" * 300, b"W" * 3000]
+    seqs = [b"W" * 3200, b"W" * 3100 + b"A" * 50, b"MKV" * 300, b"W" * 3000, b"ACDEFGHIKL" * 310,
+            b"MKVL" * 770]
     D, st = ctx.score_all(seqs, mode=MODE_BATCHED, stats=True)
-    assert st["pairs_int32"] > 0
+    assert st["reruns"] > 0            # int16 attempt rejected by the bound, re-run on int32
     assert np.array_equal(D, O.score_all(seqs, threads=os.cpu_count()))
     assert D[0, 0] == 3200 * 11
+    # lengths above the int16 length guard take int32 lanes for the whole set
+    long = [b"MKV" * 2400, b"W" * 10, b"ACDEFGHIKL" * 30]
+    D, st = ctx.score_all(long, mode=MODE_BATCHED, stats=True)
+    assert st["pairs_int32"] == 6 and st["pairs_int16"] == 0
+    assert np.array_equal(D, O.score_all(long, threads=os.cpu_count()))
+
+
+def test_cached_plan_and_graph_replay_with_new_residues(ctx):
+    # same lengths, different residues: the cached plan and graph are reused
+    a = _rand_set(31, 50, 20, 700)
+    lens_a = [len(x) for x in a]
+    rng = np.random.default_rng(3)
+    letters = np.frombuffer(b"ARNDCQEGHILKMFPSTWYV", dtype=np.uint8)
+    b = [letters[rng.integers(0, 20, L)].tobytes() for L in lens_a]
+    for seqs in (a, b, a):
+        for _ in range(2):
+            assert np.array_equal(ctx.score_all(seqs), O.score_all(seqs, threads=os.cpu_count()))
 
 
 def test_block_shape_with_column_offset(ctx):
