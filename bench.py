@@ -258,6 +258,9 @@ def main():
     d_D = torch.empty((n, n), dtype=torch.float32, device="cuda")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 256 MB > L2
 
+    # kernel choice per length class (cached per device after the first run)
+    tuning = ctx.autotune()
+
     # roofline denominator: the bare DPX cell update on every SM
     peak16 = ctx.dpx_peak(True)
     peak32 = ctx.dpx_peak(False)
@@ -304,7 +307,8 @@ def main():
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                               "quick": True, "n": n, "cells_per_step": cells,
-                              "launch_records": recs, "peak16_gcups": peak16 / 1e9}), flush=True)
+                              "launch_records": recs, "peak16_gcups": peak16 / 1e9, "tuning": tuning}),
+                  flush=True)
         return
 
     # parity spot check of this run's matrix against the oracle (small sample)
@@ -362,7 +366,8 @@ def main():
         ach = dom["cells"] / (dom["ms"] / 1e3)
         roof = {"bound": "int", "achieved": ach / 1e9, "peak": peak / 1e9, "unit": "GCUPS",
                 "frac": ach / peak, "traffic": None,
-                "kernel": f"wave_kernel<R={dom['rows_per_lane']},{'int16x2' if dom['lanes16'] else 'int32'}>",
+                "kernel": f"wave_kernel<R={dom['rows_per_lane']},{'int16x2' if dom['lanes16'] else 'int32'},"
+                          f"V={dom['variant']}>",
                 "launch_ms": dom["ms"], "launch_cells": dom["cells"],
                 "peak_source": "nwg_dpx_peak: 5-instruction DPX cell update on every SM, registers only, "
                                "measured in this run",
@@ -380,7 +385,9 @@ def main():
         "e2e": e2e,
         "gpu_launches": launches,
         "launches_per_step": per_step_launches,
-        "launch_records": [{k: r[k] for k in ("rows_per_lane", "lanes16", "grid", "cells", "ms")} for r in recs],
+        "launch_records": [{k: r[k] for k in ("rows_per_lane", "variant", "lanes16", "grid", "cells", "ms")}
+                           for r in recs],
+        "tuning": tuning,
         "sequential_launch_sum_ms": timed_sum_ms,
         "reruns": st["reruns"],
         "plain": plain,

@@ -132,6 +132,8 @@ typedef struct {
   int64_t pairs;        /* pairs (i<j) this launch computes                    */
   int64_t cells;        /* their L_i*L_j sum                                   */
   double ms;            /* device time (events around this launch alone)       */
+  int32_t variant;      /* register layout of the wave kernel (0 or 1)         */
+  int32_t pad;
 } nwg_launch_rec;
 
 /* Per-launch event timing for the next calls (0 = off, the default: timing
@@ -141,6 +143,33 @@ int nwg_set_launch_timing(nwg_ctx* ctx, int on);
 /* Records of the launches of the last scoring call; returns how many exist
  * (copies at most cap). */
 int nwg_launch_records(nwg_ctx* ctx, nwg_launch_rec* out, int cap);
+
+/* ---- autotuner --------------------------------------------------------------
+ * The batched form has a kernel choice per length class of the shorter
+ * sequences of a pair (the Y rows): rows per lane (4..32, band = 32 x that)
+ * and register layout.  nwg_autotune times every candidate of every class on
+ * synthetic inputs of that class's length and keeps the fastest; the result is
+ * cached in a text file per device (directory $NWG_TUNE_CACHE, else
+ * $HOME/.cache/nwgpu) and reused by later contexts.  Not part of the
+ * reference's interface, which had one fixed window/strip shape
+ * (definitions.cuh:26,47-48). */
+#define NWG_TUNE_CLASSES 8
+
+typedef struct {
+  int32_t classes;                          /* NWG_TUNE_CLASSES                          */
+  int32_t from_cache;                       /* 1 if read from the cache file              */
+  int32_t max_rows[NWG_TUNE_CLASSES];       /* class k: Y rows <= max_rows[k]             */
+  int32_t rows_per_lane[NWG_TUNE_CLASSES];
+  int32_t variant[NWG_TUNE_CLASSES];
+  double gcups[NWG_TUNE_CLASSES];           /* the winner's throughput on the probe       */
+  double seconds;                           /* tuning time (0 from cache)                 */
+} nwg_tune_result;
+
+/* flags: 1 = ignore (and overwrite) the cache. */
+int nwg_autotune(nwg_ctx* ctx, int flags, nwg_tune_result* out);
+
+/* Set the choice per class explicitly (NWG_TUNE_CLASSES entries each). */
+int nwg_set_tuning(nwg_ctx* ctx, const int32_t* rows_per_lane, const int32_t* variant);
 
 #ifdef __cplusplus
 }

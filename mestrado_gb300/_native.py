@@ -111,13 +111,35 @@ class LaunchRec(ctypes.Structure):
         ("pairs", ctypes.c_int64),
         ("cells", ctypes.c_int64),
         ("ms", ctypes.c_double),
+        ("variant", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
     ]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
+
+
+class TuneResult(ctypes.Structure):
+    _fields_ = [
+        ("classes", ctypes.c_int32),
+        ("from_cache", ctypes.c_int32),
+        ("max_rows", ctypes.c_int32 * 8),
+        ("rows_per_lane", ctypes.c_int32 * 8),
+        ("variant", ctypes.c_int32 * 8),
+        ("gcups", ctypes.c_double * 8),
+        ("seconds", ctypes.c_double),
+    ]
+
+    def as_dict(self):
+        n = self.classes
+        return {"from_cache": bool(self.from_cache), "seconds": self.seconds,
+                "classes": [{"max_rows": self.max_rows[k], "rows_per_lane": self.rows_per_lane[k],
+                             "variant": self.variant[k], "gcups": self.gcups[k]} for k in range(n)]}
 
 
 EXTRA_SIGS: dict = {
+    "nwg_autotune": ([ctypes.c_void_p, ctypes.c_int, P(TuneResult)], ctypes.c_int),
+    "nwg_set_tuning": ([ctypes.c_void_p, c_i32p, c_i32p], ctypes.c_int),
     "nwg_dpx_peak": ([ctypes.c_void_p, ctypes.c_int, P(ctypes.c_double)], ctypes.c_int),
     "nwg_set_launch_timing": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "nwg_launch_records": ([ctypes.c_void_p, P(LaunchRec), ctypes.c_int], ctypes.c_int),

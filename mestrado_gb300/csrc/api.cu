@@ -148,13 +148,10 @@ int Ctx::prepare_set(const int8_t* d_codes, const int64_t* offsets, int n, SetVi
   return NWG_OK;
 }
 
-int choose_rows_per_lane(int rows, const int* table) {
-  // table: rows-per-lane choice for band-fitting lengths; the last entry is
-  // used (with several bands) for anything longer.
-  static const int kR[] = {4, 8, 12, 16, 24};
-  for (int k = 0; k < 5; ++k)
-    if (rows <= 32 * kR[k]) return table ? table[k] : kR[k];
-  return table ? table[5] : 24;
+int tune_class(int rows) {
+  for (int k = 0; k < kTuneClasses; ++k)
+    if (rows <= kClassRows[k]) return k;
+  return kTuneClasses - 1;
 }
 
 // Build and launch the batched (wavefront) plan for X rows against Y groups.
@@ -333,6 +330,7 @@ int nwg_ctx_create(int gap_open, int gap_ext, const int8_t* sub, nwg_ctx** out) 
     return rc;
   }
   c->stream = c->own_stream;
+  for (int k = 0; k < nwg::kTuneClasses; ++k) c->tune[k] = nwg::kDefaultTune[k];
   for (int k = 0; k < 2; ++k) {
     cudaStream_t b;
     cudaEvent_t e;

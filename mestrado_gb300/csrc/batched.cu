@@ -70,12 +70,13 @@ struct BatchPlan {
   bool triangle = true;
   int mode = -1;
   uint64_t hx = 0, hy = 0;
-  const int* tune = nullptr;
+  uint64_t tune_version = 0;
   // sorted sets (host copies + device arrays)
   SetView X, Y;
   DevBuf bxs, bxl, bxo, bxb, bys, byl, byo, byb;
   // groups, buckets
-  struct Bucket { int R, P, check, g0, ng; int64_t j0, njobs, pairs; double cells; int grid; };
+  struct Bucket { int R, P, V, check, g0, ng; int64_t j0, njobs, pairs; double cells; int grid; size_t scratch_off;
+                  int maxrows; };
   std::vector<Bucket> buckets;
   DevBuf gy, gy2, gx, jobs, counters, rerun, rerun_scratch, wscratch;
   int64_t rerun_cap = 0, rerun_threads = 0;
@@ -146,7 +147,7 @@ static int get_plan(Ctx* c, const int64_t* xoff, int nx, const int64_t* yoff, in
   const uint64_t hx = fnv(xoff, nx), hy = triangle ? hx : fnv(yoff, ny, 7);
   BatchPlan*& slot = c->plans[triangle ? 0 : 1];
   if (slot && slot->nx == nx && slot->ny == ny && slot->mode == mode && slot->hx == hx && slot->hy == hy &&
-      slot->tune == c->tune_table) {
+      slot->tune_version == c->tune_version) {
     *out = slot;
     return NWG_OK;
   }
@@ -154,7 +155,7 @@ static int get_plan(Ctx* c, const int64_t* xoff, int nx, const int64_t* yoff, in
   slot = nullptr;
   BatchPlan* p = new BatchPlan();
   p->nx = nx; p->ny = ny; p->triangle = triangle; p->mode = mode; p->hx = hx; p->hy = hy;
-  p->tune = c->tune_table;
+  p->tune_version = c->tune_version;
   int rc;
   if ((rc = upload_set(c, xoff, nx, p->X, p->bxs, p->bxl, p->bxo, p->bxb))) { delete p; return rc; }
   if (triangle) {
@@ -173,11 +174,12 @@ static int get_plan(Ctx* c, const int64_t* xoff, int nx, const int64_t* yoff, in
   for (int k = 0; k < kLetters * kLetters; ++k) maxs = std::max<int>(maxs, c->sub[k]);
   const int certain_len = maxs > 0 ? kInt16MaxH / maxs : 1 << 30;
 
-  struct Group { int y, y2, nx, R, P, check; };
+  struct Group { int y, y2, nx, R, V, P, check; };
   std::vector<Group> groups;
   groups.reserve((size_t)Y.n / 2 + 1);
   for (int y = 0; y < Y.n;) {
-    const int R = choose_rows_per_lane(Y.len[y], c->tune_table);
+    const TuneChoice tc = c->tune[tune_class(Y.len[y])];
+    const int R = tc.R, V = tc.V;
     if (!force32) {
       const int y2 = y + 1 < Y.n ? y + 1 : -1;
       const int last = y2 >= 0 ? y2 : y;
@@ -185,15 +187,16 @@ static int get_plan(Ctx* c, const int64_t* xoff, int nx, const int64_t* yoff, in
       // Y sorted by length: Y.len[y] is the group's longest; the pair's
       // shorter sequence is at most that long.
       const int check = Y.len[y] > certain_len ? 1 : 0;
-      groups.push_back({y, y2, nxg, R, 2, check});
+      groups.push_back({y, y2, nxg, R, V, 2, check});
       y = last + 1;
     } else {
-      groups.push_back({y, -1, triangle ? y + 1 : X.n, R, 1, 0});
+      groups.push_back({y, -1, triangle ? y + 1 : X.n, R, V, 1, 0});
       ++y;
     }
   }
   std::stable_sort(groups.begin(), groups.end(), [](const Group& a, const Group& b) {
     if (a.R != b.R) return a.R > b.R;
+    if (a.V != b.V) return a.V > b.V;
     if (a.P != b.P) return a.P > b.P;
     return a.check > b.check;
   });
@@ -206,13 +209,16 @@ static int get_plan(Ctx* c, const int64_t* xoff, int nx, const int64_t* yoff, in
   prefix.reserve(ng + 16);
   for (int k = 0; k < ng;) {
     int e = k;
-    while (e < ng && groups[e].R == groups[k].R && groups[e].P == groups[k].P && groups[e].check == groups[k].check)
+    while (e < ng && groups[e].R == groups[k].R && groups[e].V == groups[k].V && groups[e].P == groups[k].P &&
+           groups[e].check == groups[k].check)
       ++e;
-    BatchPlan::Bucket b{groups[k].R, groups[k].P, groups[k].check, k, e - k, (int64_t)prefix.size(), 0, 0, 0.0, 0};
+    BatchPlan::Bucket b{groups[k].R, groups[k].P, groups[k].V, groups[k].check, k, e - k, (int64_t)prefix.size(),
+                        0, 0, 0.0, 0, 0, 0};
     int64_t acc = 0;
     for (int g = k; g < e; ++g) {
       prefix.push_back(acc);
       acc += (groups[g].nx + kWaveWarps - 1) / kWaveWarps;
+      b.maxrows = std::max(b.maxrows, Y.len[groups[g].y]);
       for (int yy : {groups[g].y, groups[g].y2}) {
         if (yy < 0) continue;
         const int cnt = triangle ? yy : X.n;   // pairs i<j only (diagonal not counted)
@@ -243,15 +249,18 @@ static int get_plan(Ctx* c, const int64_t* xoff, int nx, const int64_t* yoff, in
     delete p;
     return rc;
   }
-  // grids (persistent: SMs x resident CTAs, capped by the jobs) and scratch
-  int grid_max = 1;
-  for (auto& b : p->buckets) {
-    b.grid = (int)std::min<int64_t>(b.njobs, (int64_t)c->sms * wave_max_ctas_per_sm(b.R, b.P));
-    b.grid = std::max(b.grid, 1);
-    grid_max = std::max(grid_max, b.grid);
-  }
+  // grids (persistent: SMs x resident CTAs, capped by the jobs) and the band
+  // boundary scratch: buckets run concurrently, so every bucket with more than
+  // one band gets its own region
   p->scols = std::max(X.maxlen, 1);
-  if ((rc = p->wscratch.ensure(sizeof(int32_t) * (size_t)grid_max * kWaveWarps * 4 * p->scols))) {
+  size_t scratch_words = 1;
+  for (auto& b : p->buckets) {
+    b.grid = (int)std::min<int64_t>(b.njobs, (int64_t)c->sms * wave_max_ctas_per_sm(b.R, b.P, b.V));
+    b.grid = std::max(b.grid, 1);
+    b.scratch_off = scratch_words;
+    if (b.maxrows > 32 * b.R) scratch_words += (size_t)b.grid * kWaveWarps * 4 * p->scols;
+  }
+  if ((rc = p->wscratch.ensure(sizeof(int32_t) * scratch_words))) {
     delete p;
     return c->fail(rc, "wave scratch");
   }
@@ -325,12 +334,13 @@ static int enqueue_step(Ctx* c, BatchPlan* p, const int8_t* d_codes, float* d_D,
     a.g_begin = b.g0;
     a.ngroups = b.ng;
     a.check_bound = b.check;
+    a.scratch = (int32_t*)p->wscratch.p + b.scratch_off;
     int ri = -1;
     if (timed) {
-      nwg_launch_rec r{0, b.R, b.P == 2 ? 1 : 0, b.grid, b.pairs, (int64_t)b.cells, 0.0};
+      nwg_launch_rec r{0, b.R, b.P == 2 ? 1 : 0, b.grid, b.pairs, (int64_t)b.cells, 0.0, b.V, 0};
       if ((ri = c->rec_begin(r)) < 0) return c->fail(NWG_ERR_CUDA, "launch timing");
     }
-    if ((rc = c->cuda(launch_wave(b.R, b.P, a, b.grid, bs), "wave launch"))) return rc;
+    if ((rc = c->cuda(launch_wave(b.R, b.P, b.V, a, b.grid, bs), "wave launch"))) return rc;
     if (ri >= 0 && (rc = c->rec_end(ri))) return rc;
     ++c->launches;
   }
@@ -353,7 +363,7 @@ int Ctx::batched(const int8_t* d_codes, const int64_t* xoff, int nx, const int64
   BatchPlan* p = nullptr;
   int rc;
   if ((rc = get_plan(this, xoff, nx, yoff, ny, triangle, mode, &p))) return rc;
-  for (const auto& b : p->buckets) prepare_wave(b.R, b.P);
+  for (const auto& b : p->buckets) prepare_wave(b.R, b.P, b.V);
   if (st) {
     st->pairs_int16 += p->pairs16;
     st->pairs_int32 += p->pairs32;

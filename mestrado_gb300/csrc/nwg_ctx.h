@@ -30,7 +30,17 @@ struct SetView {
 
 const int8_t* builtin_matrix();
 const char* letter_order();
-int choose_rows_per_lane(int rows, const int* table);
+
+struct TuneChoice {
+  int R;   // rows per lane (4, 8, 12, 16, 20, 24, 32)
+  int V;   // register layout (0 or 1)
+};
+constexpr int kTuneClasses = 8;
+// Upper bound of the Y rows of each class; the last class takes every longer Y.
+constexpr int kClassRows[kTuneClasses] = {128, 256, 384, 512, 640, 768, 1024, 1 << 30};
+constexpr TuneChoice kDefaultTune[kTuneClasses] = {{4, 1}, {8, 1}, {12, 1}, {16, 1},
+                                                   {20, 1}, {24, 1}, {32, 1}, {32, 1}};
+int tune_class(int rows);
 
 struct BatchPlan;
 struct Ctx;
@@ -45,8 +55,11 @@ struct Ctx {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::string last_err;
   int launches = 0;
-  const int* tune_table = nullptr;   // rows-per-lane per length class (6 entries) or null
-  int tune_storage[6] = {4, 8, 12, 16, 24, 24};
+  // Kernel choice per length class of the Y rows (rows <= kClassRows[k]):
+  // rows per lane and register layout, set by the autotuner (tune.cu).
+  TuneChoice tune[kTuneClasses];
+  uint64_t tune_version = 0;        // bumped on every change (part of the plan key)
+  bool tuned = false;
 
   DevBuf b_codes, b_start, b_len, b_orig, b_bound, b_bad;
   DevBuf b_start2, b_len2, b_orig2;
@@ -66,6 +79,7 @@ struct Ctx {
   std::vector<cudaStream_t> branch;     // parallel branches for bucket launches
   cudaEvent_t fork_ev = nullptr;
   std::vector<cudaEvent_t> join_ev;
+  int autotune(bool force, nwg_tune_result* out);
   int batched(const int8_t* d_codes, const int64_t* xoff, int nx, const int64_t* yoff, int ny, bool triangle,
               float* d_D, int64_t ld, int64_t col0, int mode, nwg_stats* st);
   // traceback / neighbor joining state (trace.cu, nj.cu)

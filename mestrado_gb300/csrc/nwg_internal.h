@@ -112,11 +112,13 @@ struct PairListArgs {
   const int8_t* sub;
 };
 
-// Launchers (score_kernels.cu).  R is the rows per lane; P = 2 for int16x2
-// lanes (two pairs per warp), 1 for int32 lanes.
-cudaError_t launch_wave(int R, int P, const WaveArgs& a, int grid, cudaStream_t s);
-int wave_max_ctas_per_sm(int R, int P);
-void prepare_wave(int R, int P);   // sets the dynamic shared memory limit (outside graph capture)
+// Launchers (score_kernels.cu, wave_r*.cu).  R is the rows per lane; P = 2
+// for int16x2 lanes (two pairs per warp), 1 for int32 lanes.
+// V: register layout of the wave kernel (0: H, H-go, E per row; 1: H, E per
+// row with a min-blocks launch bound).
+cudaError_t launch_wave(int R, int P, int V, const WaveArgs& a, int grid, cudaStream_t s);
+int wave_max_ctas_per_sm(int R, int P, int V);
+void prepare_wave(int R, int P, int V);   // sets the dynamic shared memory limit (outside graph capture)
 size_t wave_smem_bytes(int R);
 cudaError_t launch_plain(const PlainArgs& a, cudaStream_t s);
 cudaError_t launch_rerun(const WaveArgs& a, int2* scratch, int64_t nthreads, cudaStream_t s);

@@ -1,0 +1,201 @@
+// tune.cu -- autotuner of the batched form: per length class of the Y rows,
+// the rows-per-lane template and register layout of the wave kernel.
+//
+// For class k a probe workload is built from uniform random residues: 128 Y
+// sequences of the class's representative length and enough X sequences
+// (10% longer) for ~2e10 cells, scored in block mode so every pair lands in
+// that class.  Each candidate (R, V) runs once to warm up and once timed with
+// CUDA events; the fastest wins.  The table is written to a cache file per
+// device (name + SM count) and read back by later contexts.
+#include <sys/stat.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "nwg_ctx.h"
+
+namespace nwg {
+
+namespace {
+
+std::string cache_path(int device) {
+  cudaDeviceProp prop;
+  std::memset(&prop, 0, sizeof(prop));
+  cudaGetDeviceProperties(&prop, device);
+  std::string name(prop.name);
+  for (char& ch : name)
+    if (!((ch >= 'a' && ch <= 'z') || (ch >= 'A' && ch <= 'Z') || (ch >= '0' && ch <= '9'))) ch = '_';
+  std::string dir;
+  if (const char* e = std::getenv("NWG_TUNE_CACHE")) dir = e;
+  else if (const char* h = std::getenv("HOME")) dir = std::string(h) + "/.cache/nwgpu";
+  else dir = "/tmp/nwgpu";
+  return dir + "/tune_v1_" + name + "_sm" + std::to_string(prop.multiProcessorCount) + ".txt";
+}
+
+void make_parent_dirs(const std::string& file) {
+  for (size_t k = 1; k < file.size(); ++k)
+    if (file[k] == '/') mkdir(file.substr(0, k).c_str(), 0755);   // existing levels just fail
+}
+
+const int kCandR[] = {4, 8, 12, 16, 20, 24, 32};
+
+int representative_rows(int k) {
+  if (k == kTuneClasses - 1) return 1300;
+  const int lo = k == 0 ? 0 : kClassRows[k - 1];
+  return lo + (kClassRows[k] - lo) * 3 / 4;
+}
+
+}  // namespace
+
+int Ctx::autotune(bool force, nwg_tune_result* out) {
+  const std::string path = cache_path(device);
+  nwg_tune_result res;
+  std::memset(&res, 0, sizeof(res));
+  res.classes = kTuneClasses;
+  for (int k = 0; k < kTuneClasses; ++k) res.max_rows[k] = kClassRows[k] > 1000000 ? 0x7fffffff : kClassRows[k];
+  if (!force) {
+    if (FILE* f = std::fopen(path.c_str(), "r")) {
+      int ok = 0;
+      TuneChoice t[kTuneClasses];
+      double g[kTuneClasses];
+      for (int k = 0; k < kTuneClasses; ++k) {
+        int kk, R, V;
+        double gc;
+        if (std::fscanf(f, "%d %d %d %lf", &kk, &R, &V, &gc) == 4 && kk == k &&
+            std::find(std::begin(kCandR), std::end(kCandR), R) != std::end(kCandR) && (V == 0 || V == 1)) {
+          t[k] = {R, V};
+          g[k] = gc;
+          ++ok;
+        }
+      }
+      std::fclose(f);
+      if (ok == kTuneClasses) {
+        for (int k = 0; k < kTuneClasses; ++k) {
+          tune[k] = t[k];
+          res.rows_per_lane[k] = t[k].R;
+          res.variant[k] = t[k].V;
+          res.gcups[k] = g[k];
+        }
+        ++tune_version;
+        tuned = true;
+        res.from_cache = 1;
+        if (out) *out = res;
+        return NWG_OK;
+      }
+    }
+  }
+  const auto t0 = std::chrono::steady_clock::now();
+  const bool saved_graphs = use_graphs;
+  use_graphs = false;
+  uint64_t lcg = 0x243F6A8885A308D3ull;
+  auto rnd = [&]() {
+    lcg = lcg * 6364136223846793005ull + 1442695040888963407ull;
+    return (uint32_t)(lcg >> 33);
+  };
+  int rc = NWG_OK;
+  DevBuf probe;
+  for (int k = 0; k < kTuneClasses && rc == NWG_OK; ++k) {
+    const int Ly = representative_rows(k);
+    const int Lx = Ly + Ly / 10;
+    const int ny = 128;
+    int nx = (int)std::min<double>(4096.0, std::max<double>(256.0, 2e10 / ((double)ny * Ly * Lx)));
+    nx = (nx + kWaveWarps - 1) / kWaveWarps * kWaveWarps;
+    std::vector<int64_t> xoff(nx + 1), yoff(ny + 1);
+    for (int i = 0; i <= nx; ++i) xoff[i] = (int64_t)i * Lx;
+    for (int j = 0; j <= ny; ++j) yoff[j] = (int64_t)nx * Lx + (int64_t)j * Ly;
+    const size_t total = (size_t)nx * Lx + (size_t)ny * Ly;
+    std::vector<int8_t> codes(total);
+    for (auto& ch : codes) ch = (int8_t)(rnd() % 20);
+    if ((rc = probe.ensure(total + sizeof(float) * (size_t)nx * ny))) {
+      rc = fail(rc, "autotune probe");
+      break;
+    }
+    int8_t* dcodes = (int8_t*)probe.p;
+    float* dD = (float*)((char*)probe.p + ((total + 255) / 256) * 256);
+    if ((size_t)((char*)dD - (char*)probe.p) + sizeof(float) * (size_t)nx * ny > probe.cap) {
+      probe.release();
+      if ((rc = probe.ensure(((total + 255) / 256) * 256 + sizeof(float) * (size_t)nx * ny))) {
+        rc = fail(rc, "autotune probe");
+        break;
+      }
+      dcodes = (int8_t*)probe.p;
+      dD = (float*)((char*)probe.p + ((total + 255) / 256) * 256);
+    }
+    if ((rc = cuda(cudaMemcpy(dcodes, codes.data(), total, cudaMemcpyHostToDevice), "autotune upload"))) break;
+    double best = -1.0;
+    TuneChoice pick = kDefaultTune[k];
+    for (int R : kCandR) {
+      const int band = 32 * R;
+      if (band * 3 < Ly || band > 2 * Ly + 128) continue;   // at most 3 bands, at most ~half idle
+      for (int V = 0; V <= 1; ++V) {
+        tune[k] = {R, V};
+        ++tune_version;
+        float ms = 0.f;
+        for (int rep = 0; rep < 2 && rc == NWG_OK; ++rep) {
+          if ((rc = cuda(cudaEventRecord(ev0, stream), "autotune event"))) break;
+          if ((rc = batched(dcodes, xoff.data(), nx, yoff.data(), ny, false, dD, ny, 0, NWG_MODE_BATCHED, nullptr)))
+            break;
+          if ((rc = cuda(cudaEventRecord(ev1, stream), "autotune event")) ||
+              (rc = cuda(cudaEventSynchronize(ev1), "autotune sync")))
+            break;
+          cudaEventElapsedTime(&ms, ev0, ev1);
+        }
+        if (rc) break;
+        const double g = (double)nx * ny * Ly * Lx / (ms * 1e-3) / 1e9;
+        if (g > best) {
+          best = g;
+          pick = {R, V};
+        }
+      }
+      if (rc) break;
+    }
+    tune[k] = pick;
+    res.rows_per_lane[k] = pick.R;
+    res.variant[k] = pick.V;
+    res.gcups[k] = best;
+  }
+  probe.release();
+  destroy_plans(this);   // the probe plans are of no further use
+  use_graphs = saved_graphs;
+  ++tune_version;
+  if (rc) {
+    for (int k = 0; k < kTuneClasses; ++k) tune[k] = kDefaultTune[k];
+    return rc;
+  }
+  tuned = true;
+  res.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  make_parent_dirs(path);
+  if (FILE* f = std::fopen(path.c_str(), "w")) {
+    for (int k = 0; k < kTuneClasses; ++k)
+      std::fprintf(f, "%d %d %d %.3f\n", k, tune[k].R, tune[k].V, res.gcups[k]);
+    std::fclose(f);
+  }
+  if (out) *out = res;
+  return NWG_OK;
+}
+
+}  // namespace nwg
+
+extern "C" int nwg_autotune(nwg_ctx* ctx, int flags, nwg_tune_result* out) {
+  if (!ctx) return NWG_ERR_INVALID;
+  return reinterpret_cast<nwg::Ctx*>(ctx)->autotune((flags & 1) != 0, out);
+}
+
+extern "C" int nwg_set_tuning(nwg_ctx* ctx, const int32_t* rows_per_lane, const int32_t* variant) {
+  if (!ctx || !rows_per_lane || !variant) return NWG_ERR_INVALID;
+  nwg::Ctx* c = reinterpret_cast<nwg::Ctx*>(ctx);
+  for (int k = 0; k < nwg::kTuneClasses; ++k) {
+    if (std::find(std::begin(nwg::kCandR), std::end(nwg::kCandR), rows_per_lane[k]) == std::end(nwg::kCandR) ||
+        (variant[k] != 0 && variant[k] != 1))
+      return NWG_ERR_INVALID;
+  }
+  for (int k = 0; k < nwg::kTuneClasses; ++k) c->tune[k] = {rows_per_lane[k], variant[k]};
+  ++c->tune_version;
+  c->tuned = true;
+  return NWG_OK;
+}

@@ -103,6 +103,20 @@ class Context:
         self._check(self._lib.nwg_dpx_peak(self.h, 1 if lanes16 else 0, ctypes.byref(v)))
         return v.value
 
+    def autotune(self, force: bool = False) -> dict:
+        """Pick the wave-kernel template per length class (cached per device)."""
+        from ._native import TuneResult
+        r = TuneResult()
+        self._check(self._lib.nwg_autotune(self.h, 1 if force else 0, ctypes.byref(r)))
+        return r.as_dict()
+
+    def set_tuning(self, rows_per_lane, variant):
+        rp = np.ascontiguousarray(rows_per_lane, dtype=np.int32)
+        vv = np.ascontiguousarray(variant, dtype=np.int32)
+        if rp.shape != (8,) or vv.shape != (8,):
+            raise ValueError("8 length classes expected")
+        self._check(self._lib.nwg_set_tuning(self.h, _p(rp, c_i32p), _p(vv, c_i32p)))
+
     def set_launch_timing(self, on: bool):
         self._check(self._lib.nwg_set_launch_timing(self.h, 1 if on else 0))
 

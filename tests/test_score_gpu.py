@@ -144,3 +144,32 @@ def test_config1_full_size_properties_and_sample(ctx):
     assert np.array_equal(Db[pi, pj], ref.astype(np.float32))
     diag = O.score_list(codes, off, np.arange(0, n, 37), np.arange(0, n, 37), threads=os.cpu_count())
     assert np.array_equal(np.diag(Db)[::37], diag.astype(np.float32))
+
+
+@pytest.mark.parametrize("R", [4, 8, 12, 16, 20, 24, 32])
+@pytest.mark.parametrize("V", [0, 1])
+def test_every_kernel_template_matches_oracle(R, V):
+    # the autotuner may pick any (rows per lane, register layout) for any
+    # length class: every template must be exact, single- and multi-band
+    from mestrado_gb300 import Context
+    seqs = _rand_set(40 + R, 26, 1, 900)
+    ref = O.score_all(seqs, threads=os.cpu_count())
+    with Context(10, 2) as c:
+        c.set_tuning([R] * 8, [V] * 8)
+        for mode in (MODE_BATCHED, MODE_BATCHED_INT32):
+            assert np.array_equal(c.score_all(seqs, mode=mode), ref)
+
+
+def test_autotune_then_exact(tmp_path, monkeypatch):
+    monkeypatch.setenv("NWG_TUNE_CACHE", str(tmp_path))
+    from mestrado_gb300 import Context
+    with Context(10, 2) as c:
+        r = c.autotune(force=True)
+        assert not r["from_cache"] and len(r["classes"]) == 8
+        assert all(k["gcups"] > 0 for k in r["classes"])
+        seqs = _rand_set(77, 40, 10, 1200)
+        assert np.array_equal(c.score_all(seqs), O.score_all(seqs, threads=os.cpu_count()))
+    with Context(10, 2) as c:
+        r2 = c.autotune()
+        assert r2["from_cache"]
+        assert [k["rows_per_lane"] for k in r2["classes"]] == [k["rows_per_lane"] for k in r["classes"]]
