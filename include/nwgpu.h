@@ -113,6 +113,76 @@ int nwg_score_pairs(nwg_ctx* ctx, const int8_t* codes, const int64_t* offsets, i
                     const int32_t* pi, const int32_t* pj, int64_t npairs, int32_t* out,
                     nwg_stats* stats);
 
+/* ---- pairwise alignment with traceback ------------------------------------ */
+
+/* Replaces AlignmentMatch::computePairwise (AlignmentMatch.cu:140-317) and
+ * its MatchKernel/BacktraceKernel/ReorderMatches launches (NeedlemanWunsch.cu:
+ * 592-613): pair k aligns X = sequence px[k] (columns) with Y = sequence
+ * py[k] (rows).  Writes the two gapped strings in forward order ('-' for a
+ * gap, letters decoded as revConvConst, definitions.cuh:134-137), each
+ * NUL-terminated, at outx + k*stride and outy + k*stride (stride >= Lx+Ly+1),
+ * the alignment length to len[k] and, if score != NULL, the score to
+ * score[k].  codes/offsets are reversed codes (nwg_encode).  Host buffers. */
+int nwg_align_pairs(nwg_ctx* ctx, const int8_t* codes, const int64_t* offsets, int n,
+                    const int32_t* px, const int32_t* py, int npairs, char* outx, char* outy,
+                    int64_t stride, int32_t* len, int32_t* score, nwg_stats* stats);
+
+/* Guide-tree cherries (AlignmentMatch.cu:167-186 over TreeNode::getNodes,
+ * TreeNode.cpp:91-117): internal node n_leaves+k joins left[k] and right[k]
+ * (node ids: leaves 0..n_leaves-1, internal nodes in creation order).  Lists
+ * every internal node whose two children are leaves, in the post-order of
+ * getNodes (left subtree, right subtree, node).  Returns the count (outputs may
+ * be NULL to only count) or a negative status. */
+int nwg_cherries(const int32_t* left, const int32_t* right, int n_leaves, int32_t* node,
+                 int32_t* l, int32_t* r);
+
+/* ---- neighbor joining ------------------------------------------------------ */
+
+/* One join: nodes i < j merged into node `node` (= n0 + step) while n nodes
+ * were active; d = D[i][j]; q the winning value; ti/tj the row sums and
+ * len_i/len_j the branch lengths TreeNode::join gives to i and j
+ * (TreeNode.cpp:31-58). */
+typedef struct {
+  int32_t i, j;
+  int32_t node;
+  int32_t n;
+  float d;
+  float pad;
+  double q;
+  double ti, tj;
+  double len_i, len_j;
+} nwg_join;
+
+typedef struct {
+  int64_t ambiguous_steps;  /* steps where the reference's heap rounding or a >4-way exact tie
+                               could pick differently (the exact-argmin pick is kept)          */
+  int64_t tie_steps;        /* steps decided by the (max j, max i) tie-break                      */
+  int64_t rebuilds;         /* row-sum rebuilds                                                   */
+  int64_t pq_trigger_open;  /* heap-size rebuild checks that could not be excluded                */
+  double device_ms;         /* device time of the join loop                                       */
+  int32_t launches;
+  int32_t pad;
+} nwg_nj_stats;
+
+/* Replaces SpeciesBlock::buildTree on one rank (SpeciesBlock.cpp:845-1343):
+ * the n-1 joins of neighbor joining on the n x n float matrix D (row-major,
+ * leading dimension ld; the caller's matrix is not modified) in the
+ * reference's order, with its FP32 matrix updates, FP64 row sums and
+ * q = d*(n-2) - T_i - T_j, and its tie-break (larger max(i,j), then larger
+ * min(i,j)).  joins must hold n-1 records.  n <= 8192. */
+int nwg_nj(nwg_ctx* ctx, const float* D, int64_t ld, int n, nwg_join* joins, nwg_nj_stats* stats);
+
+/* Same with D already on the device (d_D). */
+int nwg_nj_dev(nwg_ctx* ctx, const float* d_D, int64_t ld, int n, nwg_join* joins, nwg_nj_stats* stats);
+
+/* The Newick text TreeNode::buildTreeOutput writes (TreeNode.cpp:61-81,
+ * SpeciesBlock.cpp:1328-1338): "(\n", ",\n", ")\n" separators, lengths as
+ * ":" setprecision(4) showpoint setw(8), terminated by ";\n".  names[k] is
+ * leaf k's label (the reference uses the whole FASTA header line, '>'
+ * included).  Writes at most cap bytes (NUL-terminated) and returns the full
+ * length, or a negative status. */
+int64_t nwg_newick(const nwg_join* joins, int n, const char* const* names, char* out, int64_t cap);
+
 /* ---- measurement ---------------------------------------------------------
  * Not part of the reference's interface (the reference times nothing on the
  * device; timer.h falls back to clock()).  These give the bench its roofline

@@ -12,9 +12,9 @@ include/nwgpu.h); this package is its Python host side:
 from __future__ import annotations
 
 from ._native import (MODE_BATCHED, MODE_BATCHED_INT32, MODE_PLAIN, NWGError, Stats, check, lib)
-from .nwgpu import AlignmentScore, Context, encode, make_wire, parse_wire
+from .nwgpu import AlignmentScore, Context, cherries, encode, make_wire, newick, parse_wire
 
 __all__ = [
-    "AlignmentScore", "Context", "encode", "make_wire", "parse_wire", "NWGError", "Stats",
+    "AlignmentScore", "Context", "cherries", "encode", "newick", "make_wire", "parse_wire", "NWGError", "Stats",
     "MODE_BATCHED", "MODE_PLAIN", "MODE_BATCHED_INT32", "check", "lib",
 ]

@@ -137,9 +137,40 @@ class TuneResult(ctypes.Structure):
                              "variant": self.variant[k], "gcups": self.gcups[k]} for k in range(n)]}
 
 
+class Join(ctypes.Structure):
+    _fields_ = [
+        ("i", ctypes.c_int32), ("j", ctypes.c_int32), ("node", ctypes.c_int32), ("n", ctypes.c_int32),
+        ("d", ctypes.c_float), ("pad", ctypes.c_float), ("q", ctypes.c_double),
+        ("ti", ctypes.c_double), ("tj", ctypes.c_double),
+        ("len_i", ctypes.c_double), ("len_j", ctypes.c_double),
+    ]
+
+
+class NJStats(ctypes.Structure):
+    _fields_ = [("ambiguous_steps", ctypes.c_int64), ("tie_steps", ctypes.c_int64),
+                ("rebuilds", ctypes.c_int64), ("pq_trigger_open", ctypes.c_int64),
+                ("device_ms", ctypes.c_double), ("launches", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
+
+
+JOIN_DTYPE = [("i", "i4"), ("j", "i4"), ("node", "i4"), ("n", "i4"), ("d", "f4"), ("pad", "f4"),
+              ("q", "f8"), ("ti", "f8"), ("tj", "f8"), ("len_i", "f8"), ("len_j", "f8")]
+
 EXTRA_SIGS: dict = {
+    "nwg_nj": ([ctypes.c_void_p, c_f32p, ctypes.c_int64, ctypes.c_int, ctypes.c_void_p, P(NJStats)],
+               ctypes.c_int),
+    "nwg_nj_dev": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_void_p,
+                    P(NJStats)], ctypes.c_int),
+    "nwg_newick": ([ctypes.c_void_p, ctypes.c_int, P(ctypes.c_char_p), ctypes.c_char_p, ctypes.c_int64],
+                   ctypes.c_int64),
     "nwg_autotune": ([ctypes.c_void_p, ctypes.c_int, P(TuneResult)], ctypes.c_int),
     "nwg_set_tuning": ([ctypes.c_void_p, c_i32p, c_i32p], ctypes.c_int),
+    "nwg_align_pairs": ([ctypes.c_void_p, c_i8p, c_i64p, ctypes.c_int, c_i32p, c_i32p, ctypes.c_int,
+                         ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int64, c_i32p, c_i32p, P(Stats)],
+                        ctypes.c_int),
+    "nwg_cherries": ([c_i32p, c_i32p, ctypes.c_int, c_i32p, c_i32p, c_i32p], ctypes.c_int),
     "nwg_dpx_peak": ([ctypes.c_void_p, ctypes.c_int, P(ctypes.c_double)], ctypes.c_int),
     "nwg_set_launch_timing": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "nwg_launch_records": ([ctypes.c_void_p, P(LaunchRec), ctypes.c_int], ctypes.c_int),

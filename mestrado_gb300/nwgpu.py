@@ -14,7 +14,7 @@ import numpy as np
 from ._native import (MODE_BATCHED, MODE_BATCHED_INT32, MODE_PLAIN, NWGError, Stats, c_f32p,
                       c_i8p, c_i32p, c_i64p, check, lib)
 
-__all__ = ["Context", "AlignmentScore", "encode", "make_wire", "parse_wire"]
+__all__ = ["Context", "AlignmentScore", "cherries", "encode", "make_wire", "newick", "parse_wire"]
 
 
 def _p(a: np.ndarray, ct):
@@ -173,6 +173,50 @@ class Context:
                                               D.strides[0] // 4, r0, mode, ctypes.byref(st)))
         return (D, st.as_dict()) if stats else D
 
+    def align_pairs(self, codes, offsets, px, py, stats: bool = False):
+        """Gapped alignments (X = px[k] columns, Y = py[k] rows): list of
+        (aligned_x, aligned_y, score) in forward order."""
+        px = np.ascontiguousarray(px, dtype=np.int32)
+        py = np.ascontiguousarray(py, dtype=np.int32)
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        codes = np.ascontiguousarray(codes, dtype=np.int8)
+        m = len(px)
+        L = np.diff(offsets)
+        stride = int((L[px] + L[py]).max()) + 1 if m else 1
+        bx = ctypes.create_string_buffer(max(m * stride, 1))
+        by = ctypes.create_string_buffer(max(m * stride, 1))
+        ln = np.zeros(max(m, 1), dtype=np.int32)
+        sc = np.zeros(max(m, 1), dtype=np.int32)
+        st = Stats()
+        self._check(self._lib.nwg_align_pairs(self.h, _p(codes, c_i8p), _p(offsets, c_i64p), len(offsets) - 1,
+                                              _p(px, c_i32p), _p(py, c_i32p), m, bx, by, stride,
+                                              _p(ln, c_i32p), _p(sc, c_i32p), ctypes.byref(st)))
+        rawx, rawy = bx.raw, by.raw
+        out = [(rawx[k * stride:k * stride + ln[k]], rawy[k * stride:k * stride + ln[k]], int(sc[k]))
+               for k in range(m)]
+        return (out, st.as_dict()) if stats else out
+
+    def nj(self, D, stats: bool = False):
+        """Neighbor joining on the device: structured array of the n-1 joins."""
+        from ._native import JOIN_DTYPE, NJStats
+        D = np.ascontiguousarray(D, dtype=np.float32)
+        n = D.shape[0]
+        joins = np.zeros(max(n - 1, 1), dtype=np.dtype(JOIN_DTYPE))
+        st = NJStats()
+        self._check(self._lib.nwg_nj(self.h, _p(D, c_f32p), D.strides[0] // 4, n,
+                                     joins.ctypes.data_as(ctypes.c_void_p), ctypes.byref(st)))
+        joins = joins[: max(n - 1, 0)]
+        return (joins, st.as_dict()) if stats else joins
+
+    def nj_dev(self, d_D: int, n: int, ld: int, stats: bool = False):
+        from ._native import JOIN_DTYPE, NJStats
+        joins = np.zeros(max(n - 1, 1), dtype=np.dtype(JOIN_DTYPE))
+        st = NJStats()
+        self._check(self._lib.nwg_nj_dev(self.h, ctypes.c_void_p(d_D), ld, n,
+                                         joins.ctypes.data_as(ctypes.c_void_p), ctypes.byref(st)))
+        joins = joins[: max(n - 1, 0)]
+        return (joins, st.as_dict()) if stats else joins
+
     def score_pairs(self, codes, offsets, pi, pj):
         """Scores of explicit pairs (int32 lanes, one thread per pair)."""
         pi = np.ascontiguousarray(pi, dtype=np.int32)
@@ -183,6 +227,35 @@ class Context:
                                               len(offsets) - 1, _p(pi, c_i32p), _p(pj, c_i32p), len(pi),
                                               _p(out, c_i32p), None))
         return out
+
+
+def cherries(left, right, n_leaves: int):
+    """(node, left, right) of every guide-tree cherry in getNodes post-order."""
+    left = np.ascontiguousarray(left, dtype=np.int32)
+    right = np.ascontiguousarray(right, dtype=np.int32)
+    n = lib().nwg_cherries(_p(left, c_i32p), _p(right, c_i32p), n_leaves, None, None, None)
+    if n < 0:
+        raise NWGError(-n, "nwg_cherries")
+    node = np.zeros(max(n, 1), dtype=np.int32)
+    l = np.zeros(max(n, 1), dtype=np.int32)
+    r = np.zeros(max(n, 1), dtype=np.int32)
+    lib().nwg_cherries(_p(left, c_i32p), _p(right, c_i32p), n_leaves, _p(node, c_i32p), _p(l, c_i32p),
+                       _p(r, c_i32p))
+    return node[:n], l[:n], r[:n]
+
+
+def newick(joins, names) -> str:
+    """The reference's .tree text (TreeNode::buildTreeOutput + ";\\n")."""
+    from ._native import JOIN_DTYPE
+    j = np.ascontiguousarray(joins, dtype=np.dtype(JOIN_DTYPE))
+    n = len(names)
+    arr = (ctypes.c_char_p * n)(*[x.encode() if isinstance(x, str) else bytes(x) for x in names])
+    need = lib().nwg_newick(j.ctypes.data_as(ctypes.c_void_p), n, arr, None, 0)
+    if need < 0:
+        raise NWGError(int(-need), "nwg_newick")
+    buf = ctypes.create_string_buffer(int(need) + 1)
+    lib().nwg_newick(j.ctypes.data_as(ctypes.c_void_p), n, arr, buf, need + 1)
+    return buf.value.decode()
 
 
 class AlignmentScore:

@@ -1,0 +1,72 @@
+"""Device neighbor joining against the reference's own buildTree (golden join
+lists made by SpeciesBlock.cpp compiled through the one-rank MPI shim) and
+against the oracle restatement."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle_py as O
+from mestrado_gb300 import newick, synth
+from fasta import read_fasta
+from test_nj_cpu import golden_joins
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _same(j, ref):
+    assert len(j) == len(ref)
+    for a, b in zip(j, ref):
+        assert (a["node"], a["i"], a["j"]) == (b["node"], b["i"], b["j"])
+        assert a["len_i"] == b["len_i"] and a["len_j"] == b["len_j"]
+
+
+@pytest.mark.parametrize("case", ["cfg0", "nj300", "nj1200"])
+def test_device_nj_matches_reference_tree(ctx, case):
+    d = os.path.join(GOLD, case)
+    names, seqs = read_fasta(os.path.join(d, "input.fasta"))
+    D = ctx.score_all(seqs)
+    meta = json.load(open(os.path.join(d, "meta.json")))
+    assert hashlib.sha256(D.tobytes()).hexdigest() == meta["D_sha256"]
+    joins, st = ctx.nj(D, stats=True)
+    _same(joins, golden_joins(case))
+    assert newick(joins, names) == open(os.path.join(d, "tree.nwk")).read()
+    assert st["ambiguous_steps"] == 0 and st["pq_trigger_open"] == 0
+
+
+@pytest.mark.parametrize("seed,n", [(1, 2), (2, 3), (3, 17), (4, 64), (5, 257), (6, 600)])
+def test_device_nj_matches_oracle(ctx, seed, n):
+    S = synth.family(n, 90, ps=0.1, pi=0.01, seed=seed)
+    D = ctx.score_all(S)
+    joins, st = ctx.nj(D, stats=True)
+    oj, ost = O.nj(D)
+    assert len(joins) == len(oj)
+    for a, b in zip(joins, oj):
+        assert (a["i"], a["j"], a["node"], a["n"]) == (b["i"], b["j"], b["node"], b["n"])
+        assert (a["len_i"], a["len_j"], a["q"], a["ti"], a["tj"]) == (b["len_i"], b["len_j"], b["q"], b["ti"], b["tj"])
+    assert st["ambiguous_steps"] == ost["ambiguous_steps"]
+    assert st["tie_steps"] == ost["tie_steps"]
+    assert st["rebuilds"] == ost["rebuilds"]
+
+
+def test_device_nj_ties_and_duplicates(ctx):
+    # identical sequences and a small integer matrix with many exact ties
+    S = synth.family(40, 60, ps=0.02, pi=0.0, seed=9)
+    seqs = [S[i] for i in range(len(S))] + [S[0], S[0], S[1]]
+    D = ctx.score_all(seqs)
+    joins, st = ctx.nj(D, stats=True)
+    oj, ost = O.nj(D)
+    for a, b in zip(joins, oj):
+        assert (a["i"], a["j"], a["len_i"], a["len_j"]) == (b["i"], b["j"], b["len_i"], b["len_j"])
+    assert st["tie_steps"] == ost["tie_steps"] and st["ambiguous_steps"] == ost["ambiguous_steps"]
+    rng = np.random.default_rng(0)
+    M = rng.integers(0, 5, size=(30, 30)).astype(np.float32)
+    M = np.triu(M, 1) + np.triu(M, 1).T
+    joins, st = ctx.nj(M, stats=True)
+    oj, ost = O.nj(M)
+    for a, b in zip(joins, oj):
+        assert (a["i"], a["j"], a["len_i"], a["len_j"]) == (b["i"], b["j"], b["len_i"], b["len_j"])
+    assert st["ambiguous_steps"] == ost["ambiguous_steps"]

@@ -1,0 +1,52 @@
+"""Traceback kernels against the oracle restatement of the match/back kernels."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle_py as O
+from mestrado_gb300 import cherries, encode, synth
+from fasta import read_fasta
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _rand_set(seed, n, lo, hi, alphabet=b"ARNDCQEGHILKMFPSTWYV"):
+    rng = np.random.default_rng(seed)
+    letters = np.frombuffer(alphabet, dtype=np.uint8)
+    lens = rng.integers(lo, hi + 1, size=n)
+    return [letters[rng.integers(0, len(letters), L)].tobytes() for L in lens]
+
+
+def _check(ctx, seqs, px, py):
+    codes, off = encode(seqs)
+    out = ctx.align_pairs(codes, off, px, py)
+    for (ax, ay, s), i, j in zip(out, px, py):
+        rx, ry, rs = O.traceback(seqs[i], seqs[j])
+        assert (ax, ay, s) == (rx, ry, rs), (i, j)
+
+
+def test_random_pairs_short_and_multiband(ctx):
+    seqs = _rand_set(5, 30, 1, 700) + _rand_set(6, 4, 1, 20, alphabet=b"ARNDCQEGHILKMFPSTWYVBZX*")
+    rng = np.random.default_rng(2)
+    px, py = rng.integers(0, len(seqs), 80), rng.integers(0, len(seqs), 80)
+    _check(ctx, seqs, px, py)
+
+
+def test_related_and_identical_pairs(ctx):
+    S = synth.family(20, 300, ps=0.1, pi=0.03, seed=8)
+    seqs = [S[i] for i in range(len(S))] + [S[0]]
+    px = np.arange(0, 20)
+    py = np.array(list(range(1, 20)) + [20])
+    _check(ctx, seqs, px, py)
+
+
+@pytest.mark.parametrize("case", ["cfg0", "nj300"])
+def test_cherries_of_reference_tree(ctx, case):
+    names, seqs = read_fasta(os.path.join(GOLD, case, "input.fasta"))
+    rows = [l.split() for l in open(os.path.join(GOLD, case, "joins.txt"))]
+    left = np.array([int(r[1]) for r in rows], dtype=np.int32)
+    right = np.array([int(r[2]) for r in rows], dtype=np.int32)
+    node, l, r = cherries(left, right, len(seqs))
+    _check(ctx, seqs, l, r)
