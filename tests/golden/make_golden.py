@@ -40,7 +40,12 @@ CASES = {
     "nj300": lambda: synth.family(300, 120, ps=0.05, pi=0.005, seed=11),
     # 1200 short sequences in 6 families: rebuilds at 600, 300, 150 active
     "nj1200": lambda: synth.family(200, 60, ps=0.08, pi=0.005, families=6, seed=12),
+    # benchmark configuration 3: 8000 sequences, 40 families, uniform root
+    # lengths 100-300 (integer-only generator path: regenerated identically
+    # on x86-64 and aarch64, so the input itself is not stored)
+    "cfg3": lambda: synth.config(3),
 }
+NO_INPUT = {"cfg3"}
 
 
 def build_ref():
@@ -55,6 +60,7 @@ def make(name: str) -> None:
     os.makedirs(out, exist_ok=True)
     fasta = os.path.join(out, "input.fasta")
     S.to_fasta(fasta)
+    keep_input = name not in NO_INPUT
     D = oracle_py.score_all(S, threads=os.cpu_count() or 4)
     ref = build_ref()
     with tempfile.TemporaryDirectory() as td:
@@ -90,9 +96,11 @@ def make(name: str) -> None:
     }
     if n <= 128:
         np.save(os.path.join(out, "D.npy"), D)
+    if not keep_input:
+        os.remove(fasta)
     with open(os.path.join(out, "meta.json"), "w") as f:
         json.dump(meta, f)
-    print(name, n, "joins", joins.count("\n"))
+    print(name, n, "joins", joins.count("\n"), flush=True)
 
 
 if __name__ == "__main__":
