@@ -183,6 +183,32 @@ int nwg_nj_dev(nwg_ctx* ctx, const float* d_D, int64_t ld, int n, nwg_join* join
  * length, or a negative status. */
 int64_t nwg_newick(const nwg_join* joins, int n, const char* const* names, char* out, int64_t cap);
 
+/* ---- pair scoring without allocation ---------------------------------------
+ * No counterpart in the reference: an entry point for hosts that cannot let a
+ * library call cudaMalloc or cudaFree -- code running while a stream is
+ * captured in the global capture mode, or hosts that hand out all device
+ * memory from their own pool and must not have a cudaFree synchronize the
+ * device under them.  Same scores as nwg_score_pairs (one pair per thread,
+ * int32), but every input and output is caller-provided device memory, no
+ * context is used, and the only work memory is a fixed 32 MiB static device
+ * array that every GPU loading the library holds until exit.
+ *
+ *   d_codes/d_start/d_len: reversed codes and per-sequence start and length;
+ *   d_pi/d_pj: npairs valid sequence indices; d_out: npairs scores (INT_MIN
+ *   for a pair whose X is longer than max_len or has an empty sequence);
+ *   max_len: the longest X of the call, at most 32768 (larger values are
+ *   rejected with NWG_ERR_INVALID); d_sub: 576-entry device matrix or NULL for
+ *   the built-in one; stream: cudaStream_t or NULL.
+ *
+ * The first call on a device looks the static array up (cudaGetSymbolAddress)
+ * with that device current; make it before any stream capture.  All calls on
+ * a device share the array and it keeps the last call's contents (nothing in
+ * it needs to start at zero); calls whose kernels overlap on the GPU race on
+ * it and must be serialized.  Returns once the kernel is queued. */
+int nwg_score_pairs_noalloc(const int8_t* d_codes, const int64_t* d_start, const int32_t* d_len,
+                            const int32_t* d_pi, const int32_t* d_pj, int64_t npairs, int32_t* d_out,
+                            int max_len, int gap_open, int gap_ext, const int8_t* d_sub, void* stream);
+
 /* ---- measurement ---------------------------------------------------------
  * Not part of the reference's interface (the reference times nothing on the
  * device; timer.h falls back to clock()).  These give the bench its roofline
