@@ -29,11 +29,16 @@
 // since the last build; that bound is tracked and any check it cannot exclude
 // is counted.
 //
-// Search: RapidNJ-style.  Every row slot keeps its partners sorted by d
-// (ascending) when the row is made; a row is scanned in that order while the
-// lower bound d*(n-2) - T_row - T_max (minus a rounding margin) stays at or
-// under the current upper bound, so a step touches a few entries per row
-// instead of the whole matrix.  All floating-point operations use the _rn
+// Search per join, two streaming passes over the live triangle of D (HBM
+// bound: 2n^2 bytes per pass):
+//  1. q in float, fl(fl(fl(d*(n-2)) - Tf_r) - Tf_c) with Tf the float copy of
+//     T: its minimum and the largest magnitude M = |d|(n-2) + |T_r| + |T_c|.
+//     Every float q is within E = 8 * 2^-24 * M of the exact q.
+//  2. every pair whose float q is at most min + 3E gets its exact double q in
+//     both roundings; those candidates (typically a handful) go to a list.
+// A single CTA then takes the winner with the tie-break and runs the
+// ambiguity check on the list: any pair left out has q > winner + E, beyond
+// reach of either rounding.  All floating-point operations use the _rn
 // intrinsics in the reference's evaluation order (no contraction).
 #include <algorithm>
 #include <cfloat>
@@ -47,39 +52,43 @@ namespace nwg {
 
 namespace {
 
-constexpr int kNJMaxN = 8192;          // row sort in shared memory
-constexpr int kScanWarps = 8;
-
-struct Entry {
-  float d;
-  int v;
-};
+constexpr int kNJMaxN = 8192;
+constexpr int kCandCap = 1 << 16;      // candidate list capacity per join
 
 struct Pick {
   double q1, q2;
   int a, b;      // a < b node ids
 };
 
+struct Cand {
+  double q1, q2;
+  int a, b;
+};
+
 struct NJDev {
   float* D;            // n0 x n0, slots
   double* T;           // per slot
+  float* Tf;           // per slot, (float)T
   int* slot;           // per node id (2n0-1), -1 dead
-  int* act;            // active node ids ascending [n0]
+  int* node;           // per slot: node id, -1 dead
+  int* act;            // active node ids ascending [n0 + 1]
   int* na;             // active count
-  Entry* rows;         // per slot: n0 entries
-  int* rowlen;         // per slot
-  int* head;           // per slot: first entry that may be live
-  double* rq;          // per active index: best q1 of the row
-  int* ra;             // per active index: best pair a
-  int* rb;             // per active index: best pair b
-  double* gl;          // [0] T max, [1] upper bound, [2] hi of winner
+  int* g32;            // [0] min float q (ordered int), [1] max magnitude (ordered int), [2] candidates
+  Cand* cand;          // candidate list
   Pick* win;
-  unsigned long long* cnt;   // [0] ties (this step), [1] ambiguous pairs (this step)
-  unsigned long long* stats; // [0] ambiguous steps, [1] tie steps
+  unsigned long long* stats;  // [0] ambiguous steps, [1] tie steps, [2] internal errors
   nwg_join* joins;
   float* vd;           // per slot, new row values
   int n0;
 };
+
+__device__ __forceinline__ int ford(float f) {
+  // order-preserving map float -> int (for atomicMin / atomicMax)
+  const int b = __float_as_int(f);
+  return b >= 0 ? b : b ^ 0x7FFFFFFF;
+}
+
+__device__ __forceinline__ float iord(int b) { return __int_as_float(b >= 0 ? b : b ^ 0x7FFFFFFF); }
 
 __device__ __forceinline__ bool better(double q, int b, int a, double q2, int b2, int a2) {
   if (q < q2) return true;
@@ -88,8 +97,7 @@ __device__ __forceinline__ bool better(double q, int b, int a, double q2, int b2
 }
 
 // q as the reference's candidate list computes it (record order).
-__device__ __forceinline__ double q_record(const NJDev& s, float d, int u, int v, int watermark, double nm2) {
-  const int a = min(u, v), b = max(u, v);
+__device__ __forceinline__ double q_record(const NJDev& s, float d, int a, int b, int watermark, double nm2) {
   const int sa = s.slot[a], sb = s.slot[b];
   int f = sa, g = sb;
   if (b >= watermark && sb < sa) {
@@ -99,173 +107,143 @@ __device__ __forceinline__ double q_record(const NJDev& s, float d, int u, int v
   return __dsub_rn(__dsub_rn(__dmul_rn((double)d, nm2), s.T[f]), s.T[g]);
 }
 
-__device__ __forceinline__ double q_heap(const NJDev& s, float d, int u, int v, double nm2) {
-  return __dsub_rn(__dmul_rn((double)d, nm2), __dadd_rn(s.T[s.slot[u]], s.T[s.slot[v]]));
+__device__ __forceinline__ double q_heap(const NJDev& s, float d, int a, int b, double nm2) {
+  return __dsub_rn(__dmul_rn((double)d, nm2), __dadd_rn(s.T[s.slot[a]], s.T[s.slot[b]]));
 }
 
-// rounding margin of the lower bound: generous multiple of the double ulp
-__device__ __forceinline__ double margin(double x, double tu, double tmax) {
-  return 1e-12 * (fabs(x) + fabs(tu) + fabs(tmax)) + 1e-300;
+// Exponent of the lowest set bit of a nonzero float (INT_MAX for zero).
+__device__ __forceinline__ int low_bit_exp(float f) {
+  const unsigned b = __float_as_uint(f) & 0x7FFFFFFFu;
+  if (b == 0) return INT_MAX;
+  const unsigned e = b >> 23, m = b & 0x7FFFFFu;
+  if (e == 0) return -149 + __ffs(m) - 1;
+  return (int)e - 150 + __ffs(m | 0x800000u) - 1;
 }
 
-// Sequential row sums (buildGblRowSums): one thread per active row.
+// A sequential double sum of floats equals any-order sum when every partial
+// sum is exact: all terms are multiples of 2^lowexp and sum|x| < 2^(53+lowexp)
+// (a multiple of 2^lowexp below that magnitude has at most 53 significant
+// bits).  absum is itself a rounded sum, hence the 1e-12 slack.
+__device__ __forceinline__ bool sum_is_exact(double absum, int lowexp) {
+  if (lowexp == INT_MAX) return true;   // every term is zero
+  return absum * (1.0 + 1e-12) < ldexp(1.0, 53 + lowexp);
+}
+
+// Sequential row sums (buildGblRowSums): one warp per active row; the lanes'
+// any-order sum is used when it is provably exact, else lane 0 sums in order.
 __global__ void rowsum_kernel(NJDev s) {
   const int na = *s.na;
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (k >= na) return;
-  const float* row = s.D + (size_t)s.slot[s.act[k]] * s.n0;
-  double sum = 0.0;
-  for (int j = 0; j < na; ++j) sum = __dadd_rn(sum, (double)row[s.slot[s.act[j]]]);
-  s.T[s.slot[s.act[k]]] = sum;
-}
-
-// Bitonic sort of (d, v) pairs in shared memory, n <= kNJMaxN (padded).
-__device__ void block_sort(Entry* e, int n) {
-  int m = 1;
-  while (m < n) m <<= 1;
-  for (int k = n + threadIdx.x; k < m; k += blockDim.x) e[k] = Entry{FLT_MAX, INT_MAX};
-  __syncthreads();
-  for (int size = 2; size <= m; size <<= 1) {
-    for (int stride = size >> 1; stride > 0; stride >>= 1) {
-      for (int t = threadIdx.x; t < m / 2; t += blockDim.x) {
-        const int i = 2 * t - (t & (stride - 1));
-        const int j = i + stride;
-        const bool up = (i & size) == 0;
-        const Entry A = e[i], B = e[j];
-        const bool gt = A.d > B.d || (A.d == B.d && A.v > B.v);
-        if (gt == up) {
-          e[i] = B;
-          e[j] = A;
-        }
-      }
-      __syncthreads();
-    }
-  }
-}
-
-// Sorted partner list of every leaf row (initial rows).
-__global__ void init_rows_kernel(NJDev s) {
-  extern __shared__ Entry sh[];
-  const int u = blockIdx.x;
-  const int n = s.n0;
-  int cnt = 0;
-  for (int v = threadIdx.x; v < n; v += blockDim.x) {
-    const int k = v < u ? v : v - 1;
-    if (v != u) sh[k] = Entry{s.D[(size_t)u * n + v], v};
-  }
-  cnt = n - 1;
-  __syncthreads();
-  block_sort(sh, cnt);
-  for (int k = threadIdx.x; k < cnt; k += blockDim.x) s.rows[(size_t)u * n + k] = sh[k];
-  if (threadIdx.x == 0) {
-    s.rowlen[u] = cnt;
-    s.head[u] = 0;
-  }
-}
-
-// T max over active rows and a first upper bound: the q of every row's first
-// live partner (dead entries at a row's head are skipped for good).
-__global__ void prepare_kernel(NJDev s, int watermark, double nm2) {
-  __shared__ double red_t[32], red_u[32];
-  const int na = *s.na;
-  double tmax = -DBL_MAX, ub = DBL_MAX;
-  for (int k = threadIdx.x; k < na; k += blockDim.x) {
-    const int u = s.act[k];
-    const int su = s.slot[u];
-    tmax = fmax(tmax, s.T[su]);
-    const Entry* row = s.rows + (size_t)su * s.n0;
-    int h = s.head[su];
-    const int len = s.rowlen[su];
-    while (h < len && s.slot[row[h].v] < 0) ++h;
-    s.head[su] = h;
-    if (h < len) ub = fmin(ub, q_record(s, row[h].d, u, row[h].v, watermark, nm2));
+  const int sk = s.slot[s.act[k]];
+  const float* row = s.D + (size_t)sk * s.n0;
+  double part = 0.0, ab = 0.0;
+  int lowexp = INT_MAX;
+  for (int j = lane; j < na; j += 32) {
+    const float x = row[s.slot[s.act[j]]];
+    part = __dadd_rn(part, (double)x);
+    ab = __dadd_rn(ab, (double)fabsf(x));
+    lowexp = min(lowexp, low_bit_exp(x));
   }
   for (int o = 16; o > 0; o >>= 1) {
-    tmax = fmax(tmax, __shfl_down_sync(0xffffffffu, tmax, o));
-    ub = fmin(ub, __shfl_down_sync(0xffffffffu, ub, o));
+    part = __dadd_rn(part, __shfl_down_sync(0xffffffffu, part, o));
+    ab = __dadd_rn(ab, __shfl_down_sync(0xffffffffu, ab, o));
+    lowexp = min(lowexp, __shfl_down_sync(0xffffffffu, lowexp, o));
   }
+  if (lane == 0) {
+    double sum = part;
+    if (!sum_is_exact(ab, lowexp)) {
+      sum = 0.0;
+      for (int j = 0; j < na; ++j) sum = __dadd_rn(sum, (double)row[s.slot[s.act[j]]]);
+    }
+    s.T[sk] = sum;
+    s.Tf[sk] = (float)sum;
+  }
+}
+
+// Pass 1: minimum float q and largest magnitude over the live triangle
+// (row slot r, column slots c > r).
+__global__ void __launch_bounds__(256) pass_min_kernel(NJDev s, float nm2f) {
+  if ((int)blockIdx.x >= *s.na) return;
+  const int r = s.slot[s.act[blockIdx.x]];
+  const float tr = s.Tf[r];
+  const float* row = s.D + (size_t)r * s.n0;
+  float qmin = FLT_MAX, mmax = 0.f;
+  for (int c = r + 1 + threadIdx.x; c < s.n0; c += blockDim.x) {
+    if (s.node[c] < 0) continue;
+    const float d = row[c];
+    const float tc = s.Tf[c];
+    const float x = __fmul_rn(d, nm2f);
+    const float q = __fsub_rn(__fsub_rn(x, tr), tc);
+    qmin = fminf(qmin, q);
+    mmax = fmaxf(mmax, __fadd_rn(__fadd_rn(fabsf(x), fabsf(tr)), fabsf(tc)));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    qmin = fminf(qmin, __shfl_down_sync(0xffffffffu, qmin, o));
+    mmax = fmaxf(mmax, __shfl_down_sync(0xffffffffu, mmax, o));
+  }
+  __shared__ float sq[8], sm[8];
   if ((threadIdx.x & 31) == 0) {
-    red_t[threadIdx.x >> 5] = tmax;
-    red_u[threadIdx.x >> 5] = ub;
+    sq[threadIdx.x >> 5] = qmin;
+    sm[threadIdx.x >> 5] = mmax;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
-      tmax = fmax(tmax, red_t[w]);
-      ub = fmin(ub, red_u[w]);
+      qmin = fminf(qmin, sq[w]);
+      mmax = fmaxf(mmax, sm[w]);
     }
-    tmax = fmax(tmax, red_t[0]);
-    ub = fmin(ub, red_u[0]);
-    s.gl[0] = tmax;
-    s.gl[1] = ub;
-    s.cnt[0] = 0;
-    s.cnt[1] = 0;
+    if (qmin < FLT_MAX) {
+      atomicMin(&s.g32[0], ford(qmin));
+      atomicMax(&s.g32[1], ford(mmax));
+    }
   }
 }
 
-// Phase 1: best pair of every active row among entries whose lower bound is
-// at most the upper bound.
-__global__ void __launch_bounds__(32 * kScanWarps) scan_kernel(NJDev s, int watermark, double nm2) {
-  const int lane = threadIdx.x & 31;
-  const int k = blockIdx.x * kScanWarps + (threadIdx.x >> 5);
-  const int na = *s.na;
-  if (k >= na) return;
-  const int u = s.act[k];
-  const int su = s.slot[u];
-  const double tu = s.T[su], tmax = s.gl[0], ub = s.gl[1];
-  const Entry* row = s.rows + (size_t)su * s.n0;
-  const int len = s.rowlen[su];
-  double bq = DBL_MAX;
-  int ba = INT_MAX, bb = -1;
-  for (int base = s.head[su]; base < len; base += 32) {
-    const int e = base + lane;
-    bool go_on = false;
-    if (e < len) {
-      const Entry en = row[e];
-      const double x = __dmul_rn((double)en.d, nm2);
-      const double lb = __dsub_rn(__dsub_rn(x, tu), tmax);
-      go_on = lb - margin(x, tu, tmax) <= ub;
-      if (go_on && s.slot[en.v] >= 0) {
-        const double q = q_record(s, en.d, u, en.v, watermark, nm2);
-        const int a = min(u, en.v), b = max(u, en.v);
-        if (better(q, b, a, bq, bb, ba)) {
-          bq = q;
-          ba = a;
-          bb = b;
-        }
-      }
-    }
-    if (!__any_sync(0xffffffffu, go_on)) break;
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    const double q2 = __shfl_down_sync(0xffffffffu, bq, o);
-    const int a2 = __shfl_down_sync(0xffffffffu, ba, o);
-    const int b2 = __shfl_down_sync(0xffffffffu, bb, o);
-    if (better(q2, b2, a2, bq, bb, ba)) {
-      bq = q2;
-      ba = a2;
-      bb = b2;
-    }
-  }
-  if (lane == 0) {
-    s.rq[k] = bq;
-    s.ra[k] = ba;
-    s.rb[k] = bb;
+// Pass 2: exact double q (both roundings) of every pair whose float q is
+// within min + 3E.
+__global__ void __launch_bounds__(256) pass_cand_kernel(NJDev s, float nm2f, double nm2, int watermark) {
+  if ((int)blockIdx.x >= *s.na) return;
+  const int ur = s.act[blockIdx.x];
+  const int r = s.slot[ur];
+  const float qmin = iord(s.g32[0]);
+  const float mmax = iord(s.g32[1]);
+  const float thr = qmin + 3.f * (8.f * 5.9604645e-8f * mmax) + 1e-30f;
+  const float tr = s.Tf[r];
+  const float* row = s.D + (size_t)r * s.n0;
+  for (int c = r + 1 + threadIdx.x; c < s.n0; c += blockDim.x) {
+    const int uc = s.node[c];
+    if (uc < 0) continue;
+    const float d = row[c];
+    const float q = __fsub_rn(__fsub_rn(__fmul_rn(d, nm2f), tr), s.Tf[c]);
+    if (q > thr) continue;
+    const int a = min(ur, uc), b = max(ur, uc);
+    Cand cd;
+    cd.q1 = q_record(s, d, a, b, watermark, nm2);
+    cd.q2 = q_heap(s, d, a, b, nm2);
+    cd.a = a;
+    cd.b = b;
+    const int k = atomicAdd(&s.g32[2], 1);
+    if (k < kCandCap) s.cand[k] = cd;
   }
 }
 
-// Winner over rows, and the bound of the ambiguity pass.
-__global__ void pick_kernel(NJDev s, double nm2) {
+// Winner among the candidates, ambiguity and tie count; resets the pass
+// accumulators for the next join.
+__global__ void __launch_bounds__(1024) pick_kernel(NJDev s) {
   __shared__ double sq[32];
   __shared__ int sa[32], sb[32];
-  const int na = *s.na;
+  __shared__ unsigned s_ties, s_amb;
+  const int nc = min(s.g32[2], kCandCap);
   double bq = DBL_MAX;
   int ba = INT_MAX, bb = -1;
-  for (int k = threadIdx.x; k < na; k += blockDim.x) {
-    if (s.rb[k] >= 0 && better(s.rq[k], s.rb[k], s.ra[k], bq, bb, ba)) {
-      bq = s.rq[k];
-      ba = s.ra[k];
-      bb = s.rb[k];
+  for (int k = threadIdx.x; k < nc; k += blockDim.x) {
+    const Cand c = s.cand[k];
+    if (better(c.q1, c.b, c.a, bq, bb, ba)) {
+      bq = c.q1;
+      ba = c.a;
+      bb = c.b;
     }
   }
   for (int o = 16; o > 0; o >>= 1) {
@@ -283,6 +261,10 @@ __global__ void pick_kernel(NJDev s, double nm2) {
     sa[threadIdx.x >> 5] = ba;
     sb[threadIdx.x >> 5] = bb;
   }
+  if (threadIdx.x == 0) {
+    s_ties = 0;
+    s_amb = 0;
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
@@ -291,77 +273,61 @@ __global__ void pick_kernel(NJDev s, double nm2) {
         ba = sa[w];
         bb = sb[w];
       }
+    sq[0] = bq;
+    sa[0] = ba;
+    sb[0] = bb;
+  }
+  __syncthreads();
+  bq = sq[0];
+  ba = sa[0];
+  bb = sb[0];
+  double q2w = DBL_MAX;
+  for (int k = 0; k < nc; ++k) {   // the winner's heap value (the list is short)
+    const Cand c = s.cand[k];
+    if (c.a == ba && c.b == bb) {
+      q2w = c.q2;
+      break;
+    }
+  }
+  const double hiw = fmax(bq, q2w);
+  const bool robust_w = bq == q2w;
+  unsigned ties = 0, amb = 0;
+  for (int k = threadIdx.x; k < nc; k += blockDim.x) {
+    const Cand c = s.cand[k];
+    const double lo = fmin(c.q1, c.q2);
+    if (lo > hiw) continue;
+    if (c.a == ba && c.b == bb) ++ties;
+    else if (robust_w && c.q1 == c.q2 && c.q1 == bq) ++ties;
+    else ++amb;
+  }
+  if (ties) atomicAdd(&s_ties, ties);
+  if (amb) atomicAdd(&s_amb, amb);
+  __syncthreads();
+  if (threadIdx.x == 0) {
     Pick p;
     p.q1 = bq;
+    p.q2 = q2w;
     p.a = ba;
     p.b = bb;
-    if (bb < 0) {            // no candidate: cannot happen with >= 2 active nodes
-      atomicAdd(&s.stats[2], 1ull);
-      *s.win = p;
-      s.gl[2] = -DBL_MAX;
-      return;
-    }
-    const float d = s.D[(size_t)s.slot[ba] * s.n0 + s.slot[bb]];
-    p.q2 = q_heap(s, d, ba, bb, nm2);
     *s.win = p;
-    s.gl[2] = fmax(p.q1, p.q2);
+    if (bb < 0 || s.g32[2] > kCandCap) atomicAdd(&s.stats[2], 1ull);   // no candidate / list overflow
+    else if (s_amb > 0 || s_ties > 4) atomicAdd(&s.stats[0], 1ull);
+    else if (s_ties > 1) atomicAdd(&s.stats[1], 1ull);
+    s.g32[0] = 0x7F7FFFFF;          // ordered-int of FLT_MAX
+    s.g32[1] = 0;
+    s.g32[2] = 0;
   }
 }
 
-// Phase 2: could the heap rounding of another pair, or a wide exact tie,
-// change the reference's pick?  Each pair is counted from the row of its
-// larger id (that row always holds it).
-__global__ void __launch_bounds__(32 * kScanWarps) ambiguity_kernel(NJDev s, int watermark, double nm2) {
-  const int lane = threadIdx.x & 31;
-  const int k = blockIdx.x * kScanWarps + (threadIdx.x >> 5);
-  const int na = *s.na;
-  if (k >= na) return;
-  const int u = s.act[k];
-  const int su = s.slot[u];
-  const double tu = s.T[su], tmax = s.gl[0], hi = s.gl[2];
-  const Pick w = *s.win;
-  if (w.b < 0) return;
-  const bool robust_w = w.q1 == w.q2;
-  const Entry* row = s.rows + (size_t)su * s.n0;
-  const int len = s.rowlen[su];
-  unsigned ties = 0, amb = 0;
-  for (int base = s.head[su]; base < len; base += 32) {
-    const int e = base + lane;
-    bool go_on = false;
-    if (e < len) {
-      const Entry en = row[e];
-      const double x = __dmul_rn((double)en.d, nm2);
-      const double lb = __dsub_rn(__dsub_rn(x, tu), tmax);
-      go_on = lb - margin(x, tu, tmax) <= hi;
-      if (go_on && en.v < u && s.slot[en.v] >= 0) {
-        const int a = en.v, b = u;
-        const double q1 = q_record(s, en.d, u, en.v, watermark, nm2);
-        const double q2 = q_heap(s, en.d, u, en.v, nm2);
-        const double lo = fmin(q1, q2);
-        if (lo <= hi) {
-          if (a == w.a && b == w.b) ++ties;
-          else if (robust_w && q1 == q2 && q1 == w.q1) ++ties;
-          else ++amb;
-        }
-      }
-    }
-    if (!__any_sync(0xffffffffu, go_on)) break;
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    ties += __shfl_down_sync(0xffffffffu, ties, o);
-    amb += __shfl_down_sync(0xffffffffu, amb, o);
-  }
-  if (lane == 0) {
-    if (ties) atomicAdd(&s.cnt[0], (unsigned long long)ties);
-    if (amb) atomicAdd(&s.cnt[1], (unsigned long long)amb);
-  }
-}
-
-// The join: record, modifyMatrix, new sorted row, active list.  One CTA.
-__global__ void join_kernel(NJDev s, int step, int next, int m_n) {
-  extern __shared__ Entry sh[];
+// The join: record, modifyMatrix, active list.  One CTA.
+__global__ void __launch_bounds__(1024) join_kernel(NJDev s, int step, int next, int m_n) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* tv = reinterpret_cast<float*>(smem_raw);                        // tmp by active index
+  int* ids = reinterpret_cast<int*>(smem_raw + sizeof(float) * s.n0);    // compacted active list
   __shared__ int s_pos[1024 / 32 + 1];
-  __shared__ float s_tmp_dummy;
+  __shared__ int s_skip[2];
+  __shared__ double s_part[32], s_ab[32];
+  __shared__ int s_low[32];
   const Pick w = *s.win;
   if (w.b < 0) return;                 // counted as an internal error by pick_kernel
   const int i = w.a, j = w.b;          // i < j
@@ -369,7 +335,6 @@ __global__ void join_kernel(NJDev s, int step, int next, int m_n) {
   const int n0 = s.n0;
   const int na = *s.na;
   const float dmin = s.D[(size_t)si * n0 + sj];
-  (void)s_tmp_dummy;
   if (threadIdx.x == 0) {
     // TreeNode::join with left = min id, right = max id
     const double Ti = s.T[si], Tj = s.T[sj];
@@ -395,41 +360,77 @@ __global__ void join_kernel(NJDev s, int step, int next, int m_n) {
     J.node = next;
     J.n = m_n;
     J.d = dmin;
+    J.pad = 0.f;
     J.q = w.q1;
     J.ti = Ti;
     J.tj = Tj;
     J.len_i = li;
     J.len_j = lj;
-    const unsigned long long ties = s.cnt[0], amb = s.cnt[1];
-    if (amb > 0 || ties > 4) atomicAdd(&s.stats[0], 1ull);
-    else if (ties > 1) atomicAdd(&s.stats[1], 1ull);
   }
   __syncthreads();
-  // new row values, T updates, D row/column of slot si (k over active, k != i, j)
+  // new row values and T updates over active k != i, j (SpeciesBlock.cpp:787-817)
   for (int k = threadIdx.x; k < na; k += blockDim.x) {
     const int v = s.act[k];
-    if (v == i || v == j) continue;
+    if (v == i || v == j) {
+      s_skip[v == i ? 0 : 1] = k;
+      tv[k] = 0.f;
+      continue;
+    }
     const int sk = s.slot[v];
     const float Dik = s.D[(size_t)si * n0 + sk];
     const float Djk = s.D[(size_t)sj * n0 + sk];
     const float sumf = __fadd_rn(Dik, Djk);
     const float tmp = __fmul_rn(__fsub_rn(sumf, dmin), 0.5f);
     s.vd[sk] = tmp;
-    s.T[sk] = __dadd_rn(s.T[sk], (double)__fsub_rn(tmp, sumf));
+    tv[k] = tmp;
+    const double t = __dadd_rn(s.T[sk], (double)__fsub_rn(tmp, sumf));
+    s.T[sk] = t;
+    s.Tf[sk] = (float)t;
   }
   __syncthreads();
-  // sequential sum of tmp in ascending id order (SpeciesBlock.cpp:799)
-  if (threadIdx.x == 0) {
-    double sum = 0.0;
-    for (int k = 0; k < na; ++k) {
-      const int v = s.act[k];
-      if (v == i || v == j) continue;
-      sum = __dadd_rn(sum, (double)s.vd[s.slot[v]]);
+  // sum of tmp in ascending id order (SpeciesBlock.cpp:799, :818): the block's
+  // any-order sum when it is provably exact, else the sequential loop
+  {
+    double part = 0.0, ab = 0.0;
+    int lowexp = INT_MAX;
+    for (int k = threadIdx.x; k < na; k += blockDim.x) {
+      const float x = tv[k];            // 0 at i and j
+      part = __dadd_rn(part, (double)x);
+      ab = __dadd_rn(ab, (double)fabsf(x));
+      lowexp = min(lowexp, low_bit_exp(x));
     }
-    s.T[si] = sum;
+    for (int o = 16; o > 0; o >>= 1) {
+      part = __dadd_rn(part, __shfl_down_sync(0xffffffffu, part, o));
+      ab = __dadd_rn(ab, __shfl_down_sync(0xffffffffu, ab, o));
+      lowexp = min(lowexp, __shfl_down_sync(0xffffffffu, lowexp, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+      s_part[threadIdx.x >> 5] = part;
+      s_ab[threadIdx.x >> 5] = ab;
+      s_low[threadIdx.x >> 5] = lowexp;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      part = 0.0;
+      ab = 0.0;
+      lowexp = INT_MAX;
+      for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2) {
+        part = __dadd_rn(part, s_part[w2]);
+        ab = __dadd_rn(ab, s_ab[w2]);
+        lowexp = min(lowexp, s_low[w2]);
+      }
+      double sum = part;
+      if (!sum_is_exact(ab, lowexp)) {
+        const int ki = s_skip[0], kj = s_skip[1];
+        sum = 0.0;
+        for (int k = 0; k < na; ++k)
+          if (k != ki && k != kj) sum = __dadd_rn(sum, (double)tv[k]);
+      }
+      s.T[si] = sum;
+      s.Tf[si] = (float)sum;
+    }
   }
-  // D updates and the new node's sorted row (entries: all remaining active)
-  int cnt = 0;
+  // D row and column of slot si (:820-841; the diagonal keeps i's old value)
   for (int k = threadIdx.x; k < na; k += blockDim.x) {
     const int v = s.act[k];
     if (v == i || v == j) continue;
@@ -439,68 +440,51 @@ __global__ void join_kernel(NJDev s, int step, int next, int m_n) {
     s.D[(size_t)si * n0 + sk] = t;
   }
   // compacted active list: ascending ids without i, j, plus next at the end
-  {
-    // block-wide exclusive scan of keep flags over the ascending list
-    const int chunk = (na + blockDim.x - 1) / blockDim.x;
-    const int k0 = threadIdx.x * chunk;
-    int keep = 0;
-    for (int k = k0; k < k0 + chunk && k < na; ++k) keep += (s.act[k] != i && s.act[k] != j);
-    // warp scan
-    int incl = keep;
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, incl, o);
-      if ((threadIdx.x & 31) >= o) incl += y;
-    }
-    if ((threadIdx.x & 31) == 31) s_pos[threadIdx.x >> 5] = incl;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      int acc = 0;
-      for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2) {
-        const int t = s_pos[w2];
-        s_pos[w2] = acc;
-        acc += t;
-      }
-      s_pos[blockDim.x >> 5] = acc;
-    }
-    __syncthreads();
-    int pos = s_pos[threadIdx.x >> 5] + incl - keep;
-    // gather into shared first (reads of s.act must finish before writes)
-    int* tmp_ids = reinterpret_cast<int*>(sh);
-    for (int k = k0; k < k0 + chunk && k < na; ++k)
-      if (s.act[k] != i && s.act[k] != j) tmp_ids[pos++] = s.act[k];
-    __syncthreads();
-    cnt = s_pos[blockDim.x >> 5];
-    for (int k = threadIdx.x; k < cnt; k += blockDim.x) s.act[k] = tmp_ids[k];
-    __syncthreads();
+  const int chunk = (na + blockDim.x - 1) / blockDim.x;
+  const int k0 = threadIdx.x * chunk;
+  int keep = 0;
+  for (int k = k0; k < k0 + chunk && k < na; ++k) keep += (s.act[k] != i && s.act[k] != j);
+  int incl = keep;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if ((threadIdx.x & 31) >= o) incl += y;
   }
-  // sorted row of the new node in slot si
-  for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
-    const int v = s.act[k];
-    sh[k] = Entry{s.vd[s.slot[v]], v};
-  }
-  __syncthreads();
-  block_sort(sh, cnt);
-  for (int k = threadIdx.x; k < cnt; k += blockDim.x) s.rows[(size_t)si * n0 + k] = sh[k];
+  if ((threadIdx.x & 31) == 31) s_pos[threadIdx.x >> 5] = incl;
   __syncthreads();
   if (threadIdx.x == 0) {
-    s.rowlen[si] = cnt;
-    s.head[si] = 0;
+    int acc = 0;
+    for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2) {
+      const int t = s_pos[w2];
+      s_pos[w2] = acc;
+      acc += t;
+    }
+    s_pos[blockDim.x >> 5] = acc;
+  }
+  __syncthreads();
+  int pos = s_pos[threadIdx.x >> 5] + incl - keep;
+  for (int k = k0; k < k0 + chunk && k < na; ++k)
+    if (s.act[k] != i && s.act[k] != j) ids[pos++] = s.act[k];
+  __syncthreads();
+  const int cnt = s_pos[blockDim.x >> 5];
+  for (int k = threadIdx.x; k < cnt; k += blockDim.x) s.act[k] = ids[k];
+  __syncthreads();
+  if (threadIdx.x == 0) {
     s.act[cnt] = next;
     *s.na = cnt + 1;
     s.slot[j] = -1;
     s.slot[i] = -1;
     s.slot[next] = si;
+    s.node[sj] = -1;
+    s.node[si] = next;
   }
 }
 
 }  // namespace
 
 struct NJState {
-  DevBuf D, T, slot, act, na, rows, rowlen, head, rq, ra, rb, gl, win, cnt, stats, joins, vd;
+  DevBuf D, T, Tf, slot, node, act, na, g32, cand, win, stats, joins, vd;
   ~NJState() {
-    for (DevBuf* b : {&D, &T, &slot, &act, &na, &rows, &rowlen, &head, &rq, &ra, &rb, &gl, &win, &cnt, &stats,
-                      &joins, &vd})
-      b->release();
+    for (DevBuf* b : {&D, &T, &Tf, &slot, &node, &act, &na, &g32, &cand, &win, &stats, &joins, &vd}) b->release();
   }
 };
 
@@ -523,12 +507,10 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
   const int nn = 2 * n - 1;
   int rc;
   if ((rc = S.D.ensure(sizeof(float) * (size_t)n * n)) || (rc = S.T.ensure(sizeof(double) * n)) ||
-      (rc = S.slot.ensure(sizeof(int) * nn)) || (rc = S.act.ensure(sizeof(int) * (n + 1))) ||
-      (rc = S.na.ensure(sizeof(int))) || (rc = S.rows.ensure(sizeof(Entry) * (size_t)n * n)) ||
-      (rc = S.rowlen.ensure(sizeof(int) * n)) || (rc = S.head.ensure(sizeof(int) * n)) ||
-      (rc = S.rq.ensure(sizeof(double) * n)) || (rc = S.ra.ensure(sizeof(int) * n)) ||
-      (rc = S.rb.ensure(sizeof(int) * n)) || (rc = S.gl.ensure(sizeof(double) * 4)) ||
-      (rc = S.win.ensure(sizeof(Pick))) || (rc = S.cnt.ensure(sizeof(unsigned long long) * 2)) ||
+      (rc = S.Tf.ensure(sizeof(float) * n)) || (rc = S.slot.ensure(sizeof(int) * nn)) ||
+      (rc = S.node.ensure(sizeof(int) * n)) || (rc = S.act.ensure(sizeof(int) * (n + 1))) ||
+      (rc = S.na.ensure(sizeof(int))) || (rc = S.g32.ensure(sizeof(int) * 4)) ||
+      (rc = S.cand.ensure(sizeof(Cand) * kCandCap)) || (rc = S.win.ensure(sizeof(Pick))) ||
       (rc = S.stats.ensure(sizeof(unsigned long long) * 3)) ||
       (rc = S.joins.ensure(sizeof(nwg_join) * (n - 1))) || (rc = S.vd.ensure(sizeof(float) * n)))
     return fail(rc, "nj allocation");
@@ -537,46 +519,40 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
   if ((rc = cuda(cudaMemcpy2DAsync(S.D.p, sizeof(float) * n, D, sizeof(float) * ld, sizeof(float) * n, n, kind, s),
                  "nj upload")))
     return rc;
-  std::vector<int> slot0(nn, -1), act0(n + 1, 0);
-  for (int k = 0; k < n; ++k) slot0[k] = k, act0[k] = k;
+  std::vector<int> slot0(nn, -1), act0(n + 1, 0), node0(n);
+  for (int k = 0; k < n; ++k) slot0[k] = k, act0[k] = k, node0[k] = k;
   const int na0 = n;
+  const int g0[4] = {0x7F7FFFFF, 0, 0, 0};
   if ((rc = cuda(cudaMemcpyAsync(S.slot.p, slot0.data(), sizeof(int) * nn, cudaMemcpyHostToDevice, s), "nj upload")) ||
+      (rc = cuda(cudaMemcpyAsync(S.node.p, node0.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s), "nj upload")) ||
       (rc = cuda(cudaMemcpyAsync(S.act.p, act0.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s), "nj upload")) ||
       (rc = cuda(cudaMemcpyAsync(S.na.p, &na0, sizeof(int), cudaMemcpyHostToDevice, s), "nj upload")) ||
+      (rc = cuda(cudaMemcpyAsync(S.g32.p, g0, sizeof(g0), cudaMemcpyHostToDevice, s), "nj upload")) ||
       (rc = cuda(cudaMemsetAsync(S.stats.p, 0, sizeof(unsigned long long) * 3, s), "nj upload")))
     return rc;
-  cudaStreamSynchronize(s);   // host vectors above are pageable and local
+  if ((rc = cuda(cudaStreamSynchronize(s), "nj upload"))) return rc;   // host vectors above are local
   NJDev d{};
   d.D = (float*)S.D.p;
   d.T = (double*)S.T.p;
+  d.Tf = (float*)S.Tf.p;
   d.slot = (int*)S.slot.p;
+  d.node = (int*)S.node.p;
   d.act = (int*)S.act.p;
   d.na = (int*)S.na.p;
-  d.rows = (Entry*)S.rows.p;
-  d.rowlen = (int*)S.rowlen.p;
-  d.head = (int*)S.head.p;
-  d.rq = (double*)S.rq.p;
-  d.ra = (int*)S.ra.p;
-  d.rb = (int*)S.rb.p;
-  d.gl = (double*)S.gl.p;
+  d.g32 = (int*)S.g32.p;
+  d.cand = (Cand*)S.cand.p;
   d.win = (Pick*)S.win.p;
-  d.cnt = (unsigned long long*)S.cnt.p;
   d.stats = (unsigned long long*)S.stats.p;
   d.joins = (nwg_join*)S.joins.p;
   d.vd = (float*)S.vd.p;
   d.n0 = n;
-  int m = 1;
-  while (m < n) m <<= 1;
-  const size_t sort_smem = sizeof(Entry) * (size_t)m;
-  if ((rc = cuda(cudaFuncSetAttribute(init_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sort_smem),
-                 "nj smem")) ||
-      (rc = cuda(cudaFuncSetAttribute(join_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sort_smem),
+  const size_t join_smem = 2 * sizeof(float) * (size_t)n;
+  if ((rc = cuda(cudaFuncSetAttribute(join_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)join_smem),
                  "nj smem")))
     return rc;
   if (st) cudaEventRecord(ev0, s);
-  rowsum_kernel<<<(n + 127) / 128, 128, 0, s>>>(d);
-  init_rows_kernel<<<n, 1024, sort_smem, s>>>(d);
-  launches += 2;
+  rowsum_kernel<<<(n + 7) / 8, 256, 0, s>>>(d);
+  ++launches;
   // host-side schedule (deterministic in n, as the reference's)
   const int kBinT = 30 * 31 / 2;
   int steps = std::max((int)((float)n * 0.5f), 200);
@@ -586,13 +562,11 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
   int watermark = n, next = n, m_n = n, na = n;
   for (int step = 0; step < n - 1; ++step) {
     const double nm2 = (double)(m_n - 2);
-    const int sg = (na + kScanWarps - 1) / kScanWarps;
-    prepare_kernel<<<1, 1024, 0, s>>>(d, watermark, nm2);
-    scan_kernel<<<sg, 32 * kScanWarps, 0, s>>>(d, watermark, nm2);
-    pick_kernel<<<1, 1024, 0, s>>>(d, nm2);
-    ambiguity_kernel<<<sg, 32 * kScanWarps, 0, s>>>(d, watermark, nm2);
-    join_kernel<<<1, 1024, sort_smem, s>>>(d, step, next, m_n);
-    launches += 5;
+    pass_min_kernel<<<na, 256, 0, s>>>(d, (float)(m_n - 2));
+    pass_cand_kernel<<<na, 256, 0, s>>>(d, (float)(m_n - 2), nm2, watermark);
+    pick_kernel<<<1, 1024, 0, s>>>(d);
+    join_kernel<<<1, 1024, join_smem, s>>>(d, step, next, m_n);
+    launches += 4;
     if (--pq_ck == 0) {
       pq_ck = 500;
       if (steps > 0) {
@@ -604,7 +578,7 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
     na -= 1;
     ++next;
     if (steps == 0) {
-      rowsum_kernel<<<(na + 127) / 128, 128, 0, s>>>(d);
+      rowsum_kernel<<<(na + 7) / 8, 256, 0, s>>>(d);
       ++launches;
       ++stats.rebuilds;
       watermark = next;
@@ -622,7 +596,7 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
       (rc = cuda(cudaMemcpyAsync(dst, S.stats.p, sizeof(dst), cudaMemcpyDeviceToHost, s), "nj download")) ||
       (rc = cuda(cudaStreamSynchronize(s), "nj sync")))
     return rc;
-  if (dst[2]) return fail(NWG_ERR_CUDA, "neighbor joining found no candidate pair");
+  if (dst[2]) return fail(NWG_ERR_CUDA, "neighbor joining candidate list empty or overflowing");
   stats.ambiguous_steps = (int64_t)dst[0];
   stats.tie_steps = (int64_t)dst[1];
   if (st) {
