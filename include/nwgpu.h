@@ -267,6 +267,49 @@ int nwg_autotune(nwg_ctx* ctx, int flags, nwg_tune_result* out);
 /* Set the choice per class explicitly (NWG_TUNE_CLASSES entries each). */
 int nwg_set_tuning(nwg_ctx* ctx, const int32_t* rows_per_lane, const int32_t* variant);
 
+/* ---- serving loop ------------------------------------------------------------
+ * Alignment jobs (one sequence family each: distance matrix + guide tree, the
+ * work of SpeciesBlock::buildTree up to the join loop, SpeciesBlock.cpp:242-403
+ * and wnj.cpp:10-52, for one job) submitted at any time from any thread.
+ * A worker thread admits pending jobs while their HBM footprint
+ * (n^2 floats of matrix + NJ workspace + codes) fits hbm_budget_bytes and puts
+ * up to max_batch_jobs of them into one batch: one persistent launch per
+ * length bucket with pairs of all the batch's jobs interleaved, then one
+ * launch with a CTA per job running the whole join loop.  Two batches can be
+ * on the device at once (own streams), so jobs arriving while one batch runs
+ * are admitted and overlap it.  Each job's matrix and join list equal what
+ * nwg_score_all and nwg_nj return for that job alone.
+ * Jobs with n <= 1024 sequences are accepted (larger: NWG_ERR_INVALID, run
+ * them through a context).  The reference has no serving loop. */
+typedef struct nwg_server nwg_server;
+
+typedef struct {
+  int32_t n;                   /* sequences                                        */
+  int32_t status;              /* NWG_OK or the job's error                         */
+  int32_t batch_jobs;          /* jobs in the batch it ran in                       */
+  int32_t pad;
+  double queue_ms;             /* submit -> admitted to a batch                     */
+  double latency_ms;           /* submit -> results on the host                     */
+  int64_t cells;               /* DP cells of the job's off-diagonal pairs          */
+  int64_t nj_ambiguous_steps;  /* as nwg_nj_stats                                   */
+  int64_t nj_tie_steps;
+  int64_t nj_rebuilds;
+} nwg_job_info;
+
+int nwg_server_create(int gap_open, int gap_ext, int64_t hbm_budget_bytes, int max_batch_jobs,
+                      nwg_server** out);
+/* Copies the job's sequences (ASCII, offsets[0..n]); returns at once. */
+int nwg_server_submit(nwg_server* srv, const char* ascii, const int64_t* offsets, int n, uint64_t* job_id);
+/* Waits up to timeout_ms (< 0: no limit; NWG_ERR_TIMEOUT when it runs out, the
+ * job stays queryable) for the job, copies its n*n matrix to D and its n-1
+ * joins to joins (either may be NULL) and releases it; returns the job's
+ * status. */
+int nwg_server_wait(nwg_server* srv, uint64_t job_id, int timeout_ms, float* D, nwg_join* joins,
+                    nwg_job_info* info);
+/* Stops admitting, finishes the batches on the device, frees everything.
+ * Jobs not yet waited for are dropped. */
+int nwg_server_destroy(nwg_server* srv);
+
 #ifdef __cplusplus
 }
 #endif

@@ -158,6 +158,16 @@ class NJStats(ctypes.Structure):
 JOIN_DTYPE = [("i", "i4"), ("j", "i4"), ("node", "i4"), ("n", "i4"), ("d", "f4"), ("pad", "f4"),
               ("q", "f8"), ("ti", "f8"), ("tj", "f8"), ("len_i", "f8"), ("len_j", "f8")]
 
+class JobInfo(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int32), ("status", ctypes.c_int32), ("batch_jobs", ctypes.c_int32),
+                ("pad", ctypes.c_int32), ("queue_ms", ctypes.c_double), ("latency_ms", ctypes.c_double),
+                ("cells", ctypes.c_int64), ("nj_ambiguous_steps", ctypes.c_int64),
+                ("nj_tie_steps", ctypes.c_int64), ("nj_rebuilds", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
+
+
 EXTRA_SIGS: dict = {
     "nwg_nj": ([ctypes.c_void_p, c_f32p, ctypes.c_int64, ctypes.c_int, ctypes.c_void_p, P(NJStats)],
                ctypes.c_int),
@@ -174,6 +184,13 @@ EXTRA_SIGS: dict = {
     "nwg_dpx_peak": ([ctypes.c_void_p, ctypes.c_int, P(ctypes.c_double)], ctypes.c_int),
     "nwg_set_launch_timing": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "nwg_launch_records": ([ctypes.c_void_p, P(LaunchRec), ctypes.c_int], ctypes.c_int),
+    "nwg_server_create": ([ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_int, P(ctypes.c_void_p)],
+                          ctypes.c_int),
+    "nwg_server_submit": ([ctypes.c_void_p, ctypes.c_char_p, c_i64p, ctypes.c_int, P(ctypes.c_uint64)],
+                          ctypes.c_int),
+    "nwg_server_wait": ([ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int, c_f32p, ctypes.c_void_p, P(JobInfo)],
+                        ctypes.c_int),
+    "nwg_server_destroy": ([ctypes.c_void_p], ctypes.c_int),
 }
 
 

@@ -76,10 +76,12 @@ struct NJDev {
   int* g32;            // [0] min float q (ordered int), [1] max magnitude (ordered int), [2] candidates
   Cand* cand;          // candidate list
   Pick* win;
-  unsigned long long* stats;  // [0] ambiguous steps, [1] tie steps, [2] internal errors
+  unsigned long long* stats;  // [0] ambiguous steps, [1] tie steps, [2] internal errors,
+                              // [3] open heap-size checks, [4] rebuilds (per-CTA path)
   nwg_join* joins;
   float* vd;           // per slot, new row values
   int n0;
+  int cand_cap;        // candidate list capacity
 };
 
 __device__ __forceinline__ int ford(float f) {
@@ -225,17 +227,17 @@ __global__ void __launch_bounds__(256) pass_cand_kernel(NJDev s, float nm2f, dou
     cd.a = a;
     cd.b = b;
     const int k = atomicAdd(&s.g32[2], 1);
-    if (k < kCandCap) s.cand[k] = cd;
+    if (k < s.cand_cap) s.cand[k] = cd;
   }
 }
 
 // Winner among the candidates, ambiguity and tie count; resets the pass
-// accumulators for the next join.
-__global__ void __launch_bounds__(1024) pick_kernel(NJDev s) {
+// accumulators for the next join.  One CTA (any multiple of 32 threads).
+__device__ void pick_body(const NJDev& s) {
   __shared__ double sq[32];
   __shared__ int sa[32], sb[32];
   __shared__ unsigned s_ties, s_amb;
-  const int nc = min(s.g32[2], kCandCap);
+  const int nc = min(s.g32[2], s.cand_cap);
   double bq = DBL_MAX;
   int ba = INT_MAX, bb = -1;
   for (int k = threadIdx.x; k < nc; k += blockDim.x) {
@@ -310,20 +312,21 @@ __global__ void __launch_bounds__(1024) pick_kernel(NJDev s) {
     p.a = ba;
     p.b = bb;
     *s.win = p;
-    if (bb < 0 || s.g32[2] > kCandCap) atomicAdd(&s.stats[2], 1ull);   // no candidate / list overflow
+    if (bb < 0 || s.g32[2] > s.cand_cap) atomicAdd(&s.stats[2], 1ull);   // no candidate / list overflow
     else if (s_amb > 0 || s_ties > 4) atomicAdd(&s.stats[0], 1ull);
     else if (s_ties > 1) atomicAdd(&s.stats[1], 1ull);
     s.g32[0] = 0x7F7FFFFF;          // ordered-int of FLT_MAX
     s.g32[1] = 0;
     s.g32[2] = 0;
   }
+  __syncthreads();
 }
 
-// The join: record, modifyMatrix, active list.  One CTA.
-__global__ void __launch_bounds__(1024) join_kernel(NJDev s, int step, int next, int m_n) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  float* tv = reinterpret_cast<float*>(smem_raw);                        // tmp by active index
-  int* ids = reinterpret_cast<int*>(smem_raw + sizeof(float) * s.n0);    // compacted active list
+__global__ void __launch_bounds__(1024) pick_kernel(NJDev s) { pick_body(s); }
+
+// The join: record, modifyMatrix, active list.  One CTA; tv and ids are
+// shared-memory arrays of n0 entries.
+__device__ void join_body(const NJDev& s, int step, int next, int m_n, float* tv, int* ids) {
   __shared__ int s_pos[1024 / 32 + 1];
   __shared__ int s_skip[2];
   __shared__ double s_part[32], s_ab[32];
@@ -477,6 +480,176 @@ __global__ void __launch_bounds__(1024) join_kernel(NJDev s, int step, int next,
     s.node[sj] = -1;
     s.node[si] = next;
   }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(1024) join_kernel(NJDev s, int step, int next, int m_n) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  join_body(s, step, next, m_n, reinterpret_cast<float*>(smem_raw),
+            reinterpret_cast<int*>(smem_raw + sizeof(float) * s.n0));
+}
+
+// ---- one job per CTA (serving: many small jobs in one launch) --------------
+
+constexpr int kCtaMaxN = 1024;
+
+struct NJJob {
+  NJDev s;
+  int n;
+};
+
+__device__ void cta_rowsums(const NJDev& s) {
+  const int na = *s.na;
+  const int lane = threadIdx.x & 31;
+  for (int k = threadIdx.x >> 5; k < na; k += blockDim.x >> 5) {
+    const int sk = s.slot[s.act[k]];
+    const float* row = s.D + (size_t)sk * s.n0;
+    double part = 0.0, ab = 0.0;
+    int lowexp = INT_MAX;
+    for (int j = lane; j < na; j += 32) {
+      const float x = row[s.slot[s.act[j]]];
+      part = __dadd_rn(part, (double)x);
+      ab = __dadd_rn(ab, (double)fabsf(x));
+      lowexp = min(lowexp, low_bit_exp(x));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      part = __dadd_rn(part, __shfl_down_sync(0xffffffffu, part, o));
+      ab = __dadd_rn(ab, __shfl_down_sync(0xffffffffu, ab, o));
+      lowexp = min(lowexp, __shfl_down_sync(0xffffffffu, lowexp, o));
+    }
+    if (lane == 0) {
+      double sum = part;
+      if (!sum_is_exact(ab, lowexp)) {
+        sum = 0.0;
+        for (int j = 0; j < na; ++j) sum = __dadd_rn(sum, (double)row[s.slot[s.act[j]]]);
+      }
+      s.T[sk] = sum;
+      s.Tf[sk] = (float)sum;
+    }
+  }
+  __syncthreads();
+}
+
+__device__ void cta_pass_min(const NJDev& s, float nm2f) {
+  __shared__ float sq[32], sm[32];
+  const int na = *s.na;
+  const int lane = threadIdx.x & 31;
+  float qmin = FLT_MAX, mmax = 0.f;
+  for (int k = threadIdx.x >> 5; k < na; k += blockDim.x >> 5) {
+    const int r = s.slot[s.act[k]];
+    const float tr = s.Tf[r];
+    const float* row = s.D + (size_t)r * s.n0;
+    for (int c = r + 1 + lane; c < s.n0; c += 32) {
+      if (s.node[c] < 0) continue;
+      const float tc = s.Tf[c];
+      const float x = __fmul_rn(row[c], nm2f);
+      qmin = fminf(qmin, __fsub_rn(__fsub_rn(x, tr), tc));
+      mmax = fmaxf(mmax, __fadd_rn(__fadd_rn(fabsf(x), fabsf(tr)), fabsf(tc)));
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    qmin = fminf(qmin, __shfl_down_sync(0xffffffffu, qmin, o));
+    mmax = fmaxf(mmax, __shfl_down_sync(0xffffffffu, mmax, o));
+  }
+  if (lane == 0) {
+    sq[threadIdx.x >> 5] = qmin;
+    sm[threadIdx.x >> 5] = mmax;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+      qmin = fminf(qmin, sq[w]);
+      mmax = fmaxf(mmax, sm[w]);
+    }
+    s.g32[0] = ford(qmin);
+    s.g32[1] = ford(mmax);
+    s.g32[2] = 0;
+  }
+  __syncthreads();
+}
+
+__device__ void cta_pass_cand(const NJDev& s, float nm2f, double nm2, int watermark) {
+  const int na = *s.na;
+  const int lane = threadIdx.x & 31;
+  const float qmin = iord(s.g32[0]);
+  const float mmax = iord(s.g32[1]);
+  const float thr = qmin + 3.f * (8.f * 5.9604645e-8f * mmax) + 1e-30f;
+  for (int k = threadIdx.x >> 5; k < na; k += blockDim.x >> 5) {
+    const int ur = s.act[k];
+    const int r = s.slot[ur];
+    const float tr = s.Tf[r];
+    const float* row = s.D + (size_t)r * s.n0;
+    for (int c = r + 1 + lane; c < s.n0; c += 32) {
+      const int uc = s.node[c];
+      if (uc < 0) continue;
+      const float d = row[c];
+      const float q = __fsub_rn(__fsub_rn(__fmul_rn(d, nm2f), tr), s.Tf[c]);
+      if (q > thr) continue;
+      const int a = min(ur, uc), b = max(ur, uc);
+      Cand cd;
+      cd.q1 = q_record(s, d, a, b, watermark, nm2);
+      cd.q2 = q_heap(s, d, a, b, nm2);
+      cd.a = a;
+      cd.b = b;
+      const int idx = atomicAdd(&s.g32[2], 1);
+      if (idx < s.cand_cap) s.cand[idx] = cd;
+    }
+  }
+  __syncthreads();
+}
+
+// The whole join loop of one job, schedule included (same as the host loop of
+// Ctx::nj).  Workspace pointers of every job are set by the host.
+__global__ void __launch_bounds__(1024) nj_cta_kernel(const NJJob* jobs, int njobs) {
+  __shared__ float tv[kCtaMaxN];
+  __shared__ int ids[kCtaMaxN];
+  if ((int)blockIdx.x >= njobs) return;
+  const NJJob J = jobs[blockIdx.x];
+  const NJDev& s = J.s;
+  const int n = J.n;
+  for (int k = threadIdx.x; k < 2 * n - 1; k += blockDim.x) s.slot[k] = k < n ? k : -1;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    s.node[k] = k;
+    s.act[k] = k;
+  }
+  if (threadIdx.x == 0) {
+    *s.na = n;
+    s.stats[0] = s.stats[1] = s.stats[2] = s.stats[3] = s.stats[4] = 0;
+  }
+  __syncthreads();
+  if (n < 2) return;
+  cta_rowsums(s);
+  const int kBinT = 30 * 31 / 2;
+  int steps = max((int)((float)n * 0.5f), 200);
+  int pq_ck = 500;
+  long long ave0 = (((long long)(n - 1) * n) / 2) / kBinT;
+  long long ub = ((long long)n * (n - 1)) / 2;
+  int watermark = n, next = n, m_n = n, na = n;
+  for (int step = 0; step < n - 1; ++step) {
+    const double nm2 = (double)(m_n - 2);
+    cta_pass_min(s, (float)(m_n - 2));
+    cta_pass_cand(s, (float)(m_n - 2), nm2, watermark);
+    pick_body(s);
+    join_body(s, step, next, m_n, tv, ids);
+    if (--pq_ck == 0) {
+      pq_ck = 500;
+      if (steps > 0 && (double)(ub / kBinT) / (double)ave0 > 2.0 && threadIdx.x == 0) s.stats[3] += 1;
+    }
+    --m_n;
+    na -= 1;
+    ++next;
+    if (steps == 0) {
+      cta_rowsums(s);
+      if (threadIdx.x == 0) s.stats[4] += 1;
+      watermark = next;
+      steps = (m_n < 200) ? INT_MAX : (int)((float)m_n * 0.5f);
+      ave0 = (((long long)(m_n - 1) * m_n) / 2) / kBinT;
+      ub = ((long long)m_n * (m_n - 1)) / 2;
+    } else {
+      --steps;
+      ub += na - 1;
+    }
+  }
 }
 
 }  // namespace
@@ -511,7 +684,7 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
       (rc = S.node.ensure(sizeof(int) * n)) || (rc = S.act.ensure(sizeof(int) * (n + 1))) ||
       (rc = S.na.ensure(sizeof(int))) || (rc = S.g32.ensure(sizeof(int) * 4)) ||
       (rc = S.cand.ensure(sizeof(Cand) * kCandCap)) || (rc = S.win.ensure(sizeof(Pick))) ||
-      (rc = S.stats.ensure(sizeof(unsigned long long) * 3)) ||
+      (rc = S.stats.ensure(sizeof(unsigned long long) * 5)) ||
       (rc = S.joins.ensure(sizeof(nwg_join) * (n - 1))) || (rc = S.vd.ensure(sizeof(float) * n)))
     return fail(rc, "nj allocation");
   cudaStream_t s = stream;
@@ -528,7 +701,7 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
       (rc = cuda(cudaMemcpyAsync(S.act.p, act0.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s), "nj upload")) ||
       (rc = cuda(cudaMemcpyAsync(S.na.p, &na0, sizeof(int), cudaMemcpyHostToDevice, s), "nj upload")) ||
       (rc = cuda(cudaMemcpyAsync(S.g32.p, g0, sizeof(g0), cudaMemcpyHostToDevice, s), "nj upload")) ||
-      (rc = cuda(cudaMemsetAsync(S.stats.p, 0, sizeof(unsigned long long) * 3, s), "nj upload")))
+      (rc = cuda(cudaMemsetAsync(S.stats.p, 0, sizeof(unsigned long long) * 5, s), "nj upload")))
     return rc;
   if ((rc = cuda(cudaStreamSynchronize(s), "nj upload"))) return rc;   // host vectors above are local
   NJDev d{};
@@ -546,6 +719,7 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
   d.joins = (nwg_join*)S.joins.p;
   d.vd = (float*)S.vd.p;
   d.n0 = n;
+  d.cand_cap = kCandCap;
   const size_t join_smem = 2 * sizeof(float) * (size_t)n;
   if ((rc = cuda(cudaFuncSetAttribute(join_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)join_smem),
                  "nj smem")))
@@ -608,6 +782,57 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
     *st = stats;
   }
   return NWG_OK;
+}
+
+}  // namespace nwg
+
+namespace nwg {
+
+// Workspace of one job of the per-CTA path, laid out from `base` (256-byte
+// aligned pieces); D is the job's matrix (modified in place).
+size_t nj_job_workspace(int n) {
+  auto al = [](size_t x) { return (x + 255) / 256 * 256; };
+  const size_t cap = std::min<size_t>(kCandCap, (size_t)n * (n - 1) / 2 + 1);
+  return al(sizeof(double) * n) + al(sizeof(float) * n) + al(sizeof(int) * (2 * n)) + al(sizeof(int) * n) +
+         al(sizeof(int) * (n + 1)) + al(sizeof(int) * 4) + al(sizeof(int) * 4) + al(sizeof(unsigned long long) * 5) +
+         al(sizeof(float) * n) + al(sizeof(Cand) * cap) + al(sizeof(Pick)) + al(sizeof(nwg_join) * (n > 1 ? n - 1 : 1));
+}
+
+// Fill the job descriptor for a job of n nodes with matrix D and workspace
+// at base; returns the addresses of its join records and statistics.
+void nj_job_setup(void* job_out, float* D, int n, char* base, nwg_join** joins, unsigned long long** stats) {
+  auto al = [](size_t x) { return (x + 255) / 256 * 256; };
+  const size_t cap = std::min<size_t>(kCandCap, (size_t)n * (n - 1) / 2 + 1);
+  NJJob J{};
+  char* p = base;
+  J.s.D = D;
+  J.s.T = (double*)p; p += al(sizeof(double) * n);
+  J.s.Tf = (float*)p; p += al(sizeof(float) * n);
+  J.s.slot = (int*)p; p += al(sizeof(int) * (2 * n));
+  J.s.node = (int*)p; p += al(sizeof(int) * n);
+  J.s.act = (int*)p; p += al(sizeof(int) * (n + 1));
+  J.s.na = (int*)p; p += al(sizeof(int) * 4);
+  J.s.g32 = (int*)p; p += al(sizeof(int) * 4);
+  J.s.stats = (unsigned long long*)p; p += al(sizeof(unsigned long long) * 5);
+  J.s.vd = (float*)p; p += al(sizeof(float) * n);
+  J.s.cand = (Cand*)p; p += al(sizeof(Cand) * cap);
+  J.s.win = (Pick*)p; p += al(sizeof(Pick));
+  J.s.joins = (nwg_join*)p;
+  J.s.n0 = n;
+  J.s.cand_cap = (int)cap;
+  J.n = n;
+  *joins = J.s.joins;
+  *stats = J.s.stats;
+  std::memcpy(job_out, &J, sizeof(J));
+}
+
+size_t nj_job_desc_bytes() { return sizeof(NJJob); }
+int nj_cta_max_n() { return kCtaMaxN; }
+
+cudaError_t launch_nj_jobs(const void* d_jobs, int njobs, cudaStream_t s) {
+  if (njobs <= 0) return cudaSuccess;
+  nj_cta_kernel<<<njobs, 1024, 0, s>>>(reinterpret_cast<const NJJob*>(d_jobs), njobs);
+  return cudaGetLastError();
 }
 
 }  // namespace nwg

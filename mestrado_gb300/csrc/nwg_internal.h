@@ -57,6 +57,12 @@ struct WaveArgs {
   const int32_t* group_y2;    // per Y group: second Y for int16x2 lanes, or -1
   const int32_t* group_x;     // per Y group: number of X rows (triangle: up to the group's last Y)
   const int64_t* job_prefix;  // per Y group of this bucket: first CTA job; ngroups+1 entries
+  // several alignment jobs in one launch (serving): per Y group, the first X
+  // (sorted index) of its job, the offset of its job's matrix in D and that
+  // matrix's leading dimension; null for a single set
+  const int32_t* group_xbase;
+  const int64_t* group_dofs;
+  const int32_t* group_ld;
   unsigned long long* counter;
   float* D;
   int32_t* scratch;           // per warp: 2 buffers x 2 words x scratch_cols
@@ -122,6 +128,12 @@ void prepare_wave(int R, int P, int V);   // sets the dynamic shared memory limi
 size_t wave_smem_bytes(int R);
 cudaError_t launch_plain(const PlainArgs& a, cudaStream_t s);
 cudaError_t launch_rerun(const WaveArgs& a, int2* scratch, int64_t nthreads, cudaStream_t s);
+// per-CTA neighbor joining for many small jobs (nj.cu)
+size_t nj_job_workspace(int n);
+void nj_job_setup(void* job_out, float* D, int n, char* base, nwg_join** joins, unsigned long long** stats);
+size_t nj_job_desc_bytes();
+int nj_cta_max_n();
+cudaError_t launch_nj_jobs(const void* d_jobs, int njobs, cudaStream_t s);
 cudaError_t launch_dpx_peak(int P, int cols, int grid, uint32_t* sink, int go, int ge, cudaStream_t s);
 int dpx_peak_ctas_per_sm(int P);
 cudaError_t launch_pairlist(const PairListArgs& a, int64_t count, cudaStream_t s);

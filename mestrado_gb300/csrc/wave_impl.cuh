@@ -104,6 +104,12 @@ __device__ __forceinline__ void put_score(const WaveArgs& a, int xo, int yo, int
   }
 }
 
+// Job-relative output (several jobs in one launch): the group's matrix.
+__device__ __forceinline__ void put_score_job(const WaveArgs& a, float* D, int64_t ld, int xo, int yo, int v) {
+  D[(int64_t)xo * ld + yo] = (float)v;
+  D[(int64_t)yo * ld + xo] = (float)v;
+}
+
 // Optimistic int16 groups: a pair whose composition bound could exceed the
 // int16 range is not reported from the int16 lanes; it goes to the int32
 // re-run queue instead.
@@ -161,7 +167,8 @@ __device__ __forceinline__ void wave_band(const WaveArgs& a, int lane, int b, in
                                           const int8_t* __restrict__ X, int Lx,
                                           const uint32_t* __restrict__ prof,
                                           int32_t* __restrict__ scratch, int rowA, int rowB,
-                                          bool wantA, bool wantB, int xo, int yoA, int yoB) {
+                                          bool wantA, bool wantB, int xo, int yoA, int yoB,
+                                          float* jobD, int64_t jobld) {
   using L = Lanes<P>;
   constexpr int BAND = 32 * R;
   constexpr int Q = R / 4;
@@ -231,11 +238,19 @@ __device__ __forceinline__ void wave_band(const WaveArgs& a, int lane, int b, in
   // H[] now holds the last column; the lane owning a pair's last row reports.
   if (wantA) {
     const int rr = rowA - b * BAND;
-    if (rr >= 0 && rr < BAND && lane == rr / R) put_score(a, xo, yoA, L::lo(pick<R>(s.H, rr % R)));
+    if (rr >= 0 && rr < BAND && lane == rr / R) {
+      const int v = L::lo(pick<R>(s.H, rr % R));
+      if (jobD) put_score_job(a, jobD, jobld, xo, yoA, v);
+      else put_score(a, xo, yoA, v);
+    }
   }
   if (P == 2 && wantB) {
     const int rr = rowB - b * BAND;
-    if (rr >= 0 && rr < BAND && lane == rr / R) put_score(a, xo, yoB, L::hi(pick<R>(s.H, rr % R)));
+    if (rr >= 0 && rr < BAND && lane == rr / R) {
+      const int v = L::hi(pick<R>(s.H, rr % R));
+      if (jobD) put_score_job(a, jobD, jobld, xo, yoB, v);
+      else put_score(a, xo, yoB, v);
+    }
   }
 }
 
@@ -275,12 +290,15 @@ __global__ void __launch_bounds__(kWaveThreads, (MinBlocks<R, P, V>::value)) wav
     const int y1 = (P == 2) ? a.group_y2[g] : -1;
     const bool has_b = y1 >= 0;
     const int nX = a.group_x[g];
-    const int i = (int)(chunk * kWaveWarps) + warp;
+    const int xbase = a.group_xbase ? a.group_xbase[g] : 0;
+    float* jobD = a.group_dofs ? a.D + a.group_dofs[g] : nullptr;
+    const int64_t jobld = a.group_ld ? a.group_ld[g] : a.ld;
+    const int i = xbase + (int)(chunk * kWaveWarps) + warp;
     const int LyA = a.ylen[y0];
     const int LyB = has_b ? a.ylen[y1] : 0;
     const int8_t* YA = a.codes + a.ystart[y0];
     const int8_t* YB = has_b ? a.codes + a.ystart[y1] : YA;
-    const bool active = i < nX;
+    const bool active = i < xbase + nX;
     const int Lx = active ? a.xlen[i] : 0;
     const int8_t* X = a.codes + (active ? a.xstart[i] : 0);
     bool wantA = active && (!a.triangle || i <= y0);
@@ -324,7 +342,8 @@ __global__ void __launch_bounds__(kWaveThreads, (MinBlocks<R, P, V>::value)) wav
       }
       __syncthreads();
       if (wantA || wantB)
-        wave_band<R, P, V>(a, lane, b, nb, X, Lx, prof, scratch, LyA - 1, LyB - 1, wantA, wantB, xo, yoA, yoB);
+        wave_band<R, P, V>(a, lane, b, nb, X, Lx, prof, scratch, LyA - 1, LyB - 1, wantA, wantB, xo, yoA, yoB,
+                           jobD, jobld);
     }
   }
 }

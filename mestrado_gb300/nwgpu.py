@@ -14,7 +14,7 @@ import numpy as np
 from ._native import (MODE_BATCHED, MODE_BATCHED_INT32, MODE_PLAIN, NWGError, Stats, c_f32p,
                       c_i8p, c_i32p, c_i64p, check, lib)
 
-__all__ = ["Context", "AlignmentScore", "cherries", "encode", "make_wire", "newick", "parse_wire"]
+__all__ = ["Context", "AlignmentScore", "Server", "cherries", "encode", "make_wire", "newick", "parse_wire"]
 
 
 def _p(a: np.ndarray, ct):
@@ -227,6 +227,58 @@ class Context:
                                               len(offsets) - 1, _p(pi, c_i32p), _p(pj, c_i32p), len(pi),
                                               _p(out, c_i32p), None))
         return out
+
+
+class Server:
+    """The serving loop: alignment jobs (distance matrix + guide tree each)
+    submitted at any time, admitted by HBM footprint and run in shared
+    batches on the device (nwg_server_* in include/nwgpu.h)."""
+
+    def __init__(self, gap_open: int = 10, gap_ext: int = 2, hbm_budget: int = 8 << 30,
+                 max_batch_jobs: int = 256):
+        self._lib = lib()
+        h = ctypes.c_void_p()
+        check(self._lib.nwg_server_create(gap_open, gap_ext, int(hbm_budget), int(max_batch_jobs),
+                                          ctypes.byref(h)))
+        self.h = h
+
+    def submit(self, seqs) -> int:
+        """Queue one job (its sequences); returns the job id at once."""
+        res, off = _as_seq_list(seqs)
+        off = np.ascontiguousarray(off, dtype=np.int64)
+        jid = ctypes.c_uint64()
+        check(self._lib.nwg_server_submit(self.h, res, _p(off, c_i64p), len(off) - 1, ctypes.byref(jid)))
+        return jid.value
+
+    def wait(self, job_id: int, n: int, timeout_ms: int = -1):
+        """(D, joins, info) of a finished job; the job is released."""
+        from ._native import JOIN_DTYPE, NWG_ERR_TIMEOUT, JobInfo
+        D = np.zeros((n, n), dtype=np.float32)
+        joins = np.zeros(max(n - 1, 1), dtype=np.dtype(JOIN_DTYPE))
+        info = JobInfo()
+        st = self._lib.nwg_server_wait(self.h, job_id, int(timeout_ms), _p(D, c_f32p),
+                                       joins.ctypes.data_as(ctypes.c_void_p), ctypes.byref(info))
+        if st == NWG_ERR_TIMEOUT:
+            raise TimeoutError(f"job {job_id} not finished within {timeout_ms} ms")
+        check(st)
+        return D, joins[: max(n - 1, 0)], info.as_dict()
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.nwg_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 def cherries(left, right, n_leaves: int):

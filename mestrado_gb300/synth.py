@@ -136,3 +136,26 @@ def lognormal_families(families: int, per_family: int, median: float, sigma: flo
     sp = Spec(families=families, per_family=per_family, root_mode=ROOT_LOGNORMAL,
               clip_lo=clip_lo, clip_hi=clip_hi, root_a=median, root_b=sigma, ps=ps, pi=pi)
     return generate(sp, seed)
+
+
+def serving_jobs(count: int, rate: float = 200.0, seed: int | None = None,
+                 n_lo: int = 8, n_hi: int = 512, median: float = 250.0, sigma: float = 0.5,
+                 clip_lo: int = 30, clip_hi: int = 2000):
+    """The serving workload: ``count`` independent families arriving as a
+    Poisson process of ``rate`` jobs/s.  Each job has a log-uniform number of
+    sequences in [n_lo, n_hi] and a lognormal root length (median, sigma)
+    clipped to [clip_lo, clip_hi]; its sequences mutate as in the 64-sequence
+    single-family configuration (ps 0.05, pi 0.005).  Returns a list of
+    (arrival_s, SeqSet); per-job sub-seeds follow from ``seed`` (default: the
+    serving configuration's seed)."""
+    if seed is None:
+        seed = config_seed(4)
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, size=count))
+    ns = np.rint(np.exp(rng.uniform(np.log(n_lo), np.log(n_hi), size=count))).astype(int)
+    sub = rng.integers(1, 2**62, size=count)
+    jobs = []
+    for k in range(count):
+        S = lognormal_families(1, int(ns[k]), median, sigma, clip_lo, clip_hi, 0.05, 0.005, int(sub[k]))
+        jobs.append((float(t[k]), S))
+    return jobs
