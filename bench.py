@@ -11,7 +11,9 @@ guard routes there).  One step = the full 10,000 x 10,000 distance matrix.
 Prints one JSON line (rank 0).  value = GCUPS (sum over i<j of L_i*L_j per
 second) with codes and matrix resident in HBM; e2e = the same metric through
 the host-buffer C ABI call (nwg_score_all: codes host->device, matrix
-device->host inside the timed region).  --impl reference times the
+device->host inside the timed region).  The line also carries the serving
+run (Poisson job arrivals, continuous batching): p50/p99 job latency and
+sustained GCUPS beside the same jobs run one by one.  --impl reference times the
 reference's recurrence restated on the CPU (its CUDA does not build on CUDA
 13) on every host core, on a bounded sample of the same pairs.
 
@@ -74,6 +76,17 @@ def _sum_over_ranks(world, v: float) -> float:
     t = torch.tensor([v], dtype=torch.float64)
     dist.all_reduce(t, op=dist.ReduceOp.SUM)
     return float(t.item())
+
+
+def replica_seed(rank: int) -> int:
+    """Seed of the workload replica a rank scores (rank 0: the configuration's own seed)."""
+    from mestrado_gb300 import synth
+    return synth.config_seed(CONFIG) + 1000003 * rank
+
+
+def aggregate_gcups(world, cells: float, seconds: float) -> float:
+    """Whole-job GCUPS: the cells of every rank over the slowest rank's time."""
+    return _sum_over_ranks(world, float(cells)) / _max_over_ranks(world, seconds) / 1e9
 
 
 class ClockSampler:
@@ -161,9 +174,115 @@ def cpu_baseline(S, target_s: float, threads: int, seed: int = 7):
     t0 = time.perf_counter()
     O.score_list(codes, off, pi, pj, threads=threads)
     dt = time.perf_counter() - t0
-    return {"value": cells / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+    value = cells / dt / 1e9
+    # one core, on a sample of about a quarter of target_s
+    k1 = int(max(16, value * 1e9 / threads * target_s / 4 / mean_cells))
+    qi, qj = sample(k1)
+    c1 = float((L[qi] * L[qj]).sum())
+    t0 = time.perf_counter()
+    O.score_list(codes, off, qi, qj, threads=1)
+    d1 = time.perf_counter() - t0
+    return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{len(pi)} seeded random pairs of configuration {CONFIG} ({cells:.3g} cells, "
-                      f"{dt:.1f} s), GCUPS = cells / time"}
+                      f"{dt:.1f} s), GCUPS = cells / time",
+            "one_core": {"value": c1 / d1 / 1e9, "pairs": len(qi), "seconds": d1}}
+
+
+def serving_leg(seconds: float, rate: float = 200.0, sample_jobs: int = 200):
+    """The serving workload: Poisson arrivals at `rate` jobs/s for `seconds`
+    (each job a family of log-uniform 8-512 sequences, lognormal root length
+    median 250, sigma 0.5, clipped 30-2000), submitted at their arrival times
+    to one Server; latency = submit -> matrix and tree on the host.  Beside it,
+    the first `sample_jobs` jobs run job by job through a context (plain
+    per-pair form, and the batched form), scoring + NJ, host buffers."""
+    import queue
+
+    from mestrado_gb300 import MODE_BATCHED, MODE_PLAIN, Context, Server, synth
+    count = max(1, int(seconds * rate))
+    jobs = synth.serving_jobs(count, rate)
+    warm = synth.serving_jobs(16, rate, seed=99)
+    cells = np.array([S.cells() for _, S in jobs], dtype=np.float64)
+    check = set(np.random.default_rng(5).choice(count, size=min(count, 24), replace=False).tolist())
+    srv = Server(10, 2, hbm_budget=16 << 30, max_batch_jobs=256)
+    for _, S in warm:
+        srv.wait(srv.submit(S), len(S))
+    q: "queue.Queue" = queue.Queue()
+    infos = [None] * count
+    kept = {}
+
+    def waiter():
+        for _ in range(count):
+            k, jid = q.get()
+            D, J, info = srv.wait(jid, len(jobs[k][1]))
+            infos[k] = info
+            if k in check:
+                kept[k] = (D, J)
+
+    th = threading.Thread(target=waiter)
+    th.start()
+    t0 = time.perf_counter()
+    lag = 0.0
+    for k, (ta, S) in enumerate(jobs):
+        dt = t0 + ta - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        else:
+            lag = max(lag, -dt)
+        q.put((k, srv.submit(S)))
+    th.join()
+    wall = time.perf_counter() - t0
+    srv.close()
+    lat = np.array([i["latency_ms"] for i in infos])
+    qms = np.array([i["queue_ms"] for i in infos])
+    batch = np.array([i["batch_jobs"] for i in infos])
+    ok = all(i["status"] == 0 for i in infos)
+    # job by job through a context, and the exactness check of the kept jobs
+    ctx = Context(10, 2)
+    ctx.autotune()
+    keys = ("i", "j", "node", "len_i", "len_j")
+    parity = ok
+    for k, (D, J) in kept.items():
+        S = jobs[k][1]
+        Dr = ctx.score_all(S)
+        parity = parity and bool(np.array_equal(D, Dr))
+        if len(S) > 1:
+            Jr = ctx.nj(Dr)
+            parity = parity and all(tuple(a[x] for x in keys) == tuple(b[x] for x in keys) for a, b in zip(J, Jr))
+    m = min(sample_jobs, count)
+    jbj = {}
+    for name, mode in (("plain", MODE_PLAIN), ("batched", MODE_BATCHED)):
+        for _, S in warm[:4]:
+            ctx.score_all(S, mode=mode)
+        ts, tn = [], []
+        for _, S in jobs[:m]:
+            t1 = time.perf_counter()
+            D = ctx.score_all(S, mode=mode)
+            t2 = time.perf_counter()
+            if len(S) > 1:
+                ctx.nj(D)
+            ts.append(t2 - t1)
+            tn.append(time.perf_counter() - t1)
+        c = float(cells[:m].sum())
+        jbj[name] = {"gcups_scoring": c / sum(ts) / 1e9, "gcups_with_nj": c / sum(tn) / 1e9,
+                     "job_p50_ms": float(np.percentile(tn, 50) * 1e3),
+                     "job_p99_ms": float(np.percentile(tn, 99) * 1e3),
+                     "jobs_per_s": m / sum(tn)}
+    ctx.close()
+    served = cells.sum() / wall / 1e9
+    return {
+        "workload": f"Poisson arrivals at {rate:g} jobs/s for {seconds:g} s ({count} jobs), seeded; per job "
+                    "log-uniform 8-512 seqs, root lognormal (median 250, sigma 0.5, clipped 30-2000)",
+        "jobs": count, "rate_jobs_per_s": rate, "wall_s": wall, "submit_lag_max_s": lag,
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p90": float(np.percentile(lat, 90)),
+                       "p99": float(np.percentile(lat, 99)), "max": float(lat.max()), "mean": float(lat.mean())},
+        "queue_ms": {"p50": float(np.percentile(qms, 50)), "p99": float(np.percentile(qms, 99))},
+        "batch_jobs": {"mean": float(batch.mean()), "max": int(batch.max())},
+        "sustained_gcups": served,
+        "offered_gcups": float(cells.sum() / jobs[-1][0] / 1e9),
+        "job_by_job": {"jobs": m, **jbj},
+        "serving_over_plain_job_by_job": served / jbj["plain"]["gcups_with_nj"],
+        "exact": parity, "checked_jobs": len(kept),
+    }
 
 
 def run_reference(args, world, rank):
@@ -226,6 +345,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--subset", type=int, default=0,
                     help="score only the first N sequences (whole families first); for profiling runs")
+    ap.add_argument("--serve-seconds", type=float, default=10.0,
+                    help="length of the serving run (Poisson arrivals at 200 jobs/s); 0 skips it")
     ap.add_argument("--quick", action="store_true",
                     help="device-resident timing only (no e2e, plain, CPU or parity legs); for profiling runs")
     args = ap.parse_args()
@@ -239,7 +360,7 @@ def main():
     from mestrado_gb300 import MODE_BATCHED, MODE_PLAIN, Context, encode, synth
 
     spec = synth.config_spec(CONFIG)
-    seed = synth.config_seed(CONFIG) + 1000003 * rank
+    seed = replica_seed(rank)
     S = synth.generate(spec, seed)
     if args.subset:
         S = S.subset(range(min(args.subset, len(S))))
@@ -289,8 +410,7 @@ def main():
     step_ms = [a.elapsed_time(b) for a, b in ev]
     tot_s = sum(step_ms) / 1e3
     tot_s_max = _max_over_ranks(world, tot_s)
-    all_cells = _sum_over_ranks(world, float(cells) * args.steps)
-    value = all_cells / tot_s_max / 1e9
+    value = aggregate_gcups(world, float(cells) * args.steps, tot_s)
 
     # launches of one step and the dominant launch, timed alone (events around each launch)
     ctx.set_launch_timing(True)
@@ -334,8 +454,7 @@ def main():
         t0 = time.perf_counter()
         ctx.score_all(codes=h_codes.numpy(), offsets=off, out=h_D.numpy(), mode=MODE_BATCHED)
         e2e_times.append(time.perf_counter() - t0)
-    e2e_s = _max_over_ranks(world, sum(e2e_times))
-    e2e = {"value": _sum_over_ranks(world, float(cells) * len(e2e_times)) / e2e_s / 1e9, "unit": UNIT,
+    e2e = {"value": aggregate_gcups(world, float(cells) * len(e2e_times), sum(e2e_times)), "unit": UNIT,
            "h2d_bytes_per_step": int(codes.nbytes + off.nbytes), "d2h_bytes_per_step": int(n * n * 4)}
     parity = parity and bool(np.array_equal(h_D.numpy(), Dh))
     ctx.set_stream(stream.cuda_stream)
@@ -360,6 +479,7 @@ def main():
 
     if rank != 0:
         return
+    serving = serving_leg(args.serve_seconds) if args.serve_seconds > 0 else None
     roof = None
     if dom is not None:
         peak = peak16 if dom["lanes16"] else peak32
@@ -396,6 +516,7 @@ def main():
         "pairs_int16": st["pairs_int16"], "pairs_int32": st["pairs_int32"],
         "wall_s": wall,
         "clocks": clk,
+        "serving": serving,
     }
     print(json.dumps(line), flush=True)
 
