@@ -487,10 +487,10 @@ def main():
         roof = {"bound": "int", "achieved": ach / 1e9, "peak": peak / 1e9, "unit": "GCUPS",
                 "frac": ach / peak, "traffic": None,
                 "kernel": f"wave_kernel<R={dom['rows_per_lane']},{'int16x2' if dom['lanes16'] else 'int32'},"
-                          f"V={dom['variant']}>",
+                          f"V={dom['variant']},W={dom['lanes']}>",
                 "launch_ms": dom["ms"], "launch_cells": dom["cells"],
-                "peak_source": "nwg_dpx_peak: 5-instruction DPX cell update on every SM, registers only, "
-                               "measured in this run",
+                "peak_source": "nwg_dpx_peak: the 5-instruction cell update (faster of the two forms the "
+                               "kernels use) on every SM, registers only, measured in this run",
                 "peak_int32_gcups": peak32 / 1e9}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -505,7 +505,7 @@ def main():
         "e2e": e2e,
         "gpu_launches": launches,
         "launches_per_step": per_step_launches,
-        "launch_records": [{k: r[k] for k in ("rows_per_lane", "variant", "lanes16", "grid", "cells", "ms")}
+        "launch_records": [{k: r[k] for k in ("rows_per_lane", "variant", "lanes", "lanes16", "grid", "cells", "ms")}
                            for r in recs],
         "tuning": tuning,
         "sequential_launch_sum_ms": timed_sum_ms,

@@ -214,10 +214,11 @@ int nwg_score_pairs_noalloc(const int8_t* d_codes, const int64_t* d_start, const
  * device; timer.h falls back to clock()).  These give the bench its roofline
  * denominator and per-launch device times. */
 
-/* Peak of the cell update alone: every SM runs the 5-instruction DPX cell
- * update (viaddmax x3, vimax3, one add) on register-resident strips, no
- * memory, no shuffles.  lanes16 != 0: int16x2 words (2 cells per word), else
- * int32.  Returns cells per second. */
+/* Peak of the cell update alone: every SM runs the 5-instruction cell update
+ * on register-resident strips, no memory, no shuffles, in both forms the
+ * wave kernels use (2 adds + 2 viaddmax + 1 vimax3; 1 add + 4 viaddmax), and
+ * the faster form counts.  lanes16 != 0: int16x2 words (2 cells per word),
+ * else int32.  Returns cells per second. */
 int nwg_dpx_peak(nwg_ctx* ctx, int lanes16, double* cells_per_s);
 
 typedef struct {
@@ -228,8 +229,8 @@ typedef struct {
   int64_t pairs;        /* pairs (i<j) this launch computes                    */
   int64_t cells;        /* their L_i*L_j sum                                   */
   double ms;            /* device time (events around this launch alone)       */
-  int32_t variant;      /* register layout of the wave kernel (0 or 1)         */
-  int32_t pad;
+  int32_t variant;      /* register layout of the wave kernel (0, 1, 2)       */
+  int32_t lanes;        /* lanes per wavefront (32, 16, 8)                    */
 } nwg_launch_rec;
 
 /* Per-launch event timing for the next calls (0 = off, the default: timing
@@ -242,14 +243,14 @@ int nwg_launch_records(nwg_ctx* ctx, nwg_launch_rec* out, int cap);
 
 /* ---- autotuner --------------------------------------------------------------
  * The batched form has a kernel choice per length class of the shorter
- * sequences of a pair (the Y rows): rows per lane (4..32, band = 32 x that)
- * and register layout.  nwg_autotune times every candidate of every class on
+ * sequences of a pair (the Y rows): rows per lane (4..32), lanes per
+ * wavefront (32, 16 or 8; band = lanes x rows per lane) and register layout.  nwg_autotune times every candidate of every class on
  * synthetic inputs of that class's length and keeps the fastest; the result is
  * cached in a text file per device (directory $NWG_TUNE_CACHE, else
  * $HOME/.cache/nwgpu) and reused by later contexts.  Not part of the
  * reference's interface, which had one fixed window/strip shape
  * (definitions.cuh:26,47-48). */
-#define NWG_TUNE_CLASSES 8
+#define NWG_TUNE_CLASSES 16
 
 typedef struct {
   int32_t classes;                          /* NWG_TUNE_CLASSES                          */
@@ -257,6 +258,8 @@ typedef struct {
   int32_t max_rows[NWG_TUNE_CLASSES];       /* class k: Y rows <= max_rows[k]             */
   int32_t rows_per_lane[NWG_TUNE_CLASSES];
   int32_t variant[NWG_TUNE_CLASSES];
+  int32_t lanes[NWG_TUNE_CLASSES];          /* lanes per wavefront                        */
+  int32_t pad;
   double gcups[NWG_TUNE_CLASSES];           /* the winner's throughput on the probe       */
   double seconds;                           /* tuning time (0 from cache)                 */
 } nwg_tune_result;
@@ -264,8 +267,12 @@ typedef struct {
 /* flags: 1 = ignore (and overwrite) the cache. */
 int nwg_autotune(nwg_ctx* ctx, int flags, nwg_tune_result* out);
 
-/* Set the choice per class explicitly (NWG_TUNE_CLASSES entries each). */
+/* Set the choice per class explicitly (NWG_TUNE_CLASSES entries each), on
+ * 32-lane wavefronts; nwg_set_tuning_lanes also sets the lanes per front
+ * (32, 16 or 8; narrow fronts take variant 0 or 2). */
 int nwg_set_tuning(nwg_ctx* ctx, const int32_t* rows_per_lane, const int32_t* variant);
+int nwg_set_tuning_lanes(nwg_ctx* ctx, const int32_t* rows_per_lane, const int32_t* variant,
+                         const int32_t* lanes);
 
 /* ---- serving loop ------------------------------------------------------------
  * Alignment jobs (one sequence family each: distance matrix + guide tree, the

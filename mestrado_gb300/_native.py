@@ -112,21 +112,28 @@ class LaunchRec(ctypes.Structure):
         ("cells", ctypes.c_int64),
         ("ms", ctypes.c_double),
         ("variant", ctypes.c_int32),
-        ("pad", ctypes.c_int32),
+        ("lanes", ctypes.c_int32),
     ]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+TUNE_CLASSES = 16
+# Y rows of the tuning classes (the last one takes every longer Y)
+TUNE_CLASS_ROWS = [64, 96, 128, 160, 192, 224, 256, 320, 384, 448, 512, 640, 768, 1024, 1536, 2**31 - 1]
 
 
 class TuneResult(ctypes.Structure):
     _fields_ = [
         ("classes", ctypes.c_int32),
         ("from_cache", ctypes.c_int32),
-        ("max_rows", ctypes.c_int32 * 8),
-        ("rows_per_lane", ctypes.c_int32 * 8),
-        ("variant", ctypes.c_int32 * 8),
-        ("gcups", ctypes.c_double * 8),
+        ("max_rows", ctypes.c_int32 * TUNE_CLASSES),
+        ("rows_per_lane", ctypes.c_int32 * TUNE_CLASSES),
+        ("variant", ctypes.c_int32 * TUNE_CLASSES),
+        ("lanes", ctypes.c_int32 * TUNE_CLASSES),
+        ("pad", ctypes.c_int32),
+        ("gcups", ctypes.c_double * TUNE_CLASSES),
         ("seconds", ctypes.c_double),
     ]
 
@@ -134,7 +141,8 @@ class TuneResult(ctypes.Structure):
         n = self.classes
         return {"from_cache": bool(self.from_cache), "seconds": self.seconds,
                 "classes": [{"max_rows": self.max_rows[k], "rows_per_lane": self.rows_per_lane[k],
-                             "variant": self.variant[k], "gcups": self.gcups[k]} for k in range(n)]}
+                             "variant": self.variant[k], "lanes": self.lanes[k], "gcups": self.gcups[k]}
+                            for k in range(n)]}
 
 
 class Join(ctypes.Structure):
@@ -177,6 +185,7 @@ EXTRA_SIGS: dict = {
                    ctypes.c_int64),
     "nwg_autotune": ([ctypes.c_void_p, ctypes.c_int, P(TuneResult)], ctypes.c_int),
     "nwg_set_tuning": ([ctypes.c_void_p, c_i32p, c_i32p], ctypes.c_int),
+    "nwg_set_tuning_lanes": ([ctypes.c_void_p, c_i32p, c_i32p, c_i32p], ctypes.c_int),
     "nwg_align_pairs": ([ctypes.c_void_p, c_i8p, c_i64p, ctypes.c_int, c_i32p, c_i32p, ctypes.c_int,
                          ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int64, c_i32p, c_i32p, P(Stats)],
                         ctypes.c_int),

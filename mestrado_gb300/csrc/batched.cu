@@ -75,8 +75,8 @@ struct BatchPlan {
   SetView X, Y;
   DevBuf bxs, bxl, bxo, bxb, bys, byl, byo, byb;
   // groups, buckets
-  struct Bucket { int R, P, V, check, g0, ng; int64_t j0, njobs, pairs; double cells; int grid; size_t scratch_off;
-                  int maxrows; };
+  struct Bucket { int R, P, V, W, check, g0, ng; int64_t j0, njobs, pairs; double cells; int grid;
+                  size_t scratch_off; int maxrows; };
   std::vector<Bucket> buckets;
   DevBuf gy, gy2, gx, jobs, counters, rerun, rerun_scratch, wscratch;
   int64_t rerun_cap = 0, rerun_threads = 0;
@@ -167,19 +167,18 @@ static int get_plan(Ctx* c, const int64_t* xoff, int nx, const int64_t* yoff, in
   const SetView& X = p->X;
   const SetView& Y = p->Y;
   const bool force32 = mode == NWG_MODE_BATCHED_INT32 ||
-                       std::max(X.maxlen, Y.maxlen) > kInt16MaxLen;
+                       std::max(X.maxlen, Y.maxlen) > c->i16.max_len;
   // certain int16: the shorter sequence of every pair is short enough that
   // even its best-case score fits (max matrix entry * length)
   int maxs = 0;
   for (int k = 0; k < kLetters * kLetters; ++k) maxs = std::max<int>(maxs, c->sub[k]);
-  const int certain_len = maxs > 0 ? kInt16MaxH / maxs : 1 << 30;
+  const int certain_len = maxs > 0 ? c->i16.max_h / maxs : 1 << 30;
 
-  struct Group { int y, y2, nx, R, V, P, check; };
+  struct Group { int y, y2, nx, R, V, W, P, check; };
   std::vector<Group> groups;
   groups.reserve((size_t)Y.n / 2 + 1);
   for (int y = 0; y < Y.n;) {
     const TuneChoice tc = c->tune[tune_class(Y.len[y])];
-    const int R = tc.R, V = tc.V;
     if (!force32) {
       const int y2 = y + 1 < Y.n ? y + 1 : -1;
       const int last = y2 >= 0 ? y2 : y;
@@ -187,14 +186,16 @@ static int get_plan(Ctx* c, const int64_t* xoff, int nx, const int64_t* yoff, in
       // Y sorted by length: Y.len[y] is the group's longest; the pair's
       // shorter sequence is at most that long.
       const int check = Y.len[y] > certain_len ? 1 : 0;
-      groups.push_back({y, y2, nxg, R, V, 2, check});
+      groups.push_back({y, y2, nxg, tc.R, tc.V, tc.W, 2, check});
       y = last + 1;
     } else {
-      groups.push_back({y, -1, triangle ? y + 1 : X.n, R, V, 1, 0});
+      const TuneChoice t32 = int32_choice(tc);
+      groups.push_back({y, -1, triangle ? y + 1 : X.n, t32.R, t32.V, 32, 1, 0});
       ++y;
     }
   }
   std::stable_sort(groups.begin(), groups.end(), [](const Group& a, const Group& b) {
+    if (a.R * a.W != b.R * b.W) return a.R * a.W > b.R * b.W;
     if (a.R != b.R) return a.R > b.R;
     if (a.V != b.V) return a.V > b.V;
     if (a.P != b.P) return a.P > b.P;
@@ -209,15 +210,16 @@ static int get_plan(Ctx* c, const int64_t* xoff, int nx, const int64_t* yoff, in
   prefix.reserve(ng + 16);
   for (int k = 0; k < ng;) {
     int e = k;
-    while (e < ng && groups[e].R == groups[k].R && groups[e].V == groups[k].V && groups[e].P == groups[k].P &&
-           groups[e].check == groups[k].check)
+    while (e < ng && groups[e].R == groups[k].R && groups[e].V == groups[k].V && groups[e].W == groups[k].W &&
+           groups[e].P == groups[k].P && groups[e].check == groups[k].check)
       ++e;
-    BatchPlan::Bucket b{groups[k].R, groups[k].P, groups[k].V, groups[k].check, k, e - k, (int64_t)prefix.size(),
-                        0, 0, 0.0, 0, 0, 0};
+    BatchPlan::Bucket b{groups[k].R, groups[k].P, groups[k].V, groups[k].W, groups[k].check, k, e - k,
+                        (int64_t)prefix.size(), 0, 0, 0.0, 0, 0, 0};
+    const int xper = kWaveWarps * (32 / b.W);   // X per CTA job
     int64_t acc = 0;
     for (int g = k; g < e; ++g) {
       prefix.push_back(acc);
-      acc += (groups[g].nx + kWaveWarps - 1) / kWaveWarps;
+      acc += (groups[g].nx + xper - 1) / xper;
       b.maxrows = std::max(b.maxrows, Y.len[groups[g].y]);
       for (int yy : {groups[g].y, groups[g].y2}) {
         if (yy < 0) continue;
@@ -255,10 +257,10 @@ static int get_plan(Ctx* c, const int64_t* xoff, int nx, const int64_t* yoff, in
   p->scols = std::max(X.maxlen, 1);
   size_t scratch_words = 1;
   for (auto& b : p->buckets) {
-    b.grid = (int)std::min<int64_t>(b.njobs, (int64_t)c->sms * wave_max_ctas_per_sm(b.R, b.P, b.V));
+    b.grid = (int)std::min<int64_t>(b.njobs, (int64_t)c->sms * wave_max_ctas_per_sm(b.R, b.P, b.V, b.W));
     b.grid = std::max(b.grid, 1);
     b.scratch_off = scratch_words;
-    if (b.maxrows > 32 * b.R) scratch_words += (size_t)b.grid * kWaveWarps * 4 * p->scols;
+    if (b.maxrows > b.W * b.R) scratch_words += (size_t)b.grid * kWaveWarps * (32 / b.W) * 4 * p->scols;
   }
   if ((rc = p->wscratch.ensure(sizeof(int32_t) * scratch_words))) {
     delete p;
@@ -334,13 +336,14 @@ static int enqueue_step(Ctx* c, BatchPlan* p, const int8_t* d_codes, float* d_D,
     a.g_begin = b.g0;
     a.ngroups = b.ng;
     a.check_bound = b.check;
+    a.max_h = c->i16.max_h;
     a.scratch = (int32_t*)p->wscratch.p + b.scratch_off;
     int ri = -1;
     if (timed) {
-      nwg_launch_rec r{0, b.R, b.P == 2 ? 1 : 0, b.grid, b.pairs, (int64_t)b.cells, 0.0, b.V, 0};
+      nwg_launch_rec r{0, b.R, b.P == 2 ? 1 : 0, b.grid, b.pairs, (int64_t)b.cells, 0.0, b.V, b.W};
       if ((ri = c->rec_begin(r)) < 0) return c->fail(NWG_ERR_CUDA, "launch timing");
     }
-    if ((rc = c->cuda(launch_wave(b.R, b.P, b.V, a, b.grid, bs), "wave launch"))) return rc;
+    if ((rc = c->cuda(launch_wave(b.R, b.P, b.V, b.W, a, b.grid, bs), "wave launch"))) return rc;
     if (ri >= 0 && (rc = c->rec_end(ri))) return rc;
     ++c->launches;
   }
@@ -363,7 +366,7 @@ int Ctx::batched(const int8_t* d_codes, const int64_t* xoff, int nx, const int64
   BatchPlan* p = nullptr;
   int rc;
   if ((rc = get_plan(this, xoff, nx, yoff, ny, triangle, mode, &p))) return rc;
-  for (const auto& b : p->buckets) prepare_wave(b.R, b.P, b.V);
+  for (const auto& b : p->buckets) prepare_wave(b.R, b.P, b.V, b.W);
   if (st) {
     st->pairs_int16 += p->pairs16;
     st->pairs_int32 += p->pairs32;

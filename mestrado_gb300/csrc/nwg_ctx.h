@@ -33,13 +33,26 @@ const char* letter_order();
 
 struct TuneChoice {
   int R;   // rows per lane (4, 8, 12, 16, 20, 24, 32)
-  int V;   // register layout (0 or 1)
+  int V;   // register layout (0, 1, 2)
+  int W;   // lanes per wavefront (32, 16, 8): band of W*R rows
 };
-constexpr int kTuneClasses = 8;
+// The same band on full-width fronts, for groups that run on int32 lanes
+// (the narrow fronts exist for int16x2 lanes only).
+inline TuneChoice int32_choice(TuneChoice t) {
+  if (t.W == 32) return t;
+  const int band = t.W * t.R;
+  int R = 32;
+  for (int r : {4, 8, 12, 16, 20, 24, 32})
+    if (32 * r >= band) { R = r; break; }
+  return {R, t.V == 1 ? 0 : t.V, 32};
+}
+constexpr int kTuneClasses = NWG_TUNE_CLASSES;
 // Upper bound of the Y rows of each class; the last class takes every longer Y.
-constexpr int kClassRows[kTuneClasses] = {128, 256, 384, 512, 640, 768, 1024, 1 << 30};
-constexpr TuneChoice kDefaultTune[kTuneClasses] = {{4, 1}, {8, 1}, {12, 1}, {16, 1},
-                                                   {20, 1}, {24, 1}, {32, 1}, {32, 1}};
+constexpr int kClassRows[kTuneClasses] = {64,  96,  128, 160, 192, 224, 256,  320,
+                                          384, 448, 512, 640, 768, 1024, 1536, 1 << 30};
+constexpr TuneChoice kDefaultTune[kTuneClasses] = {
+    {4, 2, 32},  {4, 2, 32},  {4, 2, 32},  {8, 0, 32},  {8, 0, 32},  {8, 0, 32},  {8, 0, 32},  {12, 0, 32},
+    {12, 0, 32}, {16, 2, 32}, {16, 2, 32}, {20, 2, 32}, {24, 2, 32}, {32, 2, 32}, {24, 2, 32}, {24, 2, 32}};
 int tune_class(int rows);
 
 struct BatchPlan;
@@ -49,6 +62,7 @@ void destroy_plans(Ctx* c);
 struct Ctx {
   int go = 10, ge = 2;
   int8_t sub[kLetters * kLetters];
+  Int16Limits i16{kInt16MaxLen, 32756 - 11};   // set from (go, ge, sub) at creation
   int device = 0, sms = 1;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;

@@ -17,18 +17,38 @@ constexpr int kWaveWarps = 8;             // warps per CTA of the wavefront kern
 constexpr int kWaveThreads = 32 * kWaveWarps;
 constexpr int kPlainThreads = 128;
 constexpr int kPlainRows = 16;            // rows per thread strip in the plain kernel
-// Overflow guard of the int16x2 lanes (offset binary, halves in [4, 65524]):
-//  * lower side: every value of a pair is >= -4*(max(Lx, rows)+1) - 16, rows
-//    including the band padding (< 32*32 rows), so lengths <= kInt16MaxLen
-//    keep values >= -32764;
+// Overflow guard of the int16x2 lanes (offset binary, halves in [4, 65524]),
+// per context from (go, ge, matrix) by int16_limits():
+//  * lower side: with w = max(ge, -min entry, 1), every H of a pair is
+//    >= -(D+2)*w, D = max(Lx, rows) and rows including the band padding
+//    (< 32*32 rows): H[-1][c] = -ge(c+1), and each diagonal step loses at most
+//    w.  Every other value (E, F, H - go, diag + S, E - ge inside the DPX max)
+//    is within go + ge + |min entry| below that, so sequences up to the
+//    context's max_len (at most kInt16MaxLen) keep values >= -32764;
 //  * upper side: every H of a pair is <= min(bound_x, bound_y), bound = sum of
-//    the residues' best matrix scores; <= kInt16MaxH keeps values <= 32756.
-//    With the built-in matrix (best score 11) a pair whose shorter sequence
-//    has <= kCertainLen residues is always inside; longer pairs run on int16
-//    lanes optimistically, are checked against the device-side bounds and
-//    re-run on int32 lanes when the check fails.
+//    the residues' best matrix scores (floored at 0); H <= max_h keeps
+//    diag + S <= 32756.  A pair whose shorter sequence has <= max_h / (best
+//    entry) residues is always inside; longer pairs run on int16 lanes
+//    optimistically, are checked against the device-side bounds and re-run on
+//    int32 lanes when the check fails.
 constexpr int kInt16MaxLen = 6900;
-constexpr int kInt16MaxH = 32756 - 11;
+struct Int16Limits {
+  int max_len;   // longest sequence of a set that may use int16 lanes (0: none)
+  int max_h;     // largest H an int16 pair may reach
+};
+inline Int16Limits int16_limits(int go, int ge, const int8_t* sub) {
+  int smin = 127, smax = -128;
+  for (int k = 0; k < kLetters * kLetters; ++k) {
+    smin = sub[k] < smin ? sub[k] : smin;
+    smax = sub[k] > smax ? sub[k] : smax;
+  }
+  int w = ge > -smin ? ge : -smin;
+  w = w > 1 ? w : 1;
+  const int slack = go + ge + (smin < 0 ? -smin : 0);
+  int len = (32764 - slack) / w - 2 - 32 * 32;
+  len = len < 0 ? 0 : (len > kInt16MaxLen ? kInt16MaxLen : len);
+  return {len, 32756 - (smax > 0 ? smax : 0)};
+}
 
 // Sequence set laid out on the device for one call: sorted by length
 // (descending), each start 16-byte aligned.
@@ -77,6 +97,7 @@ struct WaveArgs {
   const int8_t* sub;          // 24*24 on device
   // overflow guard (optimistic int16 buckets)
   int check_bound;
+  int max_h;                  // the context's int16 upper limit of H (checked groups)
   const int32_t* xbound;      // per sorted X: composition bound
   const int32_t* ybound;
   int2* rerun;                // (sorted x, sorted y) pairs to re-run on int32 lanes
@@ -122,10 +143,11 @@ struct PairListArgs {
 // for int16x2 lanes (two pairs per warp), 1 for int32 lanes.
 // V: register layout of the wave kernel (0: H, H-go, E per row; 1: H, E per
 // row with a min-blocks launch bound).
-cudaError_t launch_wave(int R, int P, int V, const WaveArgs& a, int grid, cudaStream_t s);
-int wave_max_ctas_per_sm(int R, int P, int V);
-void prepare_wave(int R, int P, int V);   // sets the dynamic shared memory limit (outside graph capture)
-size_t wave_smem_bytes(int R);
+// wave kernel <R rows per lane, P pairs per word, V layout, W lanes per front>
+cudaError_t launch_wave(int R, int P, int V, int W, const WaveArgs& a, int grid, cudaStream_t s);
+int wave_max_ctas_per_sm(int R, int P, int V, int W);
+void prepare_wave(int R, int P, int V, int W);   // sets the dynamic shared memory limit (outside graph capture)
+bool wave_exists(int R, int P, int V, int W);
 cudaError_t launch_plain(const PlainArgs& a, cudaStream_t s);
 cudaError_t launch_rerun(const WaveArgs& a, int2* scratch, int64_t nthreads, cudaStream_t s);
 // per-CTA neighbor joining for many small jobs (nj.cu)
@@ -134,8 +156,8 @@ void nj_job_setup(void* job_out, float* D, int n, char* base, nwg_join** joins, 
 size_t nj_job_desc_bytes();
 int nj_cta_max_n();
 cudaError_t launch_nj_jobs(const void* d_jobs, int njobs, cudaStream_t s);
-cudaError_t launch_dpx_peak(int P, int cols, int grid, uint32_t* sink, int go, int ge, cudaStream_t s);
-int dpx_peak_ctas_per_sm(int P);
+cudaError_t launch_dpx_peak(int P, int form, int cols, int grid, uint32_t* sink, int go, int ge, cudaStream_t s);
+int dpx_peak_ctas_per_sm(int P, int form);
 cudaError_t launch_pairlist(const PairListArgs& a, int64_t count, cudaStream_t s);
 
 }  // namespace nwg

@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(kPlainThreads) pairlist_kernel(const PairListA
 // Peak of the cell update alone (roofline denominator): the inner loop of
 // wave_band on a 16-row register strip, with the profile words and the
 // incoming boundary taken from registers -- no memory, no shuffles.
-template <int P>
+template <int P, int F>
 __global__ void __launch_bounds__(256) dpx_peak_kernel(uint32_t p0, uint32_t p1, uint32_t p2,
                                                        uint32_t p3, int go, int ge, int cols,
                                                        uint32_t* sink) {
@@ -146,24 +146,42 @@ __global__ void __launch_bounds__(256) dpx_peak_kernel(uint32_t p0, uint32_t p1,
   }
   uint32_t hprev = 0, hin = L::splat(-ge), fin = L::splat(kShortMin + ge);
   const uint32_t pv[4] = {p0, p1, p2, p3};
+  const uint32_t NGOP = L::packed(-go);
   for (int c = 0; c < cols; ++c) {
     uint32_t diag = hprev;
     hprev = hin;
     uint32_t f = fin;
-    uint32_t tup = L::add(hin, NGO);
+    if (F == 2) {
+      // the shifted form of wave kernel layout V = 2: 4 DPX + 1 add per word
+      uint32_t hup = hin;
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-      f = L::addmax(f, NGE, tup);
-      const uint32_t e = L::addmax(E[r], NGE, T[r]);
-      const uint32_t hd = L::add(diag, pv[r & 3]);
-      const uint32_t h = L::max3(e, f, hd);
-      diag = H[r];
-      H[r] = h;
-      E[r] = e;
-      T[r] = L::add(h, NGO);
-      tup = T[r];
+      for (int r = 0; r < R; ++r) {
+        f = L::addmax(f, NGE, hup);
+        const uint32_t e = L::addmax(E[r], NGE, H[r]);
+        const uint32_t m = L::addmax(e, NGOP, L::add(diag, pv[r & 3]));
+        const uint32_t h = L::addmax(f, NGOP, m);
+        diag = H[r];
+        H[r] = h;
+        E[r] = e;
+        hup = h;
+      }
+      hin = H[3];
+    } else {
+      uint32_t tup = L::add(hin, NGO);
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        f = L::addmax(f, NGE, tup);
+        const uint32_t e = L::addmax(E[r], NGE, T[r]);
+        const uint32_t hd = L::add(diag, pv[r & 3]);
+        const uint32_t h = L::max3(e, f, hd);
+        diag = H[r];
+        H[r] = h;
+        E[r] = e;
+        T[r] = L::add(h, NGO);
+        tup = T[r];
+      }
+      hin = T[3];
     }
-    hin = T[3];
     fin = f;
   }
   uint32_t acc = 0;
@@ -175,8 +193,8 @@ __global__ void __launch_bounds__(256) dpx_peak_kernel(uint32_t p0, uint32_t p1,
 }  // namespace
 
 #define NWG_CASE(r) \
-  if (R == r) return wave_launch_r##r(P, V, a, grid, s);
-cudaError_t launch_wave(int R, int P, int V, const WaveArgs& a, int grid, cudaStream_t s) {
+  if (R == r) return wave_launch_r##r(P, V, W, a, grid, s);
+cudaError_t launch_wave(int R, int P, int V, int W, const WaveArgs& a, int grid, cudaStream_t s) {
   NWG_WAVE_ROWS(NWG_CASE)
   return cudaErrorInvalidValue;
 }
@@ -184,34 +202,48 @@ cudaError_t launch_wave(int R, int P, int V, const WaveArgs& a, int grid, cudaSt
 
 #define NWG_CASE(r) \
   if (R == r) {     \
-    wave_prepare_r##r(P, V); \
+    wave_prepare_r##r(P, V, W); \
     return;         \
   }
-void prepare_wave(int R, int P, int V) { NWG_WAVE_ROWS(NWG_CASE) }
+void prepare_wave(int R, int P, int V, int W) { NWG_WAVE_ROWS(NWG_CASE) }
 #undef NWG_CASE
 
 #define NWG_CASE(r) \
-  if (R == r) return wave_occupancy_r##r(P, V);
-int wave_max_ctas_per_sm(int R, int P, int V) {
+  if (R == r) return wave_occupancy_r##r(P, V, W);
+int wave_max_ctas_per_sm(int R, int P, int V, int W) {
   NWG_WAVE_ROWS(NWG_CASE)
   return 1;
 }
 #undef NWG_CASE
 
-size_t wave_smem_bytes(int R) { return (size_t)kLetters * 32 * R * sizeof(uint32_t); }
+#define NWG_CASE(r) (R == r) ||
+bool wave_exists(int R, int P, int V, int W) {
+  return (NWG_WAVE_ROWS(NWG_CASE) false) && wave::wave_variant_exists(P, V, W);
+}
+#undef NWG_CASE
 
-cudaError_t launch_dpx_peak(int P, int cols, int grid, uint32_t* sink, int go, int ge, cudaStream_t s) {
+cudaError_t launch_dpx_peak(int P, int form, int cols, int grid, uint32_t* sink, int go, int ge, cudaStream_t s) {
   const uint32_t p0 = 4u * 65536u + 3u, p1 = (uint32_t)(-2 * 65536 + 1), p2 = (uint32_t)(2 * 65536 - 1),
                  p3 = 5u * 65536u;
-  if (P == 2) dpx_peak_kernel<2><<<grid, 256, 0, s>>>(p0, p1, p2, p3, go, ge, cols, sink);
-  else dpx_peak_kernel<1><<<grid, 256, 0, s>>>(p0, 1u, 0xFFFFFFFEu, 3u, go, ge, cols, sink);
+  if (P == 2) {
+    if (form == 2) dpx_peak_kernel<2, 2><<<grid, 256, 0, s>>>(p0, p1, p2, p3, go, ge, cols, sink);
+    else dpx_peak_kernel<2, 0><<<grid, 256, 0, s>>>(p0, p1, p2, p3, go, ge, cols, sink);
+  } else {
+    if (form == 2) dpx_peak_kernel<1, 2><<<grid, 256, 0, s>>>(p0, 1u, 0xFFFFFFFEu, 3u, go, ge, cols, sink);
+    else dpx_peak_kernel<1, 0><<<grid, 256, 0, s>>>(p0, 1u, 0xFFFFFFFEu, 3u, go, ge, cols, sink);
+  }
   return cudaGetLastError();
 }
 
-int dpx_peak_ctas_per_sm(int P) {
+int dpx_peak_ctas_per_sm(int P, int form) {
   int n = 0;
-  if (P == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dpx_peak_kernel<2>, 256, 0);
-  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dpx_peak_kernel<1>, 256, 0);
+  if (P == 2) {
+    if (form == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dpx_peak_kernel<2, 2>, 256, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dpx_peak_kernel<2, 0>, 256, 0);
+  } else {
+    if (form == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dpx_peak_kernel<1, 2>, 256, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dpx_peak_kernel<1, 0>, 256, 0);
+  }
   return n > 0 ? n : 1;
 }
 

@@ -138,7 +138,7 @@ int Server::launch_batch(Slot& S) {
   }
   std::vector<int64_t> start((size_t)total_seqs);
   std::vector<int32_t> len((size_t)total_seqs), orig((size_t)total_seqs);
-  struct Group { int y, y2, nx, xbase, R, V, P; int64_t dofs; int ld; };
+  struct Group { int y, y2, nx, xbase, R, V, W, P; int64_t dofs; int ld; };
   std::vector<Group> groups;
   int maxlen = 1;
   int64_t base = 0;
@@ -155,43 +155,48 @@ int Server::launch_batch(Slot& S) {
       orig[base + k] = o;
       maxlen = std::max(maxlen, len[base + k]);
     }
-    const bool long_set = len[base] > kInt16MaxLen;
+    const bool long_set = len[base] > c.i16.max_len;
     int maxs = 0;
     for (int k = 0; k < kLetters * kLetters; ++k) maxs = std::max<int>(maxs, c.sub[k]);
-    const int certain = maxs > 0 ? kInt16MaxH / maxs : 1 << 30;
+    const int certain = maxs > 0 ? c.i16.max_h / maxs : 1 << 30;
     for (int y = 0; y < n;) {
       const int gyi = (int)base + y;
       const TuneChoice tc = c.tune[tune_class(len[gyi])];
       if (!long_set && len[gyi] <= certain) {
         const int y2 = y + 1 < n ? gyi + 1 : -1;
         const int last = y2 >= 0 ? y + 1 : y;
-        groups.push_back({gyi, y2, last + 1, (int)base, tc.R, tc.V, 2, (int64_t)J->d_off, n});
+        groups.push_back({gyi, y2, last + 1, (int)base, tc.R, tc.V, tc.W, 2, (int64_t)J->d_off, n});
         y = last + 1;
       } else {
-        groups.push_back({gyi, -1, y + 1, (int)base, tc.R, tc.V, 1, (int64_t)J->d_off, n});
+        const TuneChoice t32 = int32_choice(tc);
+        groups.push_back({gyi, -1, y + 1, (int)base, t32.R, t32.V, 32, 1, (int64_t)J->d_off, n});
         ++y;
       }
     }
     base += n;
   }
   std::stable_sort(groups.begin(), groups.end(), [](const Group& a, const Group& b) {
+    if (a.R * a.W != b.R * b.W) return a.R * a.W > b.R * b.W;
     if (a.R != b.R) return a.R > b.R;
     if (a.V != b.V) return a.V > b.V;
     return a.P > b.P;
   });
   const int ng = (int)groups.size();
-  struct Bucket { int R, V, P, g0, ng; int64_t j0, njobs; int grid; size_t soff; bool multi; };
+  struct Bucket { int R, V, W, P, g0, ng; int64_t j0, njobs; int grid; size_t soff; bool multi; };
   std::vector<Bucket> buckets;
   std::vector<int64_t> prefix;
   for (int k = 0; k < ng;) {
     int e = k;
-    while (e < ng && groups[e].R == groups[k].R && groups[e].V == groups[k].V && groups[e].P == groups[k].P) ++e;
-    Bucket b{groups[k].R, groups[k].V, groups[k].P, k, e - k, (int64_t)prefix.size(), 0, 0, 0, false};
+    while (e < ng && groups[e].R == groups[k].R && groups[e].V == groups[k].V && groups[e].W == groups[k].W &&
+           groups[e].P == groups[k].P)
+      ++e;
+    Bucket b{groups[k].R, groups[k].V, groups[k].W, groups[k].P, k, e - k, (int64_t)prefix.size(), 0, 0, 0, false};
+    const int xper = kWaveWarps * (32 / b.W);   // X per CTA job
     int64_t acc = 0;
     for (int g = k; g < e; ++g) {
       prefix.push_back(acc);
-      acc += (groups[g].nx + kWaveWarps - 1) / kWaveWarps;
-      if (len[groups[g].y] > 32 * groups[g].R) b.multi = true;
+      acc += (groups[g].nx + xper - 1) / xper;
+      if (len[groups[g].y] > b.W * groups[g].R) b.multi = true;
     }
     prefix.push_back(acc);
     b.njobs = acc;
@@ -200,10 +205,11 @@ int Server::launch_batch(Slot& S) {
   }
   size_t scratch_words = 1;
   for (auto& b : buckets) {
-    b.grid = (int)std::max<int64_t>(1, std::min<int64_t>(b.njobs, (int64_t)c.sms * wave_max_ctas_per_sm(b.R, b.P, b.V)));
+    b.grid = (int)std::max<int64_t>(
+        1, std::min<int64_t>(b.njobs, (int64_t)c.sms * wave_max_ctas_per_sm(b.R, b.P, b.V, b.W)));
     b.soff = scratch_words;
-    if (b.multi) scratch_words += (size_t)b.grid * kWaveWarps * 4 * maxlen;
-    prepare_wave(b.R, b.P, b.V);
+    if (b.multi) scratch_words += (size_t)b.grid * kWaveWarps * (32 / b.W) * 4 * maxlen;
+    prepare_wave(b.R, b.P, b.V, b.W);
   }
   // device buffers of the slot (grow-only)
   int rc;
@@ -296,7 +302,7 @@ int Server::launch_batch(Slot& S) {
     a.g_begin = b.g0;
     a.ngroups = b.ng;
     a.scratch = (int32_t*)S.scratch.p + b.soff;
-    if ((rc = c.cuda(launch_wave(b.R, b.P, b.V, a, b.grid, st), "serve wave launch"))) return rc;
+    if ((rc = c.cuda(launch_wave(b.R, b.P, b.V, b.W, a, b.grid, st), "serve wave launch"))) return rc;
   }
   if ((rc = c.cuda(cudaMemcpyAsync(S.h_D.p, S.D.p, sizeof(float) * total_D, cudaMemcpyDeviceToHost, st), "serve")))
     return rc;

@@ -44,11 +44,11 @@ void make_parent_dirs(const std::string& file) {
 
 const int kCandR[] = {4, 8, 12, 16, 20, 24, 32};
 
-int representative_rows(int k) {
-  if (k == kTuneClasses - 1) return 1300;
-  const int lo = k == 0 ? 0 : kClassRows[k - 1];
-  return lo + (kClassRows[k] - lo) * 3 / 4;
-}
+// Probe length of a class: its longest Y (so a candidate whose band holds the
+// probe holds every Y of the class); the open last class probes 2000 rows.
+int representative_rows(int k) { return k == kTuneClasses - 1 ? 2000 : kClassRows[k]; }
+
+const char kCacheTag[] = "nwgpu-tune-3";
 
 }  // namespace
 
@@ -63,14 +63,16 @@ int Ctx::autotune(bool force, nwg_tune_result* out) {
       int ok = 0;
       TuneChoice t[kTuneClasses];
       double g[kTuneClasses];
-      for (int k = 0; k < kTuneClasses; ++k) {
-        int kk, R, V;
-        double gc;
-        if (std::fscanf(f, "%d %d %d %lf", &kk, &R, &V, &gc) == 4 && kk == k &&
-            std::find(std::begin(kCandR), std::end(kCandR), R) != std::end(kCandR) && (V == 0 || V == 1)) {
-          t[k] = {R, V};
-          g[k] = gc;
-          ++ok;
+      char tag[32] = {0};
+      if (std::fscanf(f, "%31s", tag) == 1 && std::strcmp(tag, kCacheTag) == 0) {
+        for (int k = 0; k < kTuneClasses; ++k) {
+          int kk, R, V, W;
+          double gc;
+          if (std::fscanf(f, "%d %d %d %d %lf", &kk, &R, &V, &W, &gc) == 5 && kk == k && wave_exists(R, 2, V, W)) {
+            t[k] = {R, V, W};
+            g[k] = gc;
+            ++ok;
+          }
         }
       }
       std::fclose(f);
@@ -79,6 +81,7 @@ int Ctx::autotune(bool force, nwg_tune_result* out) {
           tune[k] = t[k];
           res.rows_per_lane[k] = t[k].R;
           res.variant[k] = t[k].V;
+          res.lanes[k] = t[k].W;
           res.gcups[k] = g[k];
         }
         ++tune_version;
@@ -103,7 +106,7 @@ int Ctx::autotune(bool force, nwg_tune_result* out) {
     const int Ly = representative_rows(k);
     const int Lx = Ly + Ly / 10;
     const int ny = 128;
-    int nx = (int)std::min<double>(4096.0, std::max<double>(256.0, 2e10 / ((double)ny * Ly * Lx)));
+    int nx = (int)std::min<double>(4096.0, std::max<double>(256.0, 1e10 / ((double)ny * Ly * Lx)));
     nx = (nx + kWaveWarps - 1) / kWaveWarps * kWaveWarps;
     std::vector<int64_t> xoff(nx + 1), yoff(ny + 1);
     for (int i = 0; i <= nx; ++i) xoff[i] = (int64_t)i * Lx;
@@ -129,11 +132,13 @@ int Ctx::autotune(bool force, nwg_tune_result* out) {
     if ((rc = cuda(cudaMemcpy(dcodes, codes.data(), total, cudaMemcpyHostToDevice), "autotune upload"))) break;
     double best = -1.0;
     TuneChoice pick = kDefaultTune[k];
+    for (int W : {32, 16, 8})
     for (int R : kCandR) {
-      const int band = 32 * R;
+      const int band = W * R;
       if (band * 3 < Ly || band > 2 * Ly + 128) continue;   // at most 3 bands, at most ~half idle
-      for (int V = 0; V <= 1; ++V) {
-        tune[k] = {R, V};
+      for (int V = 0; V <= 2; ++V) {
+        if (!wave_exists(R, 2, V, W)) continue;
+        tune[k] = {R, V, W};
         ++tune_version;
         float ms = 0.f;
         for (int rep = 0; rep < 2 && rc == NWG_OK; ++rep) {
@@ -149,7 +154,7 @@ int Ctx::autotune(bool force, nwg_tune_result* out) {
         const double g = (double)nx * ny * Ly * Lx / (ms * 1e-3) / 1e9;
         if (g > best) {
           best = g;
-          pick = {R, V};
+          pick = {R, V, W};
         }
       }
       if (rc) break;
@@ -157,6 +162,7 @@ int Ctx::autotune(bool force, nwg_tune_result* out) {
     tune[k] = pick;
     res.rows_per_lane[k] = pick.R;
     res.variant[k] = pick.V;
+    res.lanes[k] = pick.W;
     res.gcups[k] = best;
   }
   probe.release();
@@ -171,8 +177,9 @@ int Ctx::autotune(bool force, nwg_tune_result* out) {
   res.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   make_parent_dirs(path);
   if (FILE* f = std::fopen(path.c_str(), "w")) {
+    std::fprintf(f, "%s\n", kCacheTag);
     for (int k = 0; k < kTuneClasses; ++k)
-      std::fprintf(f, "%d %d %d %.3f\n", k, tune[k].R, tune[k].V, res.gcups[k]);
+      std::fprintf(f, "%d %d %d %d %.3f\n", k, tune[k].R, tune[k].V, tune[k].W, res.gcups[k]);
     std::fclose(f);
   }
   if (out) *out = res;
@@ -186,16 +193,18 @@ extern "C" int nwg_autotune(nwg_ctx* ctx, int flags, nwg_tune_result* out) {
   return reinterpret_cast<nwg::Ctx*>(ctx)->autotune((flags & 1) != 0, out);
 }
 
-extern "C" int nwg_set_tuning(nwg_ctx* ctx, const int32_t* rows_per_lane, const int32_t* variant) {
+extern "C" int nwg_set_tuning_lanes(nwg_ctx* ctx, const int32_t* rows_per_lane, const int32_t* variant,
+                                    const int32_t* lanes) {
   if (!ctx || !rows_per_lane || !variant) return NWG_ERR_INVALID;
   nwg::Ctx* c = reinterpret_cast<nwg::Ctx*>(ctx);
-  for (int k = 0; k < nwg::kTuneClasses; ++k) {
-    if (std::find(std::begin(nwg::kCandR), std::end(nwg::kCandR), rows_per_lane[k]) == std::end(nwg::kCandR) ||
-        (variant[k] != 0 && variant[k] != 1))
-      return NWG_ERR_INVALID;
-  }
-  for (int k = 0; k < nwg::kTuneClasses; ++k) c->tune[k] = {rows_per_lane[k], variant[k]};
+  for (int k = 0; k < nwg::kTuneClasses; ++k)
+    if (!nwg::wave_exists(rows_per_lane[k], 2, variant[k], lanes ? lanes[k] : 32)) return NWG_ERR_INVALID;
+  for (int k = 0; k < nwg::kTuneClasses; ++k) c->tune[k] = {rows_per_lane[k], variant[k], lanes ? lanes[k] : 32};
   ++c->tune_version;
   c->tuned = true;
   return NWG_OK;
+}
+
+extern "C" int nwg_set_tuning(nwg_ctx* ctx, const int32_t* rows_per_lane, const int32_t* variant) {
+  return nwg_set_tuning_lanes(ctx, rows_per_lane, variant, nullptr);
 }

@@ -10,9 +10,12 @@
 //   H[r][c] = max(E, F, H[r-1][c-1] + S[y_r][x_c])                 (:145-146)
 //   score   = H[Ly-1][Lx-1]                                        (:160)
 //
-// A warp aligns one X (streamed as columns) against a band of 32*R rows:
-// lane k owns rows [kR, kR+R) and runs one column behind lane k-1; the bottom
-// (H, F) of each lane's strip goes to lane k+1 by __shfl_up_sync.  P = 2 packs
+// A wavefront of W lanes (W = 32, 16 or 8: 32/W wavefronts per warp, each on
+// its own X) aligns one X (streamed as columns) against a band of W*R rows:
+// lane k of the front owns rows [kR, kR+R) and runs one column behind lane
+// k-1; the bottom (H, F) of each lane's strip goes to lane k+1 by
+// __shfl_up_sync within the front.  Narrow fronts give bands of 8R and 16R
+// rows (finer than 32R) and a ramp of W-1 columns instead of 31.  P = 2 packs
 // two Y sequences into the halves of every register (offset-binary int16x2,
 // unsigned DPX max + full-rate 32-bit adds), P = 1 runs int32 lanes.  All
 // warps of a CTA share one Y group, so the per-letter score profile of the
@@ -21,6 +24,11 @@
 // device counter.  V selects the register layout: V = 0 keeps H, H-go and E
 // per row (fewest instructions), V = 1 keeps H and E and recomputes H-go with
 // one add (fewer registers, more resident warps: min-blocks launch bound).
+// V = 2 keeps E' = E + go and F' = F + go instead of E and F:
+//   F'[r] = max(F'[r-1] - ge, H[r-1]),  E'[c] = max(E'[c-1] - ge, H[c-1]),
+//   H = max(F' - go, max(E' - go, diag + S)),
+// the same values (go >= ge is not even needed: it is a change of variables),
+// with two dependent operations per row down the strip instead of three.
 #pragma once
 
 #include <type_traits>
@@ -114,7 +122,7 @@ __device__ __forceinline__ void put_score_job(const WaveArgs& a, float* D, int64
 // int16 range is not reported from the int16 lanes; it goes to the int32
 // re-run queue instead.
 __device__ __forceinline__ bool int16_safe(const WaveArgs& a, int i, int y) {
-  return !a.check_bound || min(a.xbound[i], a.ybound[y]) <= kInt16MaxH;
+  return !a.check_bound || min(a.xbound[i], a.ybound[y]) <= a.max_h;
 }
 
 __device__ __forceinline__ void queue_rerun(const WaveArgs& a, int i, int y) {
@@ -130,18 +138,41 @@ struct BandState {
 };
 
 // One column of the lane's R-row strip: H/E (and H-go for V == 0) updated in
-// place; f carries F down the strip; returns the bottom F.
-template <int R, int P, int V>
+// place; f carries F down the strip; returns the bottom F (F' for V == 2).
+// NGO: word added to H to get H - go; NGOP: -go as the per-half addmax operand.
+template <int R, int P, int V, int W>
 __device__ __forceinline__ uint32_t strip_column(BandState<R, P, V>& s, const uint4* __restrict__ pp,
                                                  uint32_t diag, uint32_t hin, uint32_t fin, uint32_t NGE,
-                                                 uint32_t NGO) {
+                                                 uint32_t NGO, uint32_t NGOP) {
   using L = Lanes<P>;
   constexpr int Q = R / 4;
   uint32_t f = fin;
+  if (V == 2) {
+    // fin is F' of the row above the strip, hin its H
+    uint32_t hup = hin;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const uint4 pv = pp[q * W];
+      const uint32_t sv[4] = {pv.x, pv.y, pv.z, pv.w};
+#pragma unroll
+      for (int w = 0; w < 4; ++w) {
+        const int r = q * 4 + w;
+        f = L::addmax(f, NGE, hup);                                      // F'[r][c]
+        const uint32_t e = L::addmax(s.E[r], NGE, s.H[r]);               // E'[r][c]
+        const uint32_t m = L::addmax(e, NGOP, L::add(diag, sv[w]));      // max(E, diag + S)
+        const uint32_t h = L::addmax(f, NGOP, m);                        // H[r][c]
+        diag = s.H[r];
+        s.H[r] = h;
+        s.E[r] = e;
+        hup = h;
+      }
+    }
+    return f;
+  }
   uint32_t tup = L::add(hin, NGO);
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
-    const uint4 pv = pp[q * 32];
+    const uint4 pv = pp[q * W];
     const uint32_t sv[4] = {pv.x, pv.y, pv.z, pv.w};
 #pragma unroll
     for (int w = 0; w < 4; ++w) {
@@ -161,24 +192,29 @@ __device__ __forceinline__ uint32_t strip_column(BandState<R, P, V>& s, const ui
   return f;
 }
 
-// One band (32*R rows starting at b*32*R) of one X for the calling warp.
-template <int R, int P, int V>
-__device__ __forceinline__ void wave_band(const WaveArgs& a, int lane, int b, int nb,
-                                          const int8_t* __restrict__ X, int Lx,
+// One band (W*R rows starting at b*W*R) of one X for the calling front.
+// sl: lane within the front; Lx: this front's X length, 0 when the front has
+// no pair to report (its lanes then only take part in the shuffles); Lmin /
+// Lmax: smallest / largest Lx over the warp's working fronts (warp-uniform).
+template <int R, int P, int V, int W>
+__device__ __forceinline__ void wave_band(const WaveArgs& a, int sl, int b, int nb,
+                                          const int8_t* __restrict__ X, int Lx, int Lmin, int Lmax,
                                           const uint32_t* __restrict__ prof,
                                           int32_t* __restrict__ scratch, int rowA, int rowB,
                                           bool wantA, bool wantB, int xo, int yoA, int yoB,
                                           float* jobD, int64_t jobld) {
   using L = Lanes<P>;
-  constexpr int BAND = 32 * R;
+  constexpr int BAND = W * R;
   constexpr int Q = R / 4;
   const uint32_t NGE = L::packed(-a.ge);        // per-half operand of addmax
   const uint32_t NGO = L::arith(-a.go, -a.go);   // word added to H to get H - go
+  const uint32_t NGOP = L::packed(-a.go);        // per-half operand: - go
   const uint32_t NGEA = L::arith(-a.ge, -a.ge);  // word added to H[-1][c] to get H[-1][c+1]
-  const uint32_t SENT = L::splat(kShortMin + a.ge);
+  // E[r][-1] = F[-1][c] = -32768 + ge; V == 2 keeps them shifted by go
+  const uint32_t SENT = L::splat(kShortMin + a.ge + (V == 2 ? a.go : 0));
 
   BandState<R, P, V> s;
-  const int rowbase = b * BAND + lane * R;
+  const int rowbase = b * BAND + sl * R;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     s.H[r] = L::splat(-a.ge * (rowbase + r + 1));   // H[row][-1]
@@ -189,37 +225,38 @@ __device__ __forceinline__ void wave_band(const WaveArgs& a, int lane, int b, in
   uint32_t hbot = 0, fbot = 0;
   uint32_t hb = L::splat(-a.ge);                    // H[-1][c] of the column lane 0 works on (band 0)
   const bool top = b == 0;
+  const bool work = Lx > 0;
   const int32_t* rd = scratch + ((b + 1) & 1) * 2 * a.scratch_cols;   // written by band b-1
   int32_t* wr = scratch + (b & 1) * 2 * a.scratch_cols;
-  const bool writer = lane == 31 && b + 1 < nb;
-  const uint4* pl = reinterpret_cast<const uint4*>(prof) + lane;
-  int xnext = (lane == 0 && Lx > 0) ? (int)X[0] : 0;
+  const bool writer = sl == W - 1 && b + 1 < nb && work;
+  const uint4* pl = reinterpret_cast<const uint4*>(prof) + sl;
+  int xnext = (sl == 0 && work) ? (int)X[0] : 0;
 
   auto step = [&](int t, auto checked) {
     constexpr bool kChecked = decltype(checked)::value;
-    const int c = t - lane;
-    uint32_t hin = __shfl_up_sync(0xffffffffu, hbot, 1);
-    uint32_t fin = __shfl_up_sync(0xffffffffu, fbot, 1);
+    const int c = t - sl;
+    uint32_t hin = __shfl_up_sync(0xffffffffu, hbot, 1, W);
+    uint32_t fin = __shfl_up_sync(0xffffffffu, fbot, 1, W);
     const int xl = xnext;
     if (kChecked) {
       if (c + 1 >= 0 && c + 1 < Lx) xnext = X[c + 1];
-    } else {
+    } else if (W == 32 || work) {
       xnext = X[min(c + 1, Lx - 1)];
     }
-    if (!kChecked || (c >= 0 && c < Lx)) {
+    if (kChecked ? (c >= 0 && c < Lx) : (W == 32 || work)) {
       uint32_t bh = hb, bf = SENT;
-      if (!top && lane == 0) {
+      if (!top && sl == 0) {
         bh = (uint32_t)rd[2 * c];
         bf = (uint32_t)rd[2 * c + 1];
       }
-      if (lane == 0) {
+      if (sl == 0) {
         hin = bh;
         fin = bf;
       }
       hb = L::add(hb, NGEA);
       const uint32_t diag = hprev;
       hprev = hin;
-      fbot = strip_column<R, P, V>(s, pl + clamp_code(xl) * (Q * 32), diag, hin, fin, NGE, NGO);
+      fbot = strip_column<R, P, V, W>(s, pl + clamp_code(xl) * (Q * W), diag, hin, fin, NGE, NGO, NGOP);
       hbot = s.H[R - 1];
       if (writer) {
         wr[2 * c] = (int32_t)hbot;
@@ -227,18 +264,18 @@ __device__ __forceinline__ void wave_band(const WaveArgs& a, int lane, int b, in
       }
     }
   };
-  // ramp-up (some lanes before column 0), steady state (every lane on a
-  // column), ramp-down (some lanes past the last column)
+  // ramp-up (some lanes before column 0), steady state (every lane of every
+  // working front on a column), ramp-down (some lanes past their last column)
   int t = 0;
-  const int t1 = Lx < 31 ? Lx : 31;
+  const int t1 = Lmin < W - 1 ? Lmin : W - 1;
   for (; t < t1; ++t) step(t, std::true_type{});
-  for (; t < Lx; ++t) step(t, std::false_type{});
-  for (; t < Lx + 31; ++t) step(t, std::true_type{});
+  for (; t < Lmin; ++t) step(t, std::false_type{});
+  for (; t < Lmax + W - 1; ++t) step(t, std::true_type{});
 
   // H[] now holds the last column; the lane owning a pair's last row reports.
   if (wantA) {
     const int rr = rowA - b * BAND;
-    if (rr >= 0 && rr < BAND && lane == rr / R) {
+    if (rr >= 0 && rr < BAND && sl == rr / R) {
       const int v = L::lo(pick<R>(s.H, rr % R));
       if (jobD) put_score_job(a, jobD, jobld, xo, yoA, v);
       else put_score(a, xo, yoA, v);
@@ -246,7 +283,7 @@ __device__ __forceinline__ void wave_band(const WaveArgs& a, int lane, int b, in
   }
   if (P == 2 && wantB) {
     const int rr = rowB - b * BAND;
-    if (rr >= 0 && rr < BAND && lane == rr / R) {
+    if (rr >= 0 && rr < BAND && sl == rr / R) {
       const int v = L::hi(pick<R>(s.H, rr % R));
       if (jobD) put_score_job(a, jobD, jobld, xo, yoB, v);
       else put_score(a, xo, yoB, v);
@@ -259,19 +296,24 @@ struct MinBlocks {
   static constexpr int value = V == 0 ? 1 : (R <= 8 ? 4 : (R <= 16 ? 3 : 2));
 };
 
-template <int R, int P, int V>
+template <int R, int P, int V, int W>
 __global__ void __launch_bounds__(kWaveThreads, (MinBlocks<R, P, V>::value)) wave_kernel(const WaveArgs a) {
-  constexpr int BAND = 32 * R;
+  constexpr int S = 32 / W;                // fronts per warp
+  constexpr int BAND = W * R;
   constexpr int Q = R / 4;
   static_assert(R % 4 == 0, "rows per lane must be a multiple of 4");
-  extern __shared__ __align__(16) uint32_t prof[];   // [letter][Q][lane][4]
+  static_assert(W == 8 || W == 16 || W == 32, "front width");
+  extern __shared__ __align__(16) uint32_t prof[];   // [letter][Q][front lane][4]
   __shared__ int8_t s_sub[kLetters * kLetters];
   __shared__ long long s_job;
 
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
+  const int sl = lane % W;                 // lane within the front
+  const int seg = lane / W;                // front within the warp
   for (int e = threadIdx.x; e < kLetters * kLetters; e += blockDim.x) s_sub[e] = a.sub[e];
-  int32_t* scratch = a.scratch + (size_t)(blockIdx.x * kWaveWarps + warp) * 4 * (size_t)a.scratch_cols;
+  int32_t* scratch =
+      a.scratch + ((size_t)(blockIdx.x * kWaveWarps + warp) * S + seg) * 4 * (size_t)a.scratch_cols;
 
   for (;;) {
     __syncthreads();
@@ -293,13 +335,12 @@ __global__ void __launch_bounds__(kWaveThreads, (MinBlocks<R, P, V>::value)) wav
     const int xbase = a.group_xbase ? a.group_xbase[g] : 0;
     float* jobD = a.group_dofs ? a.D + a.group_dofs[g] : nullptr;
     const int64_t jobld = a.group_ld ? a.group_ld[g] : a.ld;
-    const int i = xbase + (int)(chunk * kWaveWarps) + warp;
+    const int i = xbase + (int)(chunk * (kWaveWarps * S)) + warp * S + seg;
     const int LyA = a.ylen[y0];
     const int LyB = has_b ? a.ylen[y1] : 0;
     const int8_t* YA = a.codes + a.ystart[y0];
     const int8_t* YB = has_b ? a.codes + a.ystart[y1] : YA;
     const bool active = i < xbase + nX;
-    const int Lx = active ? a.xlen[i] : 0;
     const int8_t* X = a.codes + (active ? a.xstart[i] : 0);
     bool wantA = active && (!a.triangle || i <= y0);
     bool wantB = active && has_b && (!a.triangle || i <= y1);
@@ -309,14 +350,17 @@ __global__ void __launch_bounds__(kWaveThreads, (MinBlocks<R, P, V>::value)) wav
       const bool safeA = int16_safe(a, i, y0);
       const bool safeB = !has_b || int16_safe(a, i, y1);
       if (wantA && !safeA) {
-        if (lane == 0) queue_rerun(a, i, y0);
+        if (sl == 0) queue_rerun(a, i, y0);
         wantA = false;
       }
       if (wantB && !(safeA && safeB)) {
-        if (lane == 0) queue_rerun(a, i, y1);
+        if (sl == 0) queue_rerun(a, i, y1);
         wantB = false;
       }
     }
+    const int Lx = (wantA || wantB) ? a.xlen[i] : 0;
+    const int Lmax = __reduce_max_sync(0xffffffffu, (unsigned)Lx);
+    const int Lmin = (int)__reduce_min_sync(0xffffffffu, Lx > 0 ? (unsigned)Lx : 0x7fffffffu);
     const int rows = LyA > LyB ? LyA : LyB;
     const int nb = (rows + BAND - 1) / BAND;
     const int xo = active ? a.xorig[i] : 0;
@@ -338,53 +382,90 @@ __global__ void __launch_bounds__(kWaveThreads, (MinBlocks<R, P, V>::value)) wav
         } else {
           w = (uint32_t)sa;
         }
-        prof[((x * Q + (r >> 2)) * 32 + k) * 4 + (r & 3)] = w;
+        prof[((x * Q + (r >> 2)) * W + k) * 4 + (r & 3)] = w;
       }
       __syncthreads();
-      if (wantA || wantB)
-        wave_band<R, P, V>(a, lane, b, nb, X, Lx, prof, scratch, LyA - 1, LyB - 1, wantA, wantB, xo, yoA, yoB,
-                           jobD, jobld);
+      if (Lmax > 0)
+        wave_band<R, P, V, W>(a, sl, b, nb, X, Lx, Lmin, Lmax, prof, scratch, LyA - 1, LyB - 1, wantA, wantB, xo,
+                              yoA, yoB, jobD, jobld);
     }
   }
 }
 
-template <int R, int P, int V>
+template <int R, int P, int V, int W>
 void prepare_one() {
-  const size_t smem = (size_t)kLetters * 32 * R * sizeof(uint32_t);
-  cudaFuncSetAttribute(wave_kernel<R, P, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const size_t smem = (size_t)kLetters * W * R * sizeof(uint32_t);
+  cudaFuncSetAttribute(wave_kernel<R, P, V, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
-template <int R, int P, int V>
+template <int R, int P, int V, int W>
 cudaError_t launch_one(const WaveArgs& a, int grid, cudaStream_t s) {
-  const size_t smem = (size_t)kLetters * 32 * R * sizeof(uint32_t);
-  wave_kernel<R, P, V><<<grid, kWaveThreads, smem, s>>>(a);
+  const size_t smem = (size_t)kLetters * W * R * sizeof(uint32_t);
+  wave_kernel<R, P, V, W><<<grid, kWaveThreads, smem, s>>>(a);
   return cudaGetLastError();
 }
 
-template <int R, int P, int V>
+template <int R, int P, int V, int W>
 int occupancy_one() {
-  const size_t smem = (size_t)kLetters * 32 * R * sizeof(uint32_t);
-  cudaFuncSetAttribute(wave_kernel<R, P, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const size_t smem = (size_t)kLetters * W * R * sizeof(uint32_t);
+  cudaFuncSetAttribute(wave_kernel<R, P, V, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, wave_kernel<R, P, V>, kWaveThreads, smem) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, wave_kernel<R, P, V, W>, kWaveThreads, smem) != cudaSuccess)
     return 1;
   return n > 0 ? n : 1;
 }
 
-// Entry points of one rows-per-lane template (all P, V).
+// The (P, V, W) combinations that exist: W = 32 with every P and V; the
+// narrow fronts (W = 16, 8) on int16x2 lanes with V = 0 or 2.
+inline bool wave_variant_exists(int P, int V, int W) {
+  if (W == 32) return (P == 1 || P == 2) && V >= 0 && V <= 2;
+  return (W == 16 || W == 8) && P == 2 && (V == 0 || V == 2);
+}
+
+// Entry points of one rows-per-lane template (every existing P, V, W).
 template <int R>
 struct Entry {
-  static cudaError_t launch(int P, int V, const WaveArgs& a, int grid, cudaStream_t s) {
-    if (P == 2) return V ? launch_one<R, 2, 1>(a, grid, s) : launch_one<R, 2, 0>(a, grid, s);
-    return V ? launch_one<R, 1, 1>(a, grid, s) : launch_one<R, 1, 0>(a, grid, s);
+  template <class Fn>
+  static auto with(int P, int V, int W, Fn&& fn) {
+    if (W == 16) return V == 2 ? fn(std::integral_constant<int, 2>{}, std::integral_constant<int, 2>{},
+                                    std::integral_constant<int, 16>{})
+                               : fn(std::integral_constant<int, 2>{}, std::integral_constant<int, 0>{},
+                                    std::integral_constant<int, 16>{});
+    if (W == 8) return V == 2 ? fn(std::integral_constant<int, 2>{}, std::integral_constant<int, 2>{},
+                                   std::integral_constant<int, 8>{})
+                              : fn(std::integral_constant<int, 2>{}, std::integral_constant<int, 0>{},
+                                   std::integral_constant<int, 8>{});
+    if (P == 2) {
+      if (V == 2) return fn(std::integral_constant<int, 2>{}, std::integral_constant<int, 2>{},
+                            std::integral_constant<int, 32>{});
+      if (V == 1) return fn(std::integral_constant<int, 2>{}, std::integral_constant<int, 1>{},
+                            std::integral_constant<int, 32>{});
+      return fn(std::integral_constant<int, 2>{}, std::integral_constant<int, 0>{}, std::integral_constant<int, 32>{});
+    }
+    if (V == 2) return fn(std::integral_constant<int, 1>{}, std::integral_constant<int, 2>{},
+                          std::integral_constant<int, 32>{});
+    if (V == 1) return fn(std::integral_constant<int, 1>{}, std::integral_constant<int, 1>{},
+                          std::integral_constant<int, 32>{});
+    return fn(std::integral_constant<int, 1>{}, std::integral_constant<int, 0>{}, std::integral_constant<int, 32>{});
   }
-  static void prepare(int P, int V) {
-    if (P == 2) V ? prepare_one<R, 2, 1>() : prepare_one<R, 2, 0>();
-    else V ? prepare_one<R, 1, 1>() : prepare_one<R, 1, 0>();
+  static cudaError_t launch(int P, int V, int W, const WaveArgs& a, int grid, cudaStream_t s) {
+    if (!wave_variant_exists(P, V, W)) return cudaErrorInvalidValue;
+    return with(P, V, W, [&](auto p, auto v, auto w) {
+      return launch_one<R, decltype(p)::value, decltype(v)::value, decltype(w)::value>(a, grid, s);
+    });
   }
-  static int occupancy(int P, int V) {
-    if (P == 2) return V ? occupancy_one<R, 2, 1>() : occupancy_one<R, 2, 0>();
-    return V ? occupancy_one<R, 1, 1>() : occupancy_one<R, 1, 0>();
+  static void prepare(int P, int V, int W) {
+    if (!wave_variant_exists(P, V, W)) return;
+    with(P, V, W, [&](auto p, auto v, auto w) {
+      prepare_one<R, decltype(p)::value, decltype(v)::value, decltype(w)::value>();
+      return 0;
+    });
+  }
+  static int occupancy(int P, int V, int W) {
+    if (!wave_variant_exists(P, V, W)) return 1;
+    return with(P, V, W, [&](auto p, auto v, auto w) {
+      return occupancy_one<R, decltype(p)::value, decltype(v)::value, decltype(w)::value>();
+    });
   }
 };
 
@@ -392,18 +473,18 @@ struct Entry {
 
 // Per-template dispatch tables (one translation unit per R).
 #define NWG_WAVE_ROWS(X) X(4) X(8) X(12) X(16) X(20) X(24) X(32)
-#define NWG_DECL_WAVE(r)                                                                  \
-  cudaError_t wave_launch_r##r(int P, int V, const WaveArgs& a, int grid, cudaStream_t s); \
-  void wave_prepare_r##r(int P, int V);                                                  \
-  int wave_occupancy_r##r(int P, int V);
+#define NWG_DECL_WAVE(r)                                                                         \
+  cudaError_t wave_launch_r##r(int P, int V, int W, const WaveArgs& a, int grid, cudaStream_t s); \
+  void wave_prepare_r##r(int P, int V, int W);                                                  \
+  int wave_occupancy_r##r(int P, int V, int W);
 NWG_WAVE_ROWS(NWG_DECL_WAVE)
 #undef NWG_DECL_WAVE
 
-#define NWG_DEFINE_WAVE(r)                                                                 \
-  cudaError_t wave_launch_r##r(int P, int V, const WaveArgs& a, int grid, cudaStream_t s) { \
-    return wave::Entry<r>::launch(P, V, a, grid, s);                                      \
-  }                                                                                       \
-  void wave_prepare_r##r(int P, int V) { wave::Entry<r>::prepare(P, V); }                 \
-  int wave_occupancy_r##r(int P, int V) { return wave::Entry<r>::occupancy(P, V); }
+#define NWG_DEFINE_WAVE(r)                                                                        \
+  cudaError_t wave_launch_r##r(int P, int V, int W, const WaveArgs& a, int grid, cudaStream_t s) { \
+    return wave::Entry<r>::launch(P, V, W, a, grid, s);                                          \
+  }                                                                                              \
+  void wave_prepare_r##r(int P, int V, int W) { wave::Entry<r>::prepare(P, V, W); }              \
+  int wave_occupancy_r##r(int P, int V, int W) { return wave::Entry<r>::occupancy(P, V, W); }
 
 }  // namespace nwg

@@ -110,12 +110,16 @@ class Context:
         self._check(self._lib.nwg_autotune(self.h, 1 if force else 0, ctypes.byref(r)))
         return r.as_dict()
 
-    def set_tuning(self, rows_per_lane, variant):
-        rp = np.ascontiguousarray(rows_per_lane, dtype=np.int32)
-        vv = np.ascontiguousarray(variant, dtype=np.int32)
-        if rp.shape != (8,) or vv.shape != (8,):
-            raise ValueError("8 length classes expected")
-        self._check(self._lib.nwg_set_tuning(self.h, _p(rp, c_i32p), _p(vv, c_i32p)))
+    def set_tuning(self, rows_per_lane, variant, lanes=None):
+        """Kernel choice per length class (TUNE_CLASSES entries each; a scalar
+        is used for every class): rows per lane, register layout, lanes per
+        wavefront (default 32)."""
+        from ._native import TUNE_CLASSES
+        k = TUNE_CLASSES
+        rp = np.ascontiguousarray(np.broadcast_to(rows_per_lane, (k,)), dtype=np.int32)
+        vv = np.ascontiguousarray(np.broadcast_to(variant, (k,)), dtype=np.int32)
+        ww = np.ascontiguousarray(np.broadcast_to(32 if lanes is None else lanes, (k,)), dtype=np.int32)
+        self._check(self._lib.nwg_set_tuning_lanes(self.h, _p(rp, c_i32p), _p(vv, c_i32p), _p(ww, c_i32p)))
 
     def set_launch_timing(self, on: bool):
         self._check(self._lib.nwg_set_launch_timing(self.h, 1 if on else 0))

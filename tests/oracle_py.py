@@ -101,21 +101,21 @@ def score_pair(x: bytes, y: bytes, go: int = 10, ge: int = 2) -> int:
                                 _p(sub, ctypes.c_int8))
 
 
-def score_all(seqset, go: int = 10, ge: int = 2, threads: int = 0) -> np.ndarray:
+def score_all(seqset, go: int = 10, ge: int = 2, threads: int = 0, sub=None) -> np.ndarray:
     codes, off = encode(seqset)
     n = len(off) - 1
     D = np.zeros((n, n), dtype=np.float32)
-    sub = blosum()
+    sub = blosum() if sub is None else np.ascontiguousarray(sub, dtype=np.int8).reshape(576)
     lib().nwo_score_all(_p(codes, ctypes.c_int8), _p(off, ctypes.c_int64), n, go, ge,
                         _p(sub, ctypes.c_int8), _p(D, ctypes.c_float), n, threads)
     return D
 
 
-def score_list(codes, off, pi, pj, go: int = 10, ge: int = 2, threads: int = 0) -> np.ndarray:
+def score_list(codes, off, pi, pj, go: int = 10, ge: int = 2, threads: int = 0, sub=None) -> np.ndarray:
     pi = np.ascontiguousarray(pi, dtype=np.int32)
     pj = np.ascontiguousarray(pj, dtype=np.int32)
     out = np.zeros(len(pi), dtype=np.int32)
-    sub = blosum()
+    sub = blosum() if sub is None else np.ascontiguousarray(sub, dtype=np.int8).reshape(576)
     lib().nwo_score_list(_p(codes, ctypes.c_int8), _p(off, ctypes.c_int64), _p(pi, ctypes.c_int32),
                          _p(pj, ctypes.c_int32), len(pi), go, ge, _p(sub, ctypes.c_int8),
                          _p(out, ctypes.c_int32), threads)

@@ -147,16 +147,59 @@ def test_config1_full_size_properties_and_sample(ctx):
 
 
 @pytest.mark.parametrize("R", [4, 8, 12, 16, 20, 24, 32])
-@pytest.mark.parametrize("V", [0, 1])
-def test_every_kernel_template_matches_oracle(R, V):
-    # the autotuner may pick any (rows per lane, register layout) for any
-    # length class: every template must be exact, single- and multi-band
+@pytest.mark.parametrize("V,W", [(0, 32), (1, 32), (2, 32), (0, 16), (2, 16), (0, 8), (2, 8)])
+def test_every_kernel_template_matches_oracle(R, V, W):
+    # the autotuner may pick any (rows per lane, register layout, front width)
+    # for any length class: every template must be exact, single- and
+    # multi-band, with fronts of one warp finishing at different columns
     from mestrado_gb300 import Context
     seqs = _rand_set(40 + R, 26, 1, 900)
     ref = O.score_all(seqs, threads=os.cpu_count())
     with Context(10, 2) as c:
-        c.set_tuning([R] * 8, [V] * 8)
+        c.set_tuning(R, V, W)
         for mode in (MODE_BATCHED, MODE_BATCHED_INT32):
+            assert np.array_equal(c.score_all(seqs, mode=mode), ref)
+        # a block (no triangle), X and Y from different sets
+        xs = _rand_set(90 + R, 13, 1, 700)
+        Db = c.score_block(xs, seqs)
+        assert np.array_equal(Db, O.score_all(xs + seqs, threads=os.cpu_count())[:13, 13:])
+
+
+def _gap_case_sets():
+    rng = np.random.default_rng(8)
+    letters = b"ARNDCQEGHILKMFPSTWYV"
+    def rnd(L):
+        return bytes(rng.choice(list(letters), L).tolist())
+    return {
+        # long sequences with a large extension penalty: int16 lanes would
+        # overflow at the boundary row alone (-ge*(c+1)), so they must not be used
+        "long_ge20": [rnd(L) for L in (2100, 1900, 1500, 700, 640, 580, 90)],
+        "short": [rnd(L) for L in rng.integers(1, 500, 30)],
+        # identical high-scoring runs: the H upper bound decides int16 vs int32
+        "runs": [b"W" * 1200, b"W" * 1100, b"C" * 1300, rnd(1250), rnd(400), b"W" * 900],
+    }
+
+
+@pytest.mark.parametrize("go,ge,mat,case", [
+    (3, 5, "blosum", "short"), (15, 1, "blosum", "short"), (0, 0, "blosum", "short"),
+    (10, 20, "blosum", "long_ge20"), (10, 2, "x3", "runs"), (10, 2, "x3", "short"),
+    (40, 30, "blosum", "short")])
+@pytest.mark.parametrize("V", [0, 1, 2])
+def test_gap_penalties_and_matrices_match_oracle(go, ge, mat, case, V):
+    # the int16 guard follows the context's penalties and matrix
+    from mestrado_gb300 import Context
+    sub = O.blosum().astype(np.int32)
+    if mat == "x3":
+        sub = np.clip(sub * 3, -128, 127)
+    sub = sub.astype(np.int8)
+    seqs = _gap_case_sets()[case]
+    ref = O.score_all(seqs, go, ge, threads=os.cpu_count(), sub=sub)
+    with Context(go, ge, sub=sub) as c:
+        # one band of 32 lanes per class where it fits: rows per lane = the
+        # class's rows / 32 rounded up to a multiple of 4, at most 32
+        rows = [min(32, -(-(-(-r // 32)) // 4) * 4) for r in _native.TUNE_CLASS_ROWS]
+        c.set_tuning(rows, V)
+        for mode in (MODE_BATCHED, MODE_PLAIN):
             assert np.array_equal(c.score_all(seqs, mode=mode), ref)
 
 
@@ -165,11 +208,12 @@ def test_autotune_then_exact(tmp_path, monkeypatch):
     from mestrado_gb300 import Context
     with Context(10, 2) as c:
         r = c.autotune(force=True)
-        assert not r["from_cache"] and len(r["classes"]) == 8
+        assert not r["from_cache"] and len(r["classes"]) == _native.TUNE_CLASSES
         assert all(k["gcups"] > 0 for k in r["classes"])
         seqs = _rand_set(77, 40, 10, 1200)
         assert np.array_equal(c.score_all(seqs), O.score_all(seqs, threads=os.cpu_count()))
     with Context(10, 2) as c:
         r2 = c.autotune()
         assert r2["from_cache"]
-        assert [k["rows_per_lane"] for k in r2["classes"]] == [k["rows_per_lane"] for k in r["classes"]]
+        assert [(k["rows_per_lane"], k["variant"], k["lanes"]) for k in r2["classes"]] == \
+            [(k["rows_per_lane"], k["variant"], k["lanes"]) for k in r["classes"]]
