@@ -214,12 +214,17 @@ int nwg_score_pairs_noalloc(const int8_t* d_codes, const int64_t* d_start, const
  * device; timer.h falls back to clock()).  These give the bench its roofline
  * denominator and per-launch device times. */
 
-/* Peak of the cell update alone: every SM runs the 5-instruction cell update
- * on register-resident strips, no memory, no shuffles, in both forms the
- * wave kernels use (2 adds + 2 viaddmax + 1 vimax3; 1 add + 4 viaddmax), and
- * the faster form counts.  lanes16 != 0: int16x2 words (2 cells per word),
- * else int32.  Returns cells per second. */
+/* Peak of the cell update alone: every SM runs the cell update on
+ * register-resident strips, no memory, no shuffles, in every form of
+ * nwg_dpx_peak_form, and the fastest form counts.  lanes16 != 0: int16x2
+ * words (2 cells per word), else int32.  Returns cells per second. */
 int nwg_dpx_peak(nwg_ctx* ctx, int lanes16, double* cells_per_s);
+
+/* The same for one form of the cell update: 0 = 2 adds + 2 viaddmax + 1
+ * vimax3; 2 = 1 add + 4 viaddmax (shifted E', F'); 3 = shifted, 5 adds + 2
+ * two-input max + 1 vimax3; 4 = unshifted, 4 adds + 2 max + 1 vimax3;
+ * 5 = shifted, viaddmax on the F chain, adds + max off it. */
+int nwg_dpx_peak_form(nwg_ctx* ctx, int lanes16, int form, double* cells_per_s);
 
 typedef struct {
   int32_t kind;         /* 0 wave (batched), 1 plain, 2 pair list, 3 other    */
@@ -229,7 +234,7 @@ typedef struct {
   int64_t pairs;        /* pairs (i<j) this launch computes                    */
   int64_t cells;        /* their L_i*L_j sum                                   */
   double ms;            /* device time (events around this launch alone)       */
-  int32_t variant;      /* register layout of the wave kernel (0, 1, 2)       */
+  int32_t variant;      /* register layout of the wave kernel (0..5)          */
   int32_t lanes;        /* lanes per wavefront (32, 16, 8)                    */
 } nwg_launch_rec;
 

@@ -619,28 +619,38 @@ int nwg_score_pairs(nwg_ctx* ctx, const int8_t* codes, const int64_t* offsets, i
   return NWG_OK;
 }
 
-int nwg_dpx_peak(nwg_ctx* ctx, int lanes16, double* cells_per_s) {
+int nwg_dpx_peak_form(nwg_ctx* ctx, int lanes16, int form, double* cells_per_s) {
   if (!ctx || !cells_per_s) return NWG_ERR_INVALID;
+  if (form != 0 && form != 2 && form != 3 && form != 4 && form != 5) return NWG_ERR_INVALID;
   Ctx* c = reinterpret_cast<Ctx*>(ctx);
   const int P = lanes16 ? 2 : 1;
   const int cols = 4096;
+  const int grid = c->sms * nwg::dpx_peak_ctas_per_sm(P, form);
+  int rc;
+  if ((rc = c->b_out.ensure(sizeof(uint32_t) * grid))) return c->fail(rc, "dpx peak");
+  for (int rep = 0; rep < 2; ++rep) {      // first launch warms up clocks and caches
+    if ((rc = c->cuda(cudaEventRecord(c->ev0, c->stream), "event")) ||
+        (rc = c->cuda(nwg::launch_dpx_peak(P, form, cols, grid, (uint32_t*)c->b_out.p, c->go, c->ge, c->stream),
+                      "dpx peak")) ||
+        (rc = c->cuda(cudaEventRecord(c->ev1, c->stream), "event")) ||
+        (rc = c->cuda(cudaEventSynchronize(c->ev1), "dpx peak sync")))
+      return rc;
+  }
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  const double cells = (double)grid * 256.0 * cols * 16 * P;
+  *cells_per_s = cells / (ms * 1e-3);
+  return NWG_OK;
+}
+
+int nwg_dpx_peak(nwg_ctx* ctx, int lanes16, double* cells_per_s) {
+  if (!ctx || !cells_per_s) return NWG_ERR_INVALID;
   double best = 0.0;
-  for (int form : {0, 2}) {
-    const int grid = c->sms * nwg::dpx_peak_ctas_per_sm(P, form);
-    int rc;
-    if ((rc = c->b_out.ensure(sizeof(uint32_t) * grid))) return c->fail(rc, "dpx peak");
-    for (int rep = 0; rep < 2; ++rep) {      // first launch warms up clocks and caches
-      if ((rc = c->cuda(cudaEventRecord(c->ev0, c->stream), "event")) ||
-          (rc = c->cuda(nwg::launch_dpx_peak(P, form, cols, grid, (uint32_t*)c->b_out.p, c->go, c->ge, c->stream),
-                        "dpx peak")) ||
-          (rc = c->cuda(cudaEventRecord(c->ev1, c->stream), "event")) ||
-          (rc = c->cuda(cudaEventSynchronize(c->ev1), "dpx peak sync")))
-        return rc;
-    }
-    float ms = 0;
-    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
-    const double cells = (double)grid * 256.0 * cols * 16 * P;
-    best = std::max(best, cells / (ms * 1e-3));
+  for (int form : {0, 2, 3, 4, 5}) {
+    double v = 0.0;
+    const int rc = nwg_dpx_peak_form(ctx, lanes16, form, &v);
+    if (rc) return rc;
+    best = std::max(best, v);
   }
   *cells_per_s = best;
   return NWG_OK;

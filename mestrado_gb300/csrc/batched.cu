@@ -178,7 +178,7 @@ static int get_plan(Ctx* c, const int64_t* xoff, int nx, const int64_t* yoff, in
   std::vector<Group> groups;
   groups.reserve((size_t)Y.n / 2 + 1);
   for (int y = 0; y < Y.n;) {
-    const TuneChoice tc = c->tune[tune_class(Y.len[y])];
+    const TuneChoice tc = c->choice(Y.len[y]);
     if (!force32) {
       const int y2 = y + 1 < Y.n ? y + 1 : -1;
       const int last = y2 >= 0 ? y2 : y;
@@ -215,7 +215,7 @@ static int get_plan(Ctx* c, const int64_t* xoff, int nx, const int64_t* yoff, in
       ++e;
     BatchPlan::Bucket b{groups[k].R, groups[k].P, groups[k].V, groups[k].W, groups[k].check, k, e - k,
                         (int64_t)prefix.size(), 0, 0, 0.0, 0, 0, 0};
-    const int xper = kWaveWarps * (32 / b.W);   // X per CTA job
+    const int xper = kWaveWarps * (32 / b.W) * wave_x_per_front(b.V);   // X per CTA job
     int64_t acc = 0;
     for (int g = k; g < e; ++g) {
       prefix.push_back(acc);
@@ -260,7 +260,8 @@ static int get_plan(Ctx* c, const int64_t* xoff, int nx, const int64_t* yoff, in
     b.grid = (int)std::min<int64_t>(b.njobs, (int64_t)c->sms * wave_max_ctas_per_sm(b.R, b.P, b.V, b.W));
     b.grid = std::max(b.grid, 1);
     b.scratch_off = scratch_words;
-    if (b.maxrows > b.W * b.R) scratch_words += (size_t)b.grid * kWaveWarps * (32 / b.W) * 4 * p->scols;
+    if (b.maxrows > b.W * b.R)
+      scratch_words += (size_t)b.grid * kWaveWarps * (32 / b.W) * wave_x_per_front(b.V) * 4 * p->scols;
   }
   if ((rc = p->wscratch.ensure(sizeof(int32_t) * scratch_words))) {
     delete p;

@@ -72,6 +72,13 @@ struct Ctx {
   // Kernel choice per length class of the Y rows (rows <= kClassRows[k]):
   // rows per lane and register layout, set by the autotuner (tune.cu).
   TuneChoice tune[kTuneClasses];
+  // The choice for Y groups of this many rows; layout 4 is exact only when
+  // go >= ge and falls back to layout 2 otherwise.
+  TuneChoice choice(int rows) const {
+    TuneChoice t = tune[tune_class(rows)];
+    if (t.V == 4 && go < ge) t.V = 2;
+    return t;
+  }
   uint64_t tune_version = 0;        // bumped on every change (part of the plan key)
   bool tuned = false;
 

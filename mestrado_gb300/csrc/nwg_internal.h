@@ -148,6 +148,7 @@ cudaError_t launch_wave(int R, int P, int V, int W, const WaveArgs& a, int grid,
 int wave_max_ctas_per_sm(int R, int P, int V, int W);
 void prepare_wave(int R, int P, int V, int W);   // sets the dynamic shared memory limit (outside graph capture)
 bool wave_exists(int R, int P, int V, int W);
+inline int wave_x_per_front(int V) { return V == 5 ? 2 : 1; }
 cudaError_t launch_plain(const PlainArgs& a, cudaStream_t s);
 cudaError_t launch_rerun(const WaveArgs& a, int2* scratch, int64_t nthreads, cudaStream_t s);
 // per-CTA neighbor joining for many small jobs (nj.cu)

@@ -151,7 +151,54 @@ __global__ void __launch_bounds__(256) dpx_peak_kernel(uint32_t p0, uint32_t p1,
     uint32_t diag = hprev;
     hprev = hin;
     uint32_t f = fin;
-    if (F == 2) {
+    if (F == 3) {
+      // shifted form with plain adds and 2-input maxima: 5 adds, 2 max, 1 max3
+      const uint32_t NGEA = L::arith(-ge, -ge), NGOA = L::arith(-go, -go);
+      uint32_t hup = hin;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        f = L::max2(L::add(f, NGEA), hup);
+        const uint32_t e = L::max2(L::add(E[r], NGEA), H[r]);
+        const uint32_t h = L::max3(L::add(f, NGOA), L::add(e, NGOA), L::add(diag, pv[r & 3]));
+        diag = H[r];
+        H[r] = h;
+        E[r] = e;
+        hup = h;
+      }
+      hin = H[3];
+    } else if (F == 4) {
+      // unshifted form with plain adds and 2-input maxima: 4 adds, 2 max, 1 max3
+      const uint32_t NGEA = L::arith(-ge, -ge);
+      uint32_t tup = L::add(hin, NGO);
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        f = L::max2(L::add(f, NGEA), tup);
+        const uint32_t e = L::max2(L::add(E[r], NGEA), T[r]);
+        const uint32_t h = L::max3(e, f, L::add(diag, pv[r & 3]));
+        diag = H[r];
+        H[r] = h;
+        E[r] = e;
+        T[r] = L::add(h, NGO);
+        tup = T[r];
+      }
+      hin = T[3];
+    } else if (F == 5) {
+      // shifted chain (viaddmax) with the off-chain maxima as adds + max
+      const uint32_t NGEA = L::arith(-ge, -ge), NGOA = L::arith(-go, -go);
+      uint32_t hup = hin;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        f = L::addmax(f, NGE, hup);
+        const uint32_t e = L::max2(L::add(E[r], NGEA), H[r]);
+        const uint32_t m = L::max2(L::add(e, NGOA), L::add(diag, pv[r & 3]));
+        const uint32_t h = L::addmax(f, NGOP, m);
+        diag = H[r];
+        H[r] = h;
+        E[r] = e;
+        hup = h;
+      }
+      hin = H[3];
+    } else if (F == 2) {
       // the shifted form of wave kernel layout V = 2: 4 DPX + 1 add per word
       uint32_t hup = hin;
 #pragma unroll
@@ -222,30 +269,38 @@ bool wave_exists(int R, int P, int V, int W) {
 }
 #undef NWG_CASE
 
-cudaError_t launch_dpx_peak(int P, int form, int cols, int grid, uint32_t* sink, int go, int ge, cudaStream_t s) {
-  const uint32_t p0 = 4u * 65536u + 3u, p1 = (uint32_t)(-2 * 65536 + 1), p2 = (uint32_t)(2 * 65536 - 1),
-                 p3 = 5u * 65536u;
-  if (P == 2) {
-    if (form == 2) dpx_peak_kernel<2, 2><<<grid, 256, 0, s>>>(p0, p1, p2, p3, go, ge, cols, sink);
-    else dpx_peak_kernel<2, 0><<<grid, 256, 0, s>>>(p0, p1, p2, p3, go, ge, cols, sink);
-  } else {
-    if (form == 2) dpx_peak_kernel<1, 2><<<grid, 256, 0, s>>>(p0, 1u, 0xFFFFFFFEu, 3u, go, ge, cols, sink);
-    else dpx_peak_kernel<1, 0><<<grid, 256, 0, s>>>(p0, 1u, 0xFFFFFFFEu, 3u, go, ge, cols, sink);
-  }
+template <int P, int F>
+static cudaError_t launch_peak_one(int cols, int grid, uint32_t* sink, int go, int ge, cudaStream_t s) {
+  const uint32_t p0 = P == 2 ? 4u * 65536u + 3u : 0u, p1 = P == 2 ? (uint32_t)(-2 * 65536 + 1) : 1u,
+                 p2 = P == 2 ? (uint32_t)(2 * 65536 - 1) : 0xFFFFFFFEu, p3 = P == 2 ? 5u * 65536u : 3u;
+  dpx_peak_kernel<P, F><<<grid, 256, 0, s>>>(p0, p1, p2, p3, go, ge, cols, sink);
   return cudaGetLastError();
 }
 
-int dpx_peak_ctas_per_sm(int P, int form) {
+template <int P, int F>
+static int peak_occupancy_one() {
   int n = 0;
-  if (P == 2) {
-    if (form == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dpx_peak_kernel<2, 2>, 256, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dpx_peak_kernel<2, 0>, 256, 0);
-  } else {
-    if (form == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dpx_peak_kernel<1, 2>, 256, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dpx_peak_kernel<1, 0>, 256, 0);
-  }
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dpx_peak_kernel<P, F>, 256, 0);
   return n > 0 ? n : 1;
 }
+
+#define NWG_PEAK_FORMS(X) X(0) X(2) X(3) X(4) X(5)
+cudaError_t launch_dpx_peak(int P, int form, int cols, int grid, uint32_t* sink, int go, int ge, cudaStream_t s) {
+#define NWG_CASE(f) \
+  if (form == f) return P == 2 ? launch_peak_one<2, f>(cols, grid, sink, go, ge, s) : launch_peak_one<1, f>(cols, grid, sink, go, ge, s);
+  NWG_PEAK_FORMS(NWG_CASE)
+#undef NWG_CASE
+  return cudaErrorInvalidValue;
+}
+
+int dpx_peak_ctas_per_sm(int P, int form) {
+#define NWG_CASE(f) \
+  if (form == f) return P == 2 ? peak_occupancy_one<2, f>() : peak_occupancy_one<1, f>();
+  NWG_PEAK_FORMS(NWG_CASE)
+#undef NWG_CASE
+  return 1;
+}
+#undef NWG_PEAK_FORMS
 
 cudaError_t launch_rerun(const WaveArgs& a, int2* scratch, int64_t nthreads, cudaStream_t s) {
   const int64_t blocks = (nthreads + kPlainThreads - 1) / kPlainThreads;

@@ -161,7 +161,7 @@ int Server::launch_batch(Slot& S) {
     const int certain = maxs > 0 ? c.i16.max_h / maxs : 1 << 30;
     for (int y = 0; y < n;) {
       const int gyi = (int)base + y;
-      const TuneChoice tc = c.tune[tune_class(len[gyi])];
+      const TuneChoice tc = c.choice(len[gyi]);
       if (!long_set && len[gyi] <= certain) {
         const int y2 = y + 1 < n ? gyi + 1 : -1;
         const int last = y2 >= 0 ? y + 1 : y;
@@ -191,7 +191,7 @@ int Server::launch_batch(Slot& S) {
            groups[e].P == groups[k].P)
       ++e;
     Bucket b{groups[k].R, groups[k].V, groups[k].W, groups[k].P, k, e - k, (int64_t)prefix.size(), 0, 0, 0, false};
-    const int xper = kWaveWarps * (32 / b.W);   // X per CTA job
+    const int xper = kWaveWarps * (32 / b.W) * wave_x_per_front(b.V);   // X per CTA job
     int64_t acc = 0;
     for (int g = k; g < e; ++g) {
       prefix.push_back(acc);
@@ -208,7 +208,7 @@ int Server::launch_batch(Slot& S) {
     b.grid = (int)std::max<int64_t>(
         1, std::min<int64_t>(b.njobs, (int64_t)c.sms * wave_max_ctas_per_sm(b.R, b.P, b.V, b.W)));
     b.soff = scratch_words;
-    if (b.multi) scratch_words += (size_t)b.grid * kWaveWarps * (32 / b.W) * 4 * maxlen;
+    if (b.multi) scratch_words += (size_t)b.grid * kWaveWarps * (32 / b.W) * wave_x_per_front(b.V) * 4 * maxlen;
     prepare_wave(b.R, b.P, b.V, b.W);
   }
   // device buffers of the slot (grow-only)

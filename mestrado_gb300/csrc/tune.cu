@@ -136,8 +136,8 @@ int Ctx::autotune(bool force, nwg_tune_result* out) {
     for (int R : kCandR) {
       const int band = W * R;
       if (band * 3 < Ly || band > 2 * Ly + 128) continue;   // at most 3 bands, at most ~half idle
-      for (int V = 0; V <= 2; ++V) {
-        if (!wave_exists(R, 2, V, W)) continue;
+      for (int V = 0; V <= 5; ++V) {
+        if (!wave_exists(R, 2, V, W) || (V == 4 && go < ge)) continue;
         tune[k] = {R, V, W};
         ++tune_version;
         float ms = 0.f;

@@ -29,6 +29,19 @@
 //   H = max(F' - go, max(E' - go, diag + S)),
 // the same values (go >= ge is not even needed: it is a change of variables),
 // with two dependent operations per row down the strip instead of three.
+// V = 3 keeps T = H - go and E per row and nothing else: the diagonal term
+// H[r-1][c-1] + S becomes T[r-1][c-1] + (S + go), with S + go stored in the
+// profile, so V = 0's instruction mix (2 adds, 2 viaddmax, 1 vimax3) runs
+// with V = 2's register footprint.
+// V = 4 is V = 2 with a one-operation F chain, exact when go >= ge: with
+// m = max(E, diag + S), H = max(F, m), so F'[r] = max(F'[r-1] - ge, H[r-1])
+// = max(F'[r-1] - ge, F'[r-1] - go, m[r-1]) = max(F'[r-1] - ge, m[r-1]);
+// m does not depend on F, so only the F' update itself stays on the path
+// from one row to the next (and from one lane to the next).
+// V = 5 is layout 3 with two X per front: every lane runs the strips of two
+// X (adjacent in length order) against the same band, row by row
+// interleaved, so two independent dependency chains share the lane's issue
+// slots.
 #pragma once
 
 #include <type_traits>
@@ -67,6 +80,7 @@ struct Lanes<2> {
   static __device__ __forceinline__ uint32_t max3(uint32_t a, uint32_t b, uint32_t c) {
     return __vimax3_u16x2(a, b, c);
   }
+  static __device__ __forceinline__ uint32_t max2(uint32_t a, uint32_t b) { return __vmaxu2(a, b); }
   static __device__ __forceinline__ int lo(uint32_t w) { return (int)(w & 0xFFFFu) - 32768; }
   static __device__ __forceinline__ int hi(uint32_t w) { return (int)(w >> 16) - 32768; }
 };
@@ -83,6 +97,7 @@ struct Lanes<1> {
   static __device__ __forceinline__ uint32_t max3(uint32_t a, uint32_t b, uint32_t c) {
     return (uint32_t)__vimax3_s32((int)a, (int)b, (int)c);
   }
+  static __device__ __forceinline__ uint32_t max2(uint32_t a, uint32_t b) { return (uint32_t)max((int)a, (int)b); }
   static __device__ __forceinline__ int lo(uint32_t w) { return (int)w; }
   static __device__ __forceinline__ int hi(uint32_t w) { return (int)w; }
 };
@@ -130,6 +145,12 @@ __device__ __forceinline__ void queue_rerun(const WaveArgs& a, int i, int y) {
   if (k < (unsigned long long)a.rerun_cap) a.rerun[k] = make_int2(i, y);
 }
 
+template <int V>
+struct Layout {
+  static constexpr int K = V == 5 ? 2 : 1;    // X per front
+  static constexpr int L = V == 5 ? 3 : V;    // register layout of each strip
+};
+
 template <int R, int P, int V>
 struct BandState {
   uint32_t H[R];
@@ -147,6 +168,48 @@ __device__ __forceinline__ uint32_t strip_column(BandState<R, P, V>& s, const ui
   using L = Lanes<P>;
   constexpr int Q = R / 4;
   uint32_t f = fin;
+  if (V == 3) {
+    // s.H holds T = H - go; hin is T of the row above; sv is S + go
+    uint32_t tup = hin;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const uint4 pv = pp[q * W];
+      const uint32_t sv[4] = {pv.x, pv.y, pv.z, pv.w};
+#pragma unroll
+      for (int w = 0; w < 4; ++w) {
+        const int r = q * 4 + w;
+        f = L::addmax(f, NGE, tup);                                      // F[r][c]
+        const uint32_t e = L::addmax(s.E[r], NGE, s.H[r]);               // E[r][c]
+        const uint32_t h = L::max3(e, f, L::add(diag, sv[w]));           // H[r][c]
+        diag = s.H[r];
+        s.H[r] = L::add(h, NGO);
+        s.E[r] = e;
+        tup = s.H[r];
+      }
+    }
+    return f;
+  }
+  if (V == 4) {
+    // fin is F' of the row above the strip, hin its H; then up carries m
+    uint32_t up = hin;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const uint4 pv = pp[q * W];
+      const uint32_t sv[4] = {pv.x, pv.y, pv.z, pv.w};
+#pragma unroll
+      for (int w = 0; w < 4; ++w) {
+        const int r = q * 4 + w;
+        f = L::addmax(f, NGE, up);                                       // F'[r][c]
+        const uint32_t e = L::addmax(s.E[r], NGE, s.H[r]);               // E'[r][c]
+        const uint32_t m = L::addmax(e, NGOP, L::add(diag, sv[w]));      // max(E, diag + S)
+        diag = s.H[r];
+        s.H[r] = L::addmax(f, NGOP, m);                                  // H[r][c]
+        s.E[r] = e;
+        up = m;
+      }
+    }
+    return f;
+  }
   if (V == 2) {
     // fin is F' of the row above the strip, hin its H
     uint32_t hup = hin;
@@ -192,113 +255,193 @@ __device__ __forceinline__ uint32_t strip_column(BandState<R, P, V>& s, const ui
   return f;
 }
 
-// One band (W*R rows starting at b*W*R) of one X for the calling front.
-// sl: lane within the front; Lx: this front's X length, 0 when the front has
-// no pair to report (its lanes then only take part in the shuffles); Lmin /
-// Lmax: smallest / largest Lx over the warp's working fronts (warp-uniform).
+// Two strips of layout 3 (two X, the same rows), interleaved row by row.
+template <int R, int P, int W>
+__device__ __forceinline__ void strip_column_pair(BandState<R, P, 3> (&s)[2], const uint4* __restrict__ pa,
+                                                  const uint4* __restrict__ pb, uint32_t (&diag)[2],
+                                                  const uint32_t (&hin)[2], uint32_t (&f)[2], uint32_t NGE,
+                                                  uint32_t NGO) {
+  using L = Lanes<P>;
+  constexpr int Q = R / 4;
+  uint32_t tup[2] = {hin[0], hin[1]};
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const uint4 va = pa[q * W], vb = pb[q * W];
+    const uint32_t sv[2][4] = {{va.x, va.y, va.z, va.w}, {vb.x, vb.y, vb.z, vb.w}};
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+      const int r = q * 4 + w;
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        f[k] = L::addmax(f[k], NGE, tup[k]);
+        const uint32_t e = L::addmax(s[k].E[r], NGE, s[k].H[r]);
+        const uint32_t h = L::max3(e, f[k], L::add(diag[k], sv[k][w]));
+        diag[k] = s[k].H[r];
+        s[k].H[r] = L::add(h, NGO);
+        s[k].E[r] = e;
+        tup[k] = s[k].H[r];
+      }
+    }
+  }
+}
+
+// One band (W*R rows starting at b*W*R) of the front's K X (K = 2 for V = 5).
+// sl: lane within the front; Lx[k]: length of X k, 0 when it has no pair to
+// report (its strip is then not computed; the lanes still take part in the
+// shuffles); Lmin / Lmax: smallest / largest Lx over the warp's working X
+// (warp-uniform).  scratch: the front's band-boundary buffers, 4 words per
+// column per X.
 template <int R, int P, int V, int W>
 __device__ __forceinline__ void wave_band(const WaveArgs& a, int sl, int b, int nb,
-                                          const int8_t* __restrict__ X, int Lx, int Lmin, int Lmax,
-                                          const uint32_t* __restrict__ prof,
+                                          const int8_t* const (&X)[Layout<V>::K], const int (&Lx)[Layout<V>::K],
+                                          int Lmin, int Lmax, const uint32_t* __restrict__ prof,
                                           int32_t* __restrict__ scratch, int rowA, int rowB,
-                                          bool wantA, bool wantB, int xo, int yoA, int yoB,
-                                          float* jobD, int64_t jobld) {
+                                          const bool (&wantA)[Layout<V>::K], const bool (&wantB)[Layout<V>::K],
+                                          const int (&xo)[Layout<V>::K], int yoA, int yoB, float* jobD,
+                                          int64_t jobld) {
   using L = Lanes<P>;
+  constexpr int K = Layout<V>::K;
+  constexpr int VL = Layout<V>::L;
   constexpr int BAND = W * R;
   constexpr int Q = R / 4;
   const uint32_t NGE = L::packed(-a.ge);        // per-half operand of addmax
   const uint32_t NGO = L::arith(-a.go, -a.go);   // word added to H to get H - go
   const uint32_t NGOP = L::packed(-a.go);        // per-half operand: - go
   const uint32_t NGEA = L::arith(-a.ge, -a.ge);  // word added to H[-1][c] to get H[-1][c+1]
-  // E[r][-1] = F[-1][c] = -32768 + ge; V == 2 keeps them shifted by go
-  const uint32_t SENT = L::splat(kShortMin + a.ge + (V == 2 ? a.go : 0));
+  // E[r][-1] = F[-1][c] = -32768 + ge; layouts 2 and 4 keep them shifted by go
+  const uint32_t SENT = L::splat(kShortMin + a.ge + ((VL == 2 || VL == 4) ? a.go : 0));
 
-  BandState<R, P, V> s;
+  BandState<R, P, VL> s[K];
   const int rowbase = b * BAND + sl * R;
+  const int gsh = VL == 3 ? a.go : 0;               // layout 3 carries T = H - go instead of H
 #pragma unroll
-  for (int r = 0; r < R; ++r) {
-    s.H[r] = L::splat(-a.ge * (rowbase + r + 1));   // H[row][-1]
-    s.E[r] = SENT;                                   // E[row][-1]
-    if (V == 0) s.T[(V == 0) ? r : 0] = L::add(s.H[r], NGO);
-  }
-  uint32_t hprev = L::splat(-a.ge * rowbase);       // H[rowbase-1][-1]: diag of column 0
-  uint32_t hbot = 0, fbot = 0;
-  uint32_t hb = L::splat(-a.ge);                    // H[-1][c] of the column lane 0 works on (band 0)
+  for (int k = 0; k < K; ++k)
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      s[k].H[r] = L::splat(-a.ge * (rowbase + r + 1) - gsh);   // H[row][-1] (T for layout 3)
+      s[k].E[r] = SENT;                                         // E[row][-1]
+      if (VL == 0) s[k].T[(VL == 0) ? r : 0] = L::add(s[k].H[r], NGO);
+    }
+  uint32_t hprev[K], hbot[K], fbot[K];
+  int xnext[K];
+  bool work[K];
+  const int32_t* rd[K];
+  int32_t* wr[K];
   const bool top = b == 0;
-  const bool work = Lx > 0;
-  const int32_t* rd = scratch + ((b + 1) & 1) * 2 * a.scratch_cols;   // written by band b-1
-  int32_t* wr = scratch + (b & 1) * 2 * a.scratch_cols;
-  const bool writer = sl == W - 1 && b + 1 < nb && work;
   const uint4* pl = reinterpret_cast<const uint4*>(prof) + sl;
-  int xnext = (sl == 0 && work) ? (int)X[0] : 0;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    hprev[k] = L::splat(-a.ge * rowbase - gsh);     // H[rowbase-1][-1]: diag of column 0
+    hbot[k] = fbot[k] = 0;
+    work[k] = Lx[k] > 0;
+    rd[k] = scratch + (size_t)k * 4 * a.scratch_cols + ((b + 1) & 1) * 2 * a.scratch_cols;   // band b-1
+    wr[k] = scratch + (size_t)k * 4 * a.scratch_cols + (b & 1) * 2 * a.scratch_cols;
+    xnext[k] = (sl == 0 && work[k]) ? (int)X[k][0] : 0;
+  }
+  uint32_t hb = L::splat(-a.ge - gsh);              // H[-1][c] of the column lane 0 works on (band 0)
+  const bool last_band = b + 1 >= nb;
 
   auto step = [&](int t, auto checked) {
     constexpr bool kChecked = decltype(checked)::value;
     const int c = t - sl;
-    uint32_t hin = __shfl_up_sync(0xffffffffu, hbot, 1, W);
-    uint32_t fin = __shfl_up_sync(0xffffffffu, fbot, 1, W);
-    const int xl = xnext;
-    if (kChecked) {
-      if (c + 1 >= 0 && c + 1 < Lx) xnext = X[c + 1];
-    } else if (W == 32 || work) {
-      xnext = X[min(c + 1, Lx - 1)];
+    uint32_t hin[K], fin[K];
+    int xl[K];
+    bool on[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      hin[k] = __shfl_up_sync(0xffffffffu, hbot[k], 1, W);
+      fin[k] = __shfl_up_sync(0xffffffffu, fbot[k], 1, W);
+      xl[k] = xnext[k];
+      if (kChecked) {
+        if (c + 1 >= 0 && c + 1 < Lx[k]) xnext[k] = X[k][c + 1];
+      } else if ((W == 32 && K == 1) || work[k]) {
+        xnext[k] = X[k][min(c + 1, Lx[k] - 1)];
+      }
+      on[k] = kChecked ? (c >= 0 && c < Lx[k]) : ((W == 32 && K == 1) || work[k]);
+      if (on[k] && sl == 0) {
+        hin[k] = top ? hb : (uint32_t)rd[k][2 * c];
+        fin[k] = top ? SENT : (uint32_t)rd[k][2 * c + 1];
+      }
     }
-    if (kChecked ? (c >= 0 && c < Lx) : (W == 32 || work)) {
-      uint32_t bh = hb, bf = SENT;
-      if (!top && sl == 0) {
-        bh = (uint32_t)rd[2 * c];
-        bf = (uint32_t)rd[2 * c + 1];
+    if (!kChecked || c >= 0) hb = L::add(hb, NGEA);
+    bool paired = false;
+    if constexpr (K == 2) {
+      if (!kChecked && on[0] && on[1]) {
+        // both strips on a column: interleaved
+        uint32_t diag[2] = {hprev[0], hprev[1]};
+        uint32_t f[2] = {fin[0], fin[1]};
+        hprev[0] = hin[0];
+        hprev[1] = hin[1];
+        strip_column_pair<R, P, W>(s, pl + clamp_code(xl[0]) * (Q * W), pl + clamp_code(xl[1]) * (Q * W), diag, hin,
+                                   f, NGE, NGO);
+        fbot[0] = f[0];
+        fbot[1] = f[1];
+        hbot[0] = s[0].H[R - 1];
+        hbot[1] = s[1].H[R - 1];
+        paired = true;
       }
-      if (sl == 0) {
-        hin = bh;
-        fin = bf;
+    }
+    if (!paired) {
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        if (!on[k]) continue;
+        const uint32_t diag = hprev[k];
+        hprev[k] = hin[k];
+        fbot[k] = strip_column<R, P, VL, W>(s[k], pl + clamp_code(xl[k]) * (Q * W), diag, hin[k], fin[k], NGE, NGO,
+                                            NGOP);
+        hbot[k] = s[k].H[R - 1];
       }
-      hb = L::add(hb, NGEA);
-      const uint32_t diag = hprev;
-      hprev = hin;
-      fbot = strip_column<R, P, V, W>(s, pl + clamp_code(xl) * (Q * W), diag, hin, fin, NGE, NGO, NGOP);
-      hbot = s.H[R - 1];
-      if (writer) {
-        wr[2 * c] = (int32_t)hbot;
-        wr[2 * c + 1] = (int32_t)fbot;
-      }
+    }
+    if (sl == W - 1 && !last_band) {
+#pragma unroll
+      for (int k = 0; k < K; ++k)
+        if (on[k]) {
+          wr[k][2 * c] = (int32_t)hbot[k];
+          wr[k][2 * c + 1] = (int32_t)fbot[k];
+        }
     }
   };
   // ramp-up (some lanes before column 0), steady state (every lane of every
-  // working front on a column), ramp-down (some lanes past their last column)
+  // working strip on a column), ramp-down (some lanes past their last column)
   int t = 0;
   const int t1 = Lmin < W - 1 ? Lmin : W - 1;
   for (; t < t1; ++t) step(t, std::true_type{});
+#pragma unroll 2
   for (; t < Lmin; ++t) step(t, std::false_type{});
   for (; t < Lmax + W - 1; ++t) step(t, std::true_type{});
 
   // H[] now holds the last column; the lane owning a pair's last row reports.
-  if (wantA) {
-    const int rr = rowA - b * BAND;
-    if (rr >= 0 && rr < BAND && sl == rr / R) {
-      const int v = L::lo(pick<R>(s.H, rr % R));
-      if (jobD) put_score_job(a, jobD, jobld, xo, yoA, v);
-      else put_score(a, xo, yoA, v);
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    if (wantA[k]) {
+      const int rr = rowA - b * BAND;
+      if (rr >= 0 && rr < BAND && sl == rr / R) {
+        const int v = L::lo(pick<R>(s[k].H, rr % R)) + gsh;
+        if (jobD) put_score_job(a, jobD, jobld, xo[k], yoA, v);
+        else put_score(a, xo[k], yoA, v);
+      }
     }
-  }
-  if (P == 2 && wantB) {
-    const int rr = rowB - b * BAND;
-    if (rr >= 0 && rr < BAND && sl == rr / R) {
-      const int v = L::hi(pick<R>(s.H, rr % R));
-      if (jobD) put_score_job(a, jobD, jobld, xo, yoB, v);
-      else put_score(a, xo, yoB, v);
+    if (P == 2 && wantB[k]) {
+      const int rr = rowB - b * BAND;
+      if (rr >= 0 && rr < BAND && sl == rr / R) {
+        const int v = L::hi(pick<R>(s[k].H, rr % R)) + gsh;
+        if (jobD) put_score_job(a, jobD, jobld, xo[k], yoB, v);
+        else put_score(a, xo[k], yoB, v);
+      }
     }
   }
 }
 
 template <int R, int P, int V>
 struct MinBlocks {
-  static constexpr int value = V == 0 ? 1 : (R <= 8 ? 4 : (R <= 16 ? 3 : 2));
+  static constexpr int rows = V == 5 ? 2 * R : R;   // register rows per lane
+  static constexpr int value = V == 0 ? 1 : (rows <= 8 ? 4 : (rows <= 16 ? 3 : 2));
 };
 
 template <int R, int P, int V, int W>
 __global__ void __launch_bounds__(kWaveThreads, (MinBlocks<R, P, V>::value)) wave_kernel(const WaveArgs a) {
   constexpr int S = 32 / W;                // fronts per warp
+  constexpr int K = Layout<V>::K;          // X per front
   constexpr int BAND = W * R;
   constexpr int Q = R / 4;
   static_assert(R % 4 == 0, "rows per lane must be a multiple of 4");
@@ -313,7 +456,7 @@ __global__ void __launch_bounds__(kWaveThreads, (MinBlocks<R, P, V>::value)) wav
   const int seg = lane / W;                // front within the warp
   for (int e = threadIdx.x; e < kLetters * kLetters; e += blockDim.x) s_sub[e] = a.sub[e];
   int32_t* scratch =
-      a.scratch + ((size_t)(blockIdx.x * kWaveWarps + warp) * S + seg) * 4 * (size_t)a.scratch_cols;
+      a.scratch + ((size_t)(blockIdx.x * kWaveWarps + warp) * S + seg) * K * 4 * (size_t)a.scratch_cols;
 
   for (;;) {
     __syncthreads();
@@ -335,35 +478,46 @@ __global__ void __launch_bounds__(kWaveThreads, (MinBlocks<R, P, V>::value)) wav
     const int xbase = a.group_xbase ? a.group_xbase[g] : 0;
     float* jobD = a.group_dofs ? a.D + a.group_dofs[g] : nullptr;
     const int64_t jobld = a.group_ld ? a.group_ld[g] : a.ld;
-    const int i = xbase + (int)(chunk * (kWaveWarps * S)) + warp * S + seg;
     const int LyA = a.ylen[y0];
     const int LyB = has_b ? a.ylen[y1] : 0;
     const int8_t* YA = a.codes + a.ystart[y0];
     const int8_t* YB = has_b ? a.codes + a.ystart[y1] : YA;
-    const bool active = i < xbase + nX;
-    const int8_t* X = a.codes + (active ? a.xstart[i] : 0);
-    bool wantA = active && (!a.triangle || i <= y0);
-    bool wantB = active && has_b && (!a.triangle || i <= y1);
-    if (P == 2 && a.check_bound && active) {
-      // A carry out of an overflowing low half would reach the high half of
-      // the same word, so an unsafe A pair also sends B to the re-run queue.
-      const bool safeA = int16_safe(a, i, y0);
-      const bool safeB = !has_b || int16_safe(a, i, y1);
-      if (wantA && !safeA) {
-        if (sl == 0) queue_rerun(a, i, y0);
-        wantA = false;
+    const int8_t* X[K];
+    int Lx[K], xo[K];
+    bool wantA[K], wantB[K];
+    unsigned lmax = 0, lmin = 0x7fffffffu;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int i = xbase + (int)(chunk * (kWaveWarps * S * K)) + (warp * S + seg) * K + k;
+      const bool active = i < xbase + nX;
+      X[k] = a.codes + (active ? a.xstart[i] : 0);
+      wantA[k] = active && (!a.triangle || i <= y0);
+      wantB[k] = active && has_b && (!a.triangle || i <= y1);
+      if (P == 2 && a.check_bound && active) {
+        // A carry out of an overflowing low half would reach the high half of
+        // the same word, so an unsafe A pair also sends B to the re-run queue.
+        const bool safeA = int16_safe(a, i, y0);
+        const bool safeB = !has_b || int16_safe(a, i, y1);
+        if (wantA[k] && !safeA) {
+          if (sl == 0) queue_rerun(a, i, y0);
+          wantA[k] = false;
+        }
+        if (wantB[k] && !(safeA && safeB)) {
+          if (sl == 0) queue_rerun(a, i, y1);
+          wantB[k] = false;
+        }
       }
-      if (wantB && !(safeA && safeB)) {
-        if (sl == 0) queue_rerun(a, i, y1);
-        wantB = false;
+      Lx[k] = (wantA[k] || wantB[k]) ? a.xlen[i] : 0;
+      xo[k] = active ? a.xorig[i] : 0;
+      if (Lx[k] > 0) {
+        lmax = max(lmax, (unsigned)Lx[k]);
+        lmin = min(lmin, (unsigned)Lx[k]);
       }
     }
-    const int Lx = (wantA || wantB) ? a.xlen[i] : 0;
-    const int Lmax = __reduce_max_sync(0xffffffffu, (unsigned)Lx);
-    const int Lmin = (int)__reduce_min_sync(0xffffffffu, Lx > 0 ? (unsigned)Lx : 0x7fffffffu);
+    const int Lmax = (int)__reduce_max_sync(0xffffffffu, lmax);
+    const int Lmin = (int)__reduce_min_sync(0xffffffffu, lmin);
     const int rows = LyA > LyB ? LyA : LyB;
     const int nb = (rows + BAND - 1) / BAND;
-    const int xo = active ? a.xorig[i] : 0;
     const int yoA = a.yorig[y0];
     const int yoB = has_b ? a.yorig[y1] : 0;
 
@@ -374,10 +528,11 @@ __global__ void __launch_bounds__(kWaveThreads, (MinBlocks<R, P, V>::value)) wav
         const int row = e - x * BAND;
         const int k = row / R, r = row - k * R;
         const int grow = b * BAND + row;
-        const int sa = grow < LyA ? (int)s_sub[clamp_code(YA[grow]) * kLetters + x] : 0;
+        const int gsh = Layout<V>::L == 3 ? a.go : 0;   // layout 3 adds the profile to T = H - go
+        const int sa = (grow < LyA ? (int)s_sub[clamp_code(YA[grow]) * kLetters + x] : 0) + gsh;
         uint32_t w;
         if (P == 2) {
-          const int sb = grow < LyB ? (int)s_sub[clamp_code(YB[grow]) * kLetters + x] : 0;
+          const int sb = (grow < LyB ? (int)s_sub[clamp_code(YB[grow]) * kLetters + x] : 0) + gsh;
           w = Lanes<2>::arith(sa, sb);
         } else {
           w = (uint32_t)sa;
@@ -416,37 +571,33 @@ int occupancy_one() {
 }
 
 // The (P, V, W) combinations that exist: W = 32 with every P and V; the
-// narrow fronts (W = 16, 8) on int16x2 lanes with V = 0 or 2.
+// narrow fronts (W = 16, 8) on int16x2 lanes with V = 0, 2, 3, 4 or 5.
 inline bool wave_variant_exists(int P, int V, int W) {
-  if (W == 32) return (P == 1 || P == 2) && V >= 0 && V <= 2;
-  return (W == 16 || W == 8) && P == 2 && (V == 0 || V == 2);
+  if (W == 32) return (P == 1 || P == 2) && V >= 0 && V <= 5;
+  return (W == 16 || W == 8) && P == 2 && (V == 0 || V == 2 || V == 3 || V == 4 || V == 5);
 }
 
 // Entry points of one rows-per-lane template (every existing P, V, W).
 template <int R>
 struct Entry {
+  template <int P, int W, class Fn>
+  static auto with_v(int V, Fn&& fn) {
+    using std::integral_constant;
+    if (V == 5) return fn(integral_constant<int, P>{}, integral_constant<int, 5>{}, integral_constant<int, W>{});
+    if (V == 4) return fn(integral_constant<int, P>{}, integral_constant<int, 4>{}, integral_constant<int, W>{});
+    if (V == 3) return fn(integral_constant<int, P>{}, integral_constant<int, 3>{}, integral_constant<int, W>{});
+    if (V == 2) return fn(integral_constant<int, P>{}, integral_constant<int, 2>{}, integral_constant<int, W>{});
+    if constexpr (W == 32) {
+      if (V == 1) return fn(integral_constant<int, P>{}, integral_constant<int, 1>{}, integral_constant<int, W>{});
+    }
+    return fn(integral_constant<int, P>{}, integral_constant<int, 0>{}, integral_constant<int, W>{});
+  }
   template <class Fn>
   static auto with(int P, int V, int W, Fn&& fn) {
-    if (W == 16) return V == 2 ? fn(std::integral_constant<int, 2>{}, std::integral_constant<int, 2>{},
-                                    std::integral_constant<int, 16>{})
-                               : fn(std::integral_constant<int, 2>{}, std::integral_constant<int, 0>{},
-                                    std::integral_constant<int, 16>{});
-    if (W == 8) return V == 2 ? fn(std::integral_constant<int, 2>{}, std::integral_constant<int, 2>{},
-                                   std::integral_constant<int, 8>{})
-                              : fn(std::integral_constant<int, 2>{}, std::integral_constant<int, 0>{},
-                                   std::integral_constant<int, 8>{});
-    if (P == 2) {
-      if (V == 2) return fn(std::integral_constant<int, 2>{}, std::integral_constant<int, 2>{},
-                            std::integral_constant<int, 32>{});
-      if (V == 1) return fn(std::integral_constant<int, 2>{}, std::integral_constant<int, 1>{},
-                            std::integral_constant<int, 32>{});
-      return fn(std::integral_constant<int, 2>{}, std::integral_constant<int, 0>{}, std::integral_constant<int, 32>{});
-    }
-    if (V == 2) return fn(std::integral_constant<int, 1>{}, std::integral_constant<int, 2>{},
-                          std::integral_constant<int, 32>{});
-    if (V == 1) return fn(std::integral_constant<int, 1>{}, std::integral_constant<int, 1>{},
-                          std::integral_constant<int, 32>{});
-    return fn(std::integral_constant<int, 1>{}, std::integral_constant<int, 0>{}, std::integral_constant<int, 32>{});
+    if (W == 16) return with_v<2, 16>(V, fn);
+    if (W == 8) return with_v<2, 8>(V, fn);
+    if (P == 2) return with_v<2, 32>(V, fn);
+    return with_v<1, 32>(V, fn);
   }
   static cudaError_t launch(int P, int V, int W, const WaveArgs& a, int grid, cudaStream_t s) {
     if (!wave_variant_exists(P, V, W)) return cudaErrorInvalidValue;

@@ -97,10 +97,14 @@ class Context:
         self._check(self._lib.nwg_set_stream(self.h, ctypes.c_void_p(stream_handle or 0)))
 
     # ---- measurement -----------------------------------------------------
-    def dpx_peak(self, lanes16: bool = True) -> float:
-        """Cells/s of the bare DPX cell update on every SM (roofline)."""
+    def dpx_peak(self, lanes16: bool = True, form: int | None = None) -> float:
+        """Cells/s of the bare cell update on every SM (roofline): the fastest
+        form, or one form (nwg_dpx_peak_form)."""
         v = ctypes.c_double()
-        self._check(self._lib.nwg_dpx_peak(self.h, 1 if lanes16 else 0, ctypes.byref(v)))
+        if form is None:
+            self._check(self._lib.nwg_dpx_peak(self.h, 1 if lanes16 else 0, ctypes.byref(v)))
+        else:
+            self._check(self._lib.nwg_dpx_peak_form(self.h, 1 if lanes16 else 0, int(form), ctypes.byref(v)))
         return v.value
 
     def autotune(self, force: bool = False) -> dict:

@@ -147,7 +147,8 @@ def test_config1_full_size_properties_and_sample(ctx):
 
 
 @pytest.mark.parametrize("R", [4, 8, 12, 16, 20, 24, 32])
-@pytest.mark.parametrize("V,W", [(0, 32), (1, 32), (2, 32), (0, 16), (2, 16), (0, 8), (2, 8)])
+@pytest.mark.parametrize("V,W", [(0, 32), (1, 32), (2, 32), (3, 32), (4, 32), (5, 32), (0, 16), (2, 16), (3, 16),
+                                 (4, 16), (5, 16), (0, 8), (2, 8), (3, 8), (4, 8), (5, 8)])
 def test_every_kernel_template_matches_oracle(R, V, W):
     # the autotuner may pick any (rows per lane, register layout, front width)
     # for any length class: every template must be exact, single- and
@@ -184,7 +185,7 @@ def _gap_case_sets():
     (3, 5, "blosum", "short"), (15, 1, "blosum", "short"), (0, 0, "blosum", "short"),
     (10, 20, "blosum", "long_ge20"), (10, 2, "x3", "runs"), (10, 2, "x3", "short"),
     (40, 30, "blosum", "short")])
-@pytest.mark.parametrize("V", [0, 1, 2])
+@pytest.mark.parametrize("V", [0, 1, 2, 3, 4, 5])
 def test_gap_penalties_and_matrices_match_oracle(go, ge, mat, case, V):
     # the int16 guard follows the context's penalties and matrix
     from mestrado_gb300 import Context
