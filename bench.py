@@ -39,6 +39,10 @@ sys.path.insert(0, ROOT)
 CONFIG = 2
 METRIC = "nw_gcups_batched"
 UNIT = "GCUPS"
+# DRAM bytes per launch of the dominant kernel of this workload, from one ncu capture of
+# the full-size launch (profiles/wave_kernel_24_v4_w16_config2_small.md); reported only
+# when that kernel is the dominant one of the run
+NCU_TRAFFIC = {"wave_kernel<R=24,int16x2,V=4,W=16>": 69883392 + 127747584}
 
 
 def _dist():
@@ -484,10 +488,12 @@ def main():
     if dom is not None:
         peak = peak16 if dom["lanes16"] else peak32
         ach = dom["cells"] / (dom["ms"] / 1e3)
+        kname = (f"wave_kernel<R={dom['rows_per_lane']},{'int16x2' if dom['lanes16'] else 'int32'},"
+                 f"V={dom['variant']},W={dom['lanes']}>")
         roof = {"bound": "int", "achieved": ach / 1e9, "peak": peak / 1e9, "unit": "GCUPS",
-                "frac": ach / peak, "traffic": None,
-                "kernel": f"wave_kernel<R={dom['rows_per_lane']},{'int16x2' if dom['lanes16'] else 'int32'},"
-                          f"V={dom['variant']},W={dom['lanes']}>",
+                "frac": ach / peak, "traffic": NCU_TRAFFIC.get(kname),
+                "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
+                "kernel": kname,
                 "launch_ms": dom["ms"], "launch_cells": dom["cells"],
                 "peak_source": "nwg_dpx_peak: the 5-instruction cell update (faster of the two forms the "
                                "kernels use) on every SM, registers only, measured in this run",
