@@ -80,6 +80,7 @@ struct NJDev {
                               // [3] open heap-size checks, [4] rebuilds (per-CTA path)
   nwg_join* joins;
   float* vd;           // per slot, new row values
+  float* rmin;         // per slot: smallest float q of the row's pairs (c > r) in this join
   int n0;
   int cand_cap;        // candidate list capacity
 };
@@ -120,6 +121,29 @@ __device__ __forceinline__ int low_bit_exp(float f) {
   const unsigned e = b >> 23, m = b & 0x7FFFFFu;
   if (e == 0) return -149 + __ffs(m) - 1;
   return (int)e - 150 + __ffs(m | 0x800000u) - 1;
+}
+
+// Exponent of the highest set bit of |f| (f = m * 2^(e) with m in [1, 2)),
+// INT_MIN for 0.
+__device__ __forceinline__ int top_bit_exp(float f) {
+  const unsigned b = __float_as_uint(f) & 0x7FFFFFFFu;
+  if (b == 0) return INT_MIN;
+  const unsigned e = b >> 23, m = b & 0x7FFFFFu;
+  if (e == 0) return -149 + (31 - __clz(m));
+  return (int)e - 127;
+}
+
+// f as a signed integer count of 2^lowexp (exact: lowexp is at most the
+// lowest set bit of f, and |f| < 2^(lowexp + 49) is checked by the caller).
+__device__ __forceinline__ long long float_units(float f, int lowexp) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xFFu, m = b & 0x7FFFFFu;
+  if (e == 0 && m == 0) return 0;
+  const long long mant = e == 0 ? (long long)m : (long long)(m | 0x800000u);
+  const int sh = (e == 0 ? -149 : (int)e - 150) - lowexp;   // value = mant * 2^(sh + lowexp)
+  // a right shift drops only zero bits: lowexp <= the lowest set bit of f
+  const long long v = sh >= 0 ? mant << sh : mant >> (-sh);
+  return (b >> 31) ? -v : v;
 }
 
 // A sequential double sum of floats equals any-order sum when every partial
@@ -196,6 +220,7 @@ __global__ void __launch_bounds__(256) pass_min_kernel(NJDev s, float nm2f) {
       qmin = fminf(qmin, sq[w]);
       mmax = fmaxf(mmax, sm[w]);
     }
+    s.rmin[r] = qmin;
     if (qmin < FLT_MAX) {
       atomicMin(&s.g32[0], ford(qmin));
       atomicMax(&s.g32[1], ford(mmax));
@@ -212,6 +237,7 @@ __global__ void __launch_bounds__(256) pass_cand_kernel(NJDev s, float nm2f, dou
   const float qmin = iord(s.g32[0]);
   const float mmax = iord(s.g32[1]);
   const float thr = qmin + 3.f * (8.f * 5.9604645e-8f * mmax) + 1e-30f;
+  if (s.rmin[r] > thr) return;   // no pair of this row is a candidate
   const float tr = s.Tf[r];
   const float* row = s.D + (size_t)r * s.n0;
   for (int c = r + 1 + threadIdx.x; c < s.n0; c += blockDim.x) {
@@ -232,92 +258,67 @@ __global__ void __launch_bounds__(256) pass_cand_kernel(NJDev s, float nm2f, dou
 }
 
 // Winner among the candidates, ambiguity and tie count; resets the pass
-// accumulators for the next join.  One CTA (any multiple of 32 threads).
+// accumulators for the next join.  Warp 0 of the CTA does the work (the list
+// holds a few entries: double-precision work on every warp would only load
+// the FP64 pipe); the other warps wait at the final barrier.
 __device__ void pick_body(const NJDev& s) {
-  __shared__ double sq[32];
-  __shared__ int sa[32], sb[32];
-  __shared__ unsigned s_ties, s_amb;
-  const int nc = min(s.g32[2], s.cand_cap);
-  double bq = DBL_MAX;
-  int ba = INT_MAX, bb = -1;
-  for (int k = threadIdx.x; k < nc; k += blockDim.x) {
-    const Cand c = s.cand[k];
-    if (better(c.q1, c.b, c.a, bq, bb, ba)) {
-      bq = c.q1;
-      ba = c.a;
-      bb = c.b;
-    }
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    const double q2 = __shfl_down_sync(0xffffffffu, bq, o);
-    const int a2 = __shfl_down_sync(0xffffffffu, ba, o);
-    const int b2 = __shfl_down_sync(0xffffffffu, bb, o);
-    if (better(q2, b2, a2, bq, bb, ba)) {
-      bq = q2;
-      ba = a2;
-      bb = b2;
-    }
-  }
-  if ((threadIdx.x & 31) == 0) {
-    sq[threadIdx.x >> 5] = bq;
-    sa[threadIdx.x >> 5] = ba;
-    sb[threadIdx.x >> 5] = bb;
-  }
-  if (threadIdx.x == 0) {
-    s_ties = 0;
-    s_amb = 0;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
-      if (better(sq[w], sb[w], sa[w], bq, bb, ba)) {
-        bq = sq[w];
-        ba = sa[w];
-        bb = sb[w];
+  if (threadIdx.x < 32) {
+    const int l = threadIdx.x;
+    const int nc = min(s.g32[2], s.cand_cap);
+    // the reduction carries the heap rounding q2 of the best entry with it
+    double bq = DBL_MAX, bq2 = DBL_MAX;
+    int ba = INT_MAX, bb = -1;
+    for (int k = l; k < nc; k += 32) {
+      const Cand c = s.cand[k];
+      if (better(c.q1, c.b, c.a, bq, bb, ba)) {
+        bq = c.q1;
+        bq2 = c.q2;
+        ba = c.a;
+        bb = c.b;
       }
-    sq[0] = bq;
-    sa[0] = ba;
-    sb[0] = bb;
-  }
-  __syncthreads();
-  bq = sq[0];
-  ba = sa[0];
-  bb = sb[0];
-  double q2w = DBL_MAX;
-  for (int k = 0; k < nc; ++k) {   // the winner's heap value (the list is short)
-    const Cand c = s.cand[k];
-    if (c.a == ba && c.b == bb) {
-      q2w = c.q2;
-      break;
     }
-  }
-  const double hiw = fmax(bq, q2w);
-  const bool robust_w = bq == q2w;
-  unsigned ties = 0, amb = 0;
-  for (int k = threadIdx.x; k < nc; k += blockDim.x) {
-    const Cand c = s.cand[k];
-    const double lo = fmin(c.q1, c.q2);
-    if (lo > hiw) continue;
-    if (c.a == ba && c.b == bb) ++ties;
-    else if (robust_w && c.q1 == c.q2 && c.q1 == bq) ++ties;
-    else ++amb;
-  }
-  if (ties) atomicAdd(&s_ties, ties);
-  if (amb) atomicAdd(&s_amb, amb);
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    Pick p;
-    p.q1 = bq;
-    p.q2 = q2w;
-    p.a = ba;
-    p.b = bb;
-    *s.win = p;
-    if (bb < 0 || s.g32[2] > s.cand_cap) atomicAdd(&s.stats[2], 1ull);   // no candidate / list overflow
-    else if (s_amb > 0 || s_ties > 4) atomicAdd(&s.stats[0], 1ull);
-    else if (s_ties > 1) atomicAdd(&s.stats[1], 1ull);
-    s.g32[0] = 0x7F7FFFFF;          // ordered-int of FLT_MAX
-    s.g32[1] = 0;
-    s.g32[2] = 0;
+    for (int o = 16; o > 0; o >>= 1) {
+      const double q = __shfl_xor_sync(0xffffffffu, bq, o);
+      const double q2 = __shfl_xor_sync(0xffffffffu, bq2, o);
+      const int a2 = __shfl_xor_sync(0xffffffffu, ba, o);
+      const int b2 = __shfl_xor_sync(0xffffffffu, bb, o);
+      if (better(q, b2, a2, bq, bb, ba)) {
+        bq = q;
+        bq2 = q2;
+        ba = a2;
+        bb = b2;
+      }
+    }
+    // every lane now holds the winner (the order is total: q, then ids)
+    const double hiw = fmax(bq, bq2);
+    const bool robust_w = bq == bq2;
+    unsigned ties = 0, amb = 0;
+    for (int k = l; k < nc; k += 32) {
+      const Cand c = s.cand[k];
+      const double lo = fmin(c.q1, c.q2);
+      if (lo > hiw) continue;
+      if (c.a == ba && c.b == bb) ++ties;
+      else if (robust_w && c.q1 == c.q2 && c.q1 == bq) ++ties;
+      else ++amb;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      ties += __shfl_xor_sync(0xffffffffu, ties, o);
+      amb += __shfl_xor_sync(0xffffffffu, amb, o);
+    }
+    if (l == 0) {
+      Pick p;
+      p.q1 = bq;
+      p.q2 = bq2;
+      p.a = ba;
+      p.b = bb;
+      *s.win = p;
+      if (bb < 0 || s.g32[2] > s.cand_cap) atomicAdd(&s.stats[2], 1ull);   // no candidate / list overflow
+      else if (amb > 0 || ties > 4) atomicAdd(&s.stats[0], 1ull);
+      else if (ties > 1) atomicAdd(&s.stats[1], 1ull);
+      s.g32[0] = 0x7F7FFFFF;          // ordered-int of FLT_MAX
+      s.g32[1] = 0;
+      s.g32[2] = 0;
+    }
   }
   __syncthreads();
 }
@@ -329,8 +330,8 @@ __global__ void __launch_bounds__(1024) pick_kernel(NJDev s) { pick_body(s); }
 __device__ void join_body(const NJDev& s, int step, int next, int m_n, float* tv, int* ids) {
   __shared__ int s_pos[1024 / 32 + 1];
   __shared__ int s_skip[2];
-  __shared__ double s_part[32], s_ab[32];
-  __shared__ int s_low[32];
+  __shared__ long long s_isum[32], s_iabs[32];
+  __shared__ int s_low[33], s_top[33];
   const Pick w = *s.win;
   if (w.b < 0) return;                 // counted as an internal error by pick_kernel
   const int i = w.a, j = w.b;          // i < j
@@ -391,39 +392,77 @@ __device__ void join_body(const NJDev& s, int step, int next, int m_n, float* tv
     s.Tf[sk] = (float)t;
   }
   __syncthreads();
-  // sum of tmp in ascending id order (SpeciesBlock.cpp:799, :818): the block's
-  // any-order sum when it is provably exact, else the sequential loop
+  // sum of tmp in ascending id order (SpeciesBlock.cpp:799, :818): the exact
+  // sum, taken in 64-bit integers of 2^e (e = the lowest set bit of any term),
+  // when it proves that every partial sum of the sequential loop is exact,
+  // else the sequential loop itself
   {
-    double part = 0.0, ab = 0.0;
-    int lowexp = INT_MAX;
+    int lowexp = INT_MAX, topexp = INT_MIN;
     for (int k = threadIdx.x; k < na; k += blockDim.x) {
       const float x = tv[k];            // 0 at i and j
-      part = __dadd_rn(part, (double)x);
-      ab = __dadd_rn(ab, (double)fabsf(x));
       lowexp = min(lowexp, low_bit_exp(x));
+      topexp = max(topexp, top_bit_exp(x));
     }
     for (int o = 16; o > 0; o >>= 1) {
-      part = __dadd_rn(part, __shfl_down_sync(0xffffffffu, part, o));
-      ab = __dadd_rn(ab, __shfl_down_sync(0xffffffffu, ab, o));
-      lowexp = min(lowexp, __shfl_down_sync(0xffffffffu, lowexp, o));
+      lowexp = min(lowexp, __shfl_xor_sync(0xffffffffu, lowexp, o));
+      topexp = max(topexp, __shfl_xor_sync(0xffffffffu, topexp, o));
     }
     if ((threadIdx.x & 31) == 0) {
-      s_part[threadIdx.x >> 5] = part;
-      s_ab[threadIdx.x >> 5] = ab;
       s_low[threadIdx.x >> 5] = lowexp;
+      s_top[threadIdx.x >> 5] = topexp;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-      part = 0.0;
-      ab = 0.0;
-      lowexp = INT_MAX;
-      for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2) {
-        part = __dadd_rn(part, s_part[w2]);
-        ab = __dadd_rn(ab, s_ab[w2]);
-        lowexp = min(lowexp, s_low[w2]);
+    if (threadIdx.x < 32) {
+      const int nw = (int)(blockDim.x >> 5);
+      lowexp = threadIdx.x < nw ? s_low[threadIdx.x] : INT_MAX;
+      topexp = threadIdx.x < nw ? s_top[threadIdx.x] : INT_MIN;
+      for (int o = 16; o > 0; o >>= 1) {
+        lowexp = min(lowexp, __shfl_xor_sync(0xffffffffu, lowexp, o));
+        topexp = max(topexp, __shfl_xor_sync(0xffffffffu, topexp, o));
       }
-      double sum = part;
-      if (!sum_is_exact(ab, lowexp)) {
+      if (threadIdx.x == 0) {
+        s_low[32] = lowexp;
+        s_top[32] = topexp;
+      }
+    }
+    __syncthreads();
+    lowexp = s_low[32];
+    topexp = s_top[32];
+    // every term below 2^49 units of 2^e: sums of up to 8192 terms stay below 2^62
+    const bool fits = lowexp == INT_MAX || topexp - lowexp < 48;
+    long long isum = 0, iabs = 0;
+    if (fits && lowexp != INT_MAX) {
+      for (int k = threadIdx.x; k < na; k += blockDim.x) {
+        const long long v = float_units(tv[k], lowexp);
+        isum += v;
+        iabs += v < 0 ? -v : v;
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        isum += __shfl_xor_sync(0xffffffffu, isum, o);
+        iabs += __shfl_xor_sync(0xffffffffu, iabs, o);
+      }
+      if ((threadIdx.x & 31) == 0) {
+        s_isum[threadIdx.x >> 5] = isum;
+        s_iabs[threadIdx.x >> 5] = iabs;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x < 32 && fits && lowexp != INT_MAX) {
+      const int nw = (int)(blockDim.x >> 5);
+      isum = threadIdx.x < nw ? s_isum[threadIdx.x] : 0;
+      iabs = threadIdx.x < nw ? s_iabs[threadIdx.x] : 0;
+      for (int o = 16; o > 0; o >>= 1) {
+        isum += __shfl_xor_sync(0xffffffffu, isum, o);
+        iabs += __shfl_xor_sync(0xffffffffu, iabs, o);
+      }
+    }
+    if (threadIdx.x == 0) {
+      double sum;
+      if (lowexp == INT_MAX) {
+        sum = 0.0;                                     // every term is zero
+      } else if (fits && iabs < (1ll << 53)) {
+        sum = ldexp((double)isum, lowexp);             // exact: |isum| < 2^53
+      } else {
         const int ki = s_skip[0], kj = s_skip[1];
         sum = 0.0;
         for (int k = 0; k < na; ++k)
@@ -530,45 +569,60 @@ __device__ void cta_rowsums(const NJDev& s) {
   __syncthreads();
 }
 
-__device__ void cta_pass_min(const NJDev& s, float nm2f) {
+// sTf / snode: shared-memory copies of s.Tf and s.node (refreshed after every
+// join); srmin: per slot, the smallest float q of the row (for the second pass)
+__device__ void cta_pass_min(const NJDev& s, float nm2f, const float* __restrict__ sTf,
+                             const int* __restrict__ snode, float* __restrict__ srmin) {
   __shared__ float sq[32], sm[32];
   const int na = *s.na;
   const int lane = threadIdx.x & 31;
   float qmin = FLT_MAX, mmax = 0.f;
   for (int k = threadIdx.x >> 5; k < na; k += blockDim.x >> 5) {
     const int r = s.slot[s.act[k]];
-    const float tr = s.Tf[r];
-    const float* row = s.D + (size_t)r * s.n0;
+    const float tr = sTf[r];
+    const float* __restrict__ row = s.D + (size_t)r * s.n0;
+    float rq = FLT_MAX;
+#pragma unroll 4
     for (int c = r + 1 + lane; c < s.n0; c += 32) {
-      if (s.node[c] < 0) continue;
-      const float tc = s.Tf[c];
-      const float x = __fmul_rn(row[c], nm2f);
-      qmin = fminf(qmin, __fsub_rn(__fsub_rn(x, tr), tc));
-      mmax = fmaxf(mmax, __fadd_rn(__fadd_rn(fabsf(x), fabsf(tr)), fabsf(tc)));
+      // branch-free: a dead slot's (finite, stale) entries are masked out
+      const float d = row[c];
+      const bool live = snode[c] >= 0;
+      const float tc = sTf[c];
+      const float x = __fmul_rn(d, nm2f);
+      const float q = __fsub_rn(__fsub_rn(x, tr), tc);
+      const float mag = __fadd_rn(__fadd_rn(fabsf(x), fabsf(tr)), fabsf(tc));
+      rq = fminf(rq, live ? q : FLT_MAX);
+      mmax = fmaxf(mmax, live ? mag : 0.f);
     }
+    for (int o = 16; o > 0; o >>= 1) rq = fminf(rq, __shfl_xor_sync(0xffffffffu, rq, o));
+    if (lane == 0) srmin[r] = rq;
+    qmin = fminf(qmin, rq);
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    qmin = fminf(qmin, __shfl_down_sync(0xffffffffu, qmin, o));
-    mmax = fmaxf(mmax, __shfl_down_sync(0xffffffffu, mmax, o));
-  }
+  for (int o = 16; o > 0; o >>= 1) mmax = fmaxf(mmax, __shfl_down_sync(0xffffffffu, mmax, o));
   if (lane == 0) {
     sq[threadIdx.x >> 5] = qmin;
     sm[threadIdx.x >> 5] = mmax;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
-      qmin = fminf(qmin, sq[w]);
-      mmax = fmaxf(mmax, sm[w]);
+  if (threadIdx.x < 32) {
+    const int nw = (int)(blockDim.x >> 5);
+    qmin = lane < nw ? sq[lane] : FLT_MAX;
+    mmax = lane < nw ? sm[lane] : 0.f;
+    for (int o = 16; o > 0; o >>= 1) {
+      qmin = fminf(qmin, __shfl_xor_sync(0xffffffffu, qmin, o));
+      mmax = fmaxf(mmax, __shfl_xor_sync(0xffffffffu, mmax, o));
     }
-    s.g32[0] = ford(qmin);
-    s.g32[1] = ford(mmax);
-    s.g32[2] = 0;
+    if (lane == 0) {
+      s.g32[0] = ford(qmin);
+      s.g32[1] = ford(mmax);
+      s.g32[2] = 0;
+    }
   }
   __syncthreads();
 }
 
-__device__ void cta_pass_cand(const NJDev& s, float nm2f, double nm2, int watermark) {
+__device__ void cta_pass_cand(const NJDev& s, float nm2f, double nm2, int watermark, const float* __restrict__ sTf,
+                              const int* __restrict__ snode, const float* __restrict__ srmin) {
   const int na = *s.na;
   const int lane = threadIdx.x & 31;
   const float qmin = iord(s.g32[0]);
@@ -577,13 +631,15 @@ __device__ void cta_pass_cand(const NJDev& s, float nm2f, double nm2, int waterm
   for (int k = threadIdx.x >> 5; k < na; k += blockDim.x >> 5) {
     const int ur = s.act[k];
     const int r = s.slot[ur];
-    const float tr = s.Tf[r];
-    const float* row = s.D + (size_t)r * s.n0;
+    if (srmin[r] > thr) continue;   // no pair of this row is a candidate
+    const float tr = sTf[r];
+    const float* __restrict__ row = s.D + (size_t)r * s.n0;
+#pragma unroll 4
     for (int c = r + 1 + lane; c < s.n0; c += 32) {
-      const int uc = s.node[c];
-      if (uc < 0) continue;
       const float d = row[c];
-      const float q = __fsub_rn(__fsub_rn(__fmul_rn(d, nm2f), tr), s.Tf[c]);
+      const int uc = snode[c];
+      if (uc < 0) continue;
+      const float q = __fsub_rn(__fsub_rn(__fmul_rn(d, nm2f), tr), sTf[c]);
       if (q > thr) continue;
       const int a = min(ur, uc), b = max(ur, uc);
       Cand cd;
@@ -598,11 +654,23 @@ __device__ void cta_pass_cand(const NJDev& s, float nm2f, double nm2, int waterm
   __syncthreads();
 }
 
+// Shared-memory copies of the float row sums and the slot -> node map.
+__device__ void cta_refresh(const NJDev& s, float* sTf, int* snode) {
+  for (int k = threadIdx.x; k < s.n0; k += blockDim.x) {
+    sTf[k] = s.Tf[k];
+    snode[k] = s.node[k];
+  }
+  __syncthreads();
+}
+
 // The whole join loop of one job, schedule included (same as the host loop of
 // Ctx::nj).  Workspace pointers of every job are set by the host.
 __global__ void __launch_bounds__(1024) nj_cta_kernel(const NJJob* jobs, int njobs) {
   __shared__ float tv[kCtaMaxN];
   __shared__ int ids[kCtaMaxN];
+  __shared__ float sTf[kCtaMaxN];
+  __shared__ int snode[kCtaMaxN];
+  __shared__ float srmin[kCtaMaxN];
   if ((int)blockIdx.x >= njobs) return;
   const NJJob J = jobs[blockIdx.x];
   const NJDev& s = J.s;
@@ -619,6 +687,7 @@ __global__ void __launch_bounds__(1024) nj_cta_kernel(const NJJob* jobs, int njo
   __syncthreads();
   if (n < 2) return;
   cta_rowsums(s);
+  cta_refresh(s, sTf, snode);
   const int kBinT = 30 * 31 / 2;
   int steps = max((int)((float)n * 0.5f), 200);
   int pq_ck = 500;
@@ -627,8 +696,8 @@ __global__ void __launch_bounds__(1024) nj_cta_kernel(const NJJob* jobs, int njo
   int watermark = n, next = n, m_n = n, na = n;
   for (int step = 0; step < n - 1; ++step) {
     const double nm2 = (double)(m_n - 2);
-    cta_pass_min(s, (float)(m_n - 2));
-    cta_pass_cand(s, (float)(m_n - 2), nm2, watermark);
+    cta_pass_min(s, (float)(m_n - 2), sTf, snode, srmin);
+    cta_pass_cand(s, (float)(m_n - 2), nm2, watermark, sTf, snode, srmin);
     pick_body(s);
     join_body(s, step, next, m_n, tv, ids);
     if (--pq_ck == 0) {
@@ -649,15 +718,16 @@ __global__ void __launch_bounds__(1024) nj_cta_kernel(const NJJob* jobs, int njo
       --steps;
       ub += na - 1;
     }
+    cta_refresh(s, sTf, snode);
   }
 }
 
 }  // namespace
 
 struct NJState {
-  DevBuf D, T, Tf, slot, node, act, na, g32, cand, win, stats, joins, vd;
+  DevBuf D, T, Tf, slot, node, act, na, g32, cand, win, stats, joins, vd, rmin;
   ~NJState() {
-    for (DevBuf* b : {&D, &T, &Tf, &slot, &node, &act, &na, &g32, &cand, &win, &stats, &joins, &vd}) b->release();
+    for (DevBuf* b : {&D, &T, &Tf, &slot, &node, &act, &na, &g32, &cand, &win, &stats, &joins, &vd, &rmin}) b->release();
   }
 };
 
@@ -685,7 +755,8 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
       (rc = S.na.ensure(sizeof(int))) || (rc = S.g32.ensure(sizeof(int) * 4)) ||
       (rc = S.cand.ensure(sizeof(Cand) * kCandCap)) || (rc = S.win.ensure(sizeof(Pick))) ||
       (rc = S.stats.ensure(sizeof(unsigned long long) * 5)) ||
-      (rc = S.joins.ensure(sizeof(nwg_join) * (n - 1))) || (rc = S.vd.ensure(sizeof(float) * n)))
+      (rc = S.joins.ensure(sizeof(nwg_join) * (n - 1))) || (rc = S.vd.ensure(sizeof(float) * n)) ||
+      (rc = S.rmin.ensure(sizeof(float) * n)))
     return fail(rc, "nj allocation");
   cudaStream_t s = stream;
   const cudaMemcpyKind kind = device_D ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
@@ -718,6 +789,7 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
   d.stats = (unsigned long long*)S.stats.p;
   d.joins = (nwg_join*)S.joins.p;
   d.vd = (float*)S.vd.p;
+  d.rmin = (float*)S.rmin.p;
   d.n0 = n;
   d.cand_cap = kCandCap;
   const size_t join_smem = 2 * sizeof(float) * (size_t)n;
