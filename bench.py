@@ -13,7 +13,10 @@ second) with codes and matrix resident in HBM; e2e = the same metric through
 the host-buffer C ABI call (nwg_score_all: codes host->device, matrix
 device->host inside the timed region).  The line also carries the serving
 run (Poisson job arrivals, continuous batching): p50/p99 job latency and
-sustained GCUPS beside the same jobs run one by one.  --impl reference times the
+sustained GCUPS beside the same jobs run one by one, and the configuration-3
+pipeline (matrix -> neighbor joining -> cherry traceback of 8,000 sequences,
+checked against the reference's own tree) with the NJ and traceback
+rooflines.  --impl reference times the
 reference's recurrence restated on the CPU (its CUDA does not build on CUDA
 13) on every host core, on a bounded sample of the same pairs.
 
@@ -289,6 +292,88 @@ def serving_leg(seconds: float, rate: float = 200.0, sample_jobs: int = 200):
     }
 
 
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0}, "fallback"
+
+
+def pipeline_leg(cpu_nj_n: int = 2000):
+    """Configuration 3 end to end through the public API (host buffers): 8,000
+    sequences -> distance matrix -> neighbor joining -> cherry traceback,
+    checked against the tree the reference's own buildTree made on the same
+    matrix (tests/golden/cfg3).  NJ roofline: the live upper triangle read
+    once per join (4 B per live pair; the candidate pass revisits only rows
+    whose float minimum is near the global one).  Traceback roofline: 0.5 B
+    of direction flags written per DP cell.  CPU: the oracle's neighbor
+    joining (the reference's buildTree restated, one core) on the leading
+    cpu_nj_n x cpu_nj_n block of the same matrix, beside the device on the
+    same block."""
+    import hashlib
+
+    from mestrado_gb300 import Context, cherries, encode, newick, synth
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_py as O
+    from test_nj_cpu import golden_joins
+    gold = os.path.join(ROOT, "tests", "golden", "cfg3")
+    meta = json.load(open(os.path.join(gold, "meta.json")))
+    S = synth.config(3)
+    n = len(S)
+    ctx = Context(10, 2)
+    ctx.autotune()
+    ctx.score_all(S)                                   # plan, graph and tuning warm
+    t0 = time.perf_counter()
+    D = ctx.score_all(S)
+    t1 = time.perf_counter()
+    joins, st = ctx.nj(D, stats=True)
+    t2 = time.perf_counter()
+    node, left, right = cherries(joins["i"], joins["j"], n)
+    codes, off = encode(S)
+    t3 = time.perf_counter()
+    aln, ast = ctx.align_pairs(codes, off, left, right, stats=True)
+    t4 = time.perf_counter()
+    ref = golden_joins("cfg3")
+    exact = (hashlib.sha256(D.tobytes()).hexdigest() == meta["D_sha256"] and len(joins) == len(ref) and
+             all((a["node"], a["i"], a["j"], a["len_i"], a["len_j"]) == (b["node"], b["i"], b["j"], b["len_i"], b["len_j"])
+                 for a, b in zip(joins, ref)) and
+             newick(joins, [f">s{i}" for i in range(n)]) == open(os.path.join(gold, "tree.nwk")).read())
+    peaks, src = _peaks()
+    hbm = float(peaks["hbm_gbs"])
+    nj_bytes = sum(4.0 * m * (m - 1) / 2 for m in range(2, n + 1))
+    nj_gbs = nj_bytes / (st["device_ms"] * 1e-3) / 1e9
+    L = S.lengths.astype(np.float64)
+    tb_cells = float((L[left] * L[right]).sum())
+    tb_s = ast["kernel_ms"] * 1e-3 if ast.get("kernel_ms") else (t4 - t3)   # match + back kernels
+    tb_gbs = 0.5 * tb_cells / tb_s / 1e9
+    # CPU neighbor joining (oracle, one core) and the device on the same leading block
+    m = min(cpu_nj_n, n)
+    Dm = np.ascontiguousarray(D[:m, :m])
+    t5 = time.perf_counter()
+    O.nj(Dm.copy())
+    t6 = time.perf_counter()
+    ctx.nj(Dm)
+    t7 = time.perf_counter()
+    ctx.nj(Dm)
+    t8 = time.perf_counter()
+    ctx.close()
+    return {
+        "workload": "configuration 3: 8,000 seqs (40 families x 200, root length U[100,300]), all pairs -> NJ -> "
+                    "pairwise alignment of every guide-tree cherry; host buffers through the public API",
+        "exact_vs_reference_tree": bool(exact),
+        "score_s": t1 - t0, "nj_s": t2 - t1, "nj_device_s": st["device_ms"] * 1e-3, "nj_launches": st["launches"],
+        "nj_rebuilds": st["rebuilds"], "nj_ambiguous_steps": st["ambiguous_steps"],
+        "traceback_s": t4 - t3, "cherries": int(len(left)), "total_s": t4 - t0,
+        "nj_roofline": {"bound": "hbm", "achieved": nj_gbs, "peak": hbm, "unit": "GB/s", "frac": nj_gbs / hbm,
+                        "bytes": nj_bytes, "peak_source": src},
+        "traceback_roofline": {"bound": "hbm", "achieved": tb_gbs, "peak": hbm, "unit": "GB/s", "frac": tb_gbs / hbm,
+                               "cells": tb_cells, "kernel_s": tb_s, "peak_source": src},
+        "cpu_nj": {"n": m, "oracle_one_core_s": t6 - t5, "device_s": t8 - t7, "kind": "port",
+                   "note": "the reference's buildTree restated (exact argmin), one core"},
+    }
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
@@ -349,6 +434,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--subset", type=int, default=0,
                     help="score only the first N sequences (whole families first); for profiling runs")
+    ap.add_argument("--no-pipeline", action="store_true", help="skip the configuration-3 pipeline leg")
     ap.add_argument("--serve-seconds", type=float, default=10.0,
                     help="length of the serving run (Poisson arrivals at 200 jobs/s); 0 skips it")
     ap.add_argument("--quick", action="store_true",
@@ -484,6 +570,7 @@ def main():
     if rank != 0:
         return
     serving = serving_leg(args.serve_seconds) if args.serve_seconds > 0 else None
+    pipeline = None if args.no_pipeline else pipeline_leg()
     roof = None
     if dom is not None:
         peak = peak16 if dom["lanes16"] else peak32
@@ -523,6 +610,7 @@ def main():
         "wall_s": wall,
         "clocks": clk,
         "serving": serving,
+        "pipeline": pipeline,
     }
     print(json.dumps(line), flush=True)
 
