@@ -287,12 +287,12 @@ int nwg_set_tuning_lanes(nwg_ctx* ctx, const int32_t* rows_per_lane, const int32
  * (n^2 floats of matrix + NJ workspace + codes) fits hbm_budget_bytes and puts
  * up to max_batch_jobs of them into one batch: one persistent launch per
  * length bucket with pairs of all the batch's jobs interleaved, then one
- * launch with a CTA per job running the whole join loop.  Two batches can be
+ * launch with a cluster of 8 CTAs per job running the whole join loop.  Two batches can be
  * on the device at once (own streams), so jobs arriving while one batch runs
  * are admitted and overlap it.  Each job's matrix and join list equal what
  * nwg_score_all and nwg_nj return for that job alone.
- * Jobs with n <= 1024 sequences are accepted (larger: NWG_ERR_INVALID, run
- * them through a context).  The reference has no serving loop. */
+ * Jobs with n <= 8192 sequences are accepted (larger: NWG_ERR_INVALID).
+ * The reference has no serving loop. */
 typedef struct nwg_server nwg_server;
 
 typedef struct {

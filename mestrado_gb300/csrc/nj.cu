@@ -29,22 +29,32 @@
 // since the last build; that bound is tracked and any check it cannot exclude
 // is counted.
 //
-// Search per join, two streaming passes over the live triangle of D (HBM
-// bound: 2n^2 bytes per pass):
-//  1. q in float, fl(fl(fl(d*(n-2)) - Tf_r) - Tf_c) with Tf the float copy of
-//     T: its minimum and the largest magnitude M = |d|(n-2) + |T_r| + |T_c|.
-//     Every float q is within E = 8 * 2^-24 * M of the exact q.
-//  2. every pair whose float q is at most min + 3E gets its exact double q in
-//     both roundings; those candidates (typically a handful) go to a list.
-// A single CTA then takes the winner with the tie-break and runs the
-// ambiguity check on the list: any pair left out has q > winner + E, beyond
-// reach of either rounding.  All floating-point operations use the _rn
-// intrinsics in the reference's evaluation order (no contraction).
+// Search per join:
+//  1. one streaming pass over the live triangle of D (4 B per live pair):
+//     q in float, fl(fl(fl(d*(n-2)) - Tf_r) - Tf_c) with Tf the float copy of
+//     T; per row its minimum, overall the minimum and the largest magnitude
+//     M = |d|(n-2) + |T_r| + |T_c|.  Every float q is within E = 8 * 2^-24 * M
+//     of the exact q.
+//  2. the rows whose minimum is at most min + 3E (usually one or two) are
+//     scanned again; every pair of them within that threshold gets its exact
+//     double q in both roundings; those candidates go to a list.
+// Warp 0 then takes the winner with the tie-break and runs the ambiguity
+// check on the list: any pair left out has q > winner + E, beyond reach of
+// either rounding.  All floating-point operations use the _rn intrinsics in
+// the reference's evaluation order (no contraction).
+//
+// Two launch forms: up to 2048 taxa (and for the serving loop, every job) one
+// thread-block cluster runs the whole loop; larger matrices take a full-GPU
+// kernel for pass 1 and one CTA for the rest of each join, and are compacted
+// to their live slots (in slot order) at every rebuild step.
 #include <algorithm>
 #include <cfloat>
 #include <climits>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
+
+#include <cooperative_groups.h>
 
 #include "nwg_ctx.h"
 
@@ -228,35 +238,6 @@ __global__ void __launch_bounds__(256) pass_min_kernel(NJDev s, float nm2f) {
   }
 }
 
-// Pass 2: exact double q (both roundings) of every pair whose float q is
-// within min + 3E.
-__global__ void __launch_bounds__(256) pass_cand_kernel(NJDev s, float nm2f, double nm2, int watermark) {
-  if ((int)blockIdx.x >= *s.na) return;
-  const int ur = s.act[blockIdx.x];
-  const int r = s.slot[ur];
-  const float qmin = iord(s.g32[0]);
-  const float mmax = iord(s.g32[1]);
-  const float thr = qmin + 3.f * (8.f * 5.9604645e-8f * mmax) + 1e-30f;
-  if (s.rmin[r] > thr) return;   // no pair of this row is a candidate
-  const float tr = s.Tf[r];
-  const float* row = s.D + (size_t)r * s.n0;
-  for (int c = r + 1 + threadIdx.x; c < s.n0; c += blockDim.x) {
-    const int uc = s.node[c];
-    if (uc < 0) continue;
-    const float d = row[c];
-    const float q = __fsub_rn(__fsub_rn(__fmul_rn(d, nm2f), tr), s.Tf[c]);
-    if (q > thr) continue;
-    const int a = min(ur, uc), b = max(ur, uc);
-    Cand cd;
-    cd.q1 = q_record(s, d, a, b, watermark, nm2);
-    cd.q2 = q_heap(s, d, a, b, nm2);
-    cd.a = a;
-    cd.b = b;
-    const int k = atomicAdd(&s.g32[2], 1);
-    if (k < s.cand_cap) s.cand[k] = cd;
-  }
-}
-
 // Winner among the candidates, ambiguity and tie count; resets the pass
 // accumulators for the next join.  Warp 0 of the CTA does the work (the list
 // holds a few entries: double-precision work on every warp would only load
@@ -322,8 +303,6 @@ __device__ void pick_body(const NJDev& s) {
   }
   __syncthreads();
 }
-
-__global__ void __launch_bounds__(1024) pick_kernel(NJDev s) { pick_body(s); }
 
 // The join: record, modifyMatrix, active list.  One CTA; tv and ids are
 // shared-memory arrays of n0 entries.
@@ -522,25 +501,156 @@ __device__ void join_body(const NJDev& s, int step, int next, int m_n, float* tv
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(1024) join_kernel(NJDev s, int step, int next, int m_n) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  join_body(s, step, next, m_n, reinterpret_cast<float*>(smem_raw),
-            reinterpret_cast<int*>(smem_raw + sizeof(float) * s.n0));
+
+// ---- large n: full-GPU first pass, one CTA for the rest of the join --------
+// Per join: pass_min_kernel (one block per live row, every SM) writes the row
+// minima and the global minimum and magnitude; step_kernel (one CTA) scans only
+// the rows whose minimum is within the candidate threshold, picks the winner
+// and applies the join.  At the rebuild steps the matrix is compacted to its
+// live rows and columns, in slot order (so every slot comparison of the
+// record-order rounding is unchanged), after the row sums.
+
+__global__ void __launch_bounds__(1024) step_kernel(NJDev s, int step, int next, int m_n, int watermark) {
+  extern __shared__ __align__(16) unsigned char st_smem[];
+  float* tv = reinterpret_cast<float*>(st_smem);
+  int* ids = reinterpret_cast<int*>(tv + s.n0);
+  constexpr int kRows = 1024;
+  __shared__ int rows[kRows];
+  __shared__ int nrows;
+  const double nm2 = (double)(m_n - 2);
+  const float nm2f = (float)(m_n - 2);
+  const float qmin = iord(s.g32[0]);
+  const float mmax = iord(s.g32[1]);
+  const float thr = qmin + 3.f * (8.f * 5.9604645e-8f * mmax) + 1e-30f;
+  if (threadIdx.x == 0) nrows = 0;
+  __syncthreads();
+  // live slots whose row minimum is within the threshold (usually one or two)
+  for (int p = threadIdx.x; p < s.n0; p += blockDim.x) {
+    if (s.node[p] >= 0 && s.rmin[p] <= thr) {
+      const int t = atomicAdd(&nrows, 1);
+      if (t < kRows) rows[t] = p;
+    }
+  }
+  __syncthreads();
+  const bool all = nrows > kRows;   // more near-minimal rows than the list holds: every live row
+  const int nr = all ? s.n0 : nrows;
+  // each selected row scanned by the whole CTA
+  for (int t = 0; t < nr; ++t) {
+    const int r = all ? t : rows[t];
+    const int ur = s.node[r];
+    if (ur < 0 || s.rmin[r] > thr) continue;
+    const float tr = s.Tf[r];
+    const float* row = s.D + (size_t)r * s.n0;
+    for (int c = r + 1 + (int)threadIdx.x; c < s.n0; c += blockDim.x) {
+      const int uc = s.node[c];
+      if (uc < 0) continue;
+      const float d = row[c];
+      const float q = __fsub_rn(__fsub_rn(__fmul_rn(d, nm2f), tr), s.Tf[c]);
+      if (q > thr) continue;
+      const int a = min(ur, uc), b = max(ur, uc);
+      Cand cd;
+      cd.q1 = q_record(s, d, a, b, watermark, nm2);
+      cd.q2 = q_heap(s, d, a, b, nm2);
+      cd.a = a;
+      cd.b = b;
+      const int idx = atomicAdd(&s.g32[2], 1);
+      if (idx < s.cand_cap) s.cand[idx] = cd;
+    }
+  }
+  __syncthreads();
+  pick_body(s);
+  join_body(s, step, next, m_n, tv, ids);
 }
 
-// ---- one job per CTA (serving: many small jobs in one launch) --------------
+// Compaction, part 1 (one CTA): map[p] = new slot of live slot p (ascending),
+// T / Tf / node into the new slots, slot[v] of every live node remapped.
+__global__ void __launch_bounds__(1024) compact_map_kernel(NJDev s, int* map, double* T2, float* Tf2, int* node2,
+                                                           int nslots) {
+  __shared__ int wsum[33];
+  const int n0 = s.n0;
+  const int chunk = (n0 + blockDim.x - 1) / blockDim.x;
+  const int p0 = threadIdx.x * chunk;
+  int keep = 0;
+  for (int p = p0; p < p0 + chunk && p < n0; ++p) keep += s.node[p] >= 0;
+  int incl = keep;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if ((threadIdx.x & 31) >= o) incl += y;
+  }
+  if ((threadIdx.x & 31) == 31) wsum[threadIdx.x >> 5] = incl;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      const int t = wsum[w];
+      wsum[w] = acc;
+      acc += t;
+    }
+    wsum[32] = acc;
+  }
+  __syncthreads();
+  int q = wsum[threadIdx.x >> 5] + incl - keep;
+  for (int p = p0; p < p0 + chunk && p < n0; ++p) {
+    const int v = s.node[p];
+    if (v >= 0) {
+      map[p] = q;
+      T2[q] = s.T[p];
+      Tf2[q] = s.Tf[p];
+      node2[q] = v;
+      ++q;
+    } else {
+      map[p] = -1;
+    }
+  }
+  __syncthreads();
+  for (int v = threadIdx.x; v < nslots; v += blockDim.x) {
+    const int p = s.slot[v];
+    if (p >= 0) s.slot[v] = map[p];
+  }
+}
 
-constexpr int kCtaMaxN = 1024;
+// Compaction, part 2: D2[map[p]][map[c]] = D[p][c] for live p, c (one block per old row).
+__global__ void __launch_bounds__(256) compact_copy_kernel(NJDev s, const int* map, float* D2, int n2) {
+  const int p = blockIdx.x;
+  const int np = map[p];
+  if (np < 0) return;
+  const float* row = s.D + (size_t)p * s.n0;
+  float* out = D2 + (size_t)np * n2;
+  for (int c = threadIdx.x; c < s.n0; c += blockDim.x) {
+    const int nc = map[c];
+    if (nc >= 0) out[nc] = row[c];
+  }
+}
+
+// ---- one job per thread-block cluster (serving and small matrices) ----------
 
 struct NJJob {
   NJDev s;
   int n;
 };
 
-__device__ void cta_rowsums(const NJDev& s) {
+// Shared-memory copies of the float row sums and the slot -> node map.
+__device__ void cta_refresh(const NJDev& s, float* sTf, int* snode) {
+  for (int k = threadIdx.x; k < s.n0; k += blockDim.x) {
+    sTf[k] = s.Tf[k];
+    snode[k] = s.node[k];
+  }
+  __syncthreads();
+}
+
+// The join loop, schedule included (as the host loop of the large-n path),
+// with the O(n^2) passes split over the C CTAs
+// of a cluster (rows dealt to the cluster's warps round robin), the global
+// minimum and magnitude combined through distributed shared memory, and
+// hardware cluster barriers between the phases.  The pick and the join are
+// O(n) and run on rank 0; every rank keeps shared-memory copies of the float
+// row sums and the slot -> node map.  Dynamic shared memory: 5 arrays of the
+// largest n of the launch (tv, ids, sTf, snode, srmin).
+
+__device__ void clu_rowsums(const NJDev& s, int w0, int wstride) {
   const int na = *s.na;
   const int lane = threadIdx.x & 31;
-  for (int k = threadIdx.x >> 5; k < na; k += blockDim.x >> 5) {
+  for (int k = w0; k < na; k += wstride) {
     const int sk = s.slot[s.act[k]];
     const float* row = s.D + (size_t)sk * s.n0;
     double part = 0.0, ab = 0.0;
@@ -566,18 +676,17 @@ __device__ void cta_rowsums(const NJDev& s) {
       s.Tf[sk] = (float)sum;
     }
   }
-  __syncthreads();
 }
 
-// sTf / snode: shared-memory copies of s.Tf and s.node (refreshed after every
-// join); srmin: per slot, the smallest float q of the row (for the second pass)
-__device__ void cta_pass_min(const NJDev& s, float nm2f, const float* __restrict__ sTf,
-                             const int* __restrict__ snode, float* __restrict__ srmin) {
+// This CTA's rows: the smallest float q and the largest magnitude, reduced
+// over the block into part[0], part[1]; srmin[r] = the row's smallest q.
+__device__ void clu_pass_min(const NJDev& s, float nm2f, const float* __restrict__ sTf, const int* __restrict__ snode,
+                             float* __restrict__ srmin, int w0, int wstride, float* part) {
   __shared__ float sq[32], sm[32];
   const int na = *s.na;
   const int lane = threadIdx.x & 31;
   float qmin = FLT_MAX, mmax = 0.f;
-  for (int k = threadIdx.x >> 5; k < na; k += blockDim.x >> 5) {
+  for (int k = w0; k < na; k += wstride) {
     const int r = s.slot[s.act[k]];
     const float tr = sTf[r];
     const float* __restrict__ row = s.D + (size_t)r * s.n0;
@@ -598,7 +707,7 @@ __device__ void cta_pass_min(const NJDev& s, float nm2f, const float* __restrict
     if (lane == 0) srmin[r] = rq;
     qmin = fminf(qmin, rq);
   }
-  for (int o = 16; o > 0; o >>= 1) mmax = fmaxf(mmax, __shfl_down_sync(0xffffffffu, mmax, o));
+  for (int o = 16; o > 0; o >>= 1) mmax = fmaxf(mmax, __shfl_xor_sync(0xffffffffu, mmax, o));
   if (lane == 0) {
     sq[threadIdx.x >> 5] = qmin;
     sm[threadIdx.x >> 5] = mmax;
@@ -613,22 +722,18 @@ __device__ void cta_pass_min(const NJDev& s, float nm2f, const float* __restrict
       mmax = fmaxf(mmax, __shfl_xor_sync(0xffffffffu, mmax, o));
     }
     if (lane == 0) {
-      s.g32[0] = ford(qmin);
-      s.g32[1] = ford(mmax);
-      s.g32[2] = 0;
+      part[0] = qmin;
+      part[1] = mmax;
     }
   }
-  __syncthreads();
 }
 
-__device__ void cta_pass_cand(const NJDev& s, float nm2f, double nm2, int watermark, const float* __restrict__ sTf,
-                              const int* __restrict__ snode, const float* __restrict__ srmin) {
+__device__ void clu_pass_cand(const NJDev& s, float nm2f, double nm2, int watermark, float thr,
+                              const float* __restrict__ sTf, const int* __restrict__ snode,
+                              const float* __restrict__ srmin, int w0, int wstride) {
   const int na = *s.na;
   const int lane = threadIdx.x & 31;
-  const float qmin = iord(s.g32[0]);
-  const float mmax = iord(s.g32[1]);
-  const float thr = qmin + 3.f * (8.f * 5.9604645e-8f * mmax) + 1e-30f;
-  for (int k = threadIdx.x >> 5; k < na; k += blockDim.x >> 5) {
+  for (int k = w0; k < na; k += wstride) {
     const int ur = s.act[k];
     const int r = s.slot[ur];
     if (srmin[r] > thr) continue;   // no pair of this row is a candidate
@@ -651,42 +756,45 @@ __device__ void cta_pass_cand(const NJDev& s, float nm2f, double nm2, int waterm
       if (idx < s.cand_cap) s.cand[idx] = cd;
     }
   }
-  __syncthreads();
 }
 
-// Shared-memory copies of the float row sums and the slot -> node map.
-__device__ void cta_refresh(const NJDev& s, float* sTf, int* snode) {
-  for (int k = threadIdx.x; k < s.n0; k += blockDim.x) {
-    sTf[k] = s.Tf[k];
-    snode[k] = s.node[k];
-  }
-  __syncthreads();
-}
-
-// The whole join loop of one job, schedule included (same as the host loop of
-// Ctx::nj).  Workspace pointers of every job are set by the host.
-__global__ void __launch_bounds__(1024) nj_cta_kernel(const NJJob* jobs, int njobs) {
-  __shared__ float tv[kCtaMaxN];
-  __shared__ int ids[kCtaMaxN];
-  __shared__ float sTf[kCtaMaxN];
-  __shared__ int snode[kCtaMaxN];
-  __shared__ float srmin[kCtaMaxN];
-  if ((int)blockIdx.x >= njobs) return;
-  const NJJob J = jobs[blockIdx.x];
+template <int C>
+__global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_cluster_kernel(const NJJob* jobs, int njobs,
+                                                                                     int nmax) {
+  namespace cg = cooperative_groups;
+  extern __shared__ __align__(16) unsigned char nj_smem[];
+  float* tv = reinterpret_cast<float*>(nj_smem);
+  int* ids = reinterpret_cast<int*>(tv + nmax);
+  float* sTf = reinterpret_cast<float*>(ids + nmax);
+  int* snode = reinterpret_cast<int*>(sTf + nmax);
+  float* srmin = reinterpret_cast<float*>(snode + nmax);
+  __shared__ float part[2];   // this CTA's pass-1 partial (read by the other ranks)
+  __shared__ float glob[2];   // the cluster's minimum and magnitude
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank();
+  const int job = (int)blockIdx.x / C;           // the same for every CTA of the cluster
+  if (job >= njobs) return;
+  const NJJob J = jobs[job];
   const NJDev& s = J.s;
   const int n = J.n;
-  for (int k = threadIdx.x; k < 2 * n - 1; k += blockDim.x) s.slot[k] = k < n ? k : -1;
-  for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    s.node[k] = k;
-    s.act[k] = k;
+  const int w0 = rank * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5);
+  const int wstride = C * (int)(blockDim.x >> 5);
+  if (rank == 0) {
+    for (int k = threadIdx.x; k < 2 * n - 1; k += blockDim.x) s.slot[k] = k < n ? k : -1;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+      s.node[k] = k;
+      s.act[k] = k;
+    }
+    if (threadIdx.x == 0) {
+      *s.na = n;
+      s.g32[2] = 0;
+      s.stats[0] = s.stats[1] = s.stats[2] = s.stats[3] = s.stats[4] = 0;
+    }
   }
-  if (threadIdx.x == 0) {
-    *s.na = n;
-    s.stats[0] = s.stats[1] = s.stats[2] = s.stats[3] = s.stats[4] = 0;
-  }
-  __syncthreads();
+  cl.sync();
   if (n < 2) return;
-  cta_rowsums(s);
+  clu_rowsums(s, w0, wstride);
+  cl.sync();
   cta_refresh(s, sTf, snode);
   const int kBinT = 30 * 31 / 2;
   int steps = max((int)((float)n * 0.5f), 200);
@@ -696,40 +804,82 @@ __global__ void __launch_bounds__(1024) nj_cta_kernel(const NJJob* jobs, int njo
   int watermark = n, next = n, m_n = n, na = n;
   for (int step = 0; step < n - 1; ++step) {
     const double nm2 = (double)(m_n - 2);
-    cta_pass_min(s, (float)(m_n - 2), sTf, snode, srmin);
-    cta_pass_cand(s, (float)(m_n - 2), nm2, watermark, sTf, snode, srmin);
-    pick_body(s);
-    join_body(s, step, next, m_n, tv, ids);
+    const float nm2f = (float)(m_n - 2);
+    clu_pass_min(s, nm2f, sTf, snode, srmin, w0, wstride, part);
+    cl.sync();
+    if (threadIdx.x < 32) {
+      const int l = threadIdx.x;
+      float q = FLT_MAX, m = 0.f;
+      if (l < C) {
+        const float* rp = cl.map_shared_rank(part, l);
+        q = rp[0];
+        m = rp[1];
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        q = fminf(q, __shfl_xor_sync(0xffffffffu, q, o));
+        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+      }
+      if (l == 0) {
+        glob[0] = q;
+        glob[1] = m;
+      }
+    }
+    __syncthreads();
+    const float thr = glob[0] + 3.f * (8.f * 5.9604645e-8f * glob[1]) + 1e-30f;
+    clu_pass_cand(s, nm2f, nm2, watermark, thr, sTf, snode, srmin, w0, wstride);
+    cl.sync();
+    if (rank == 0) {
+      pick_body(s);
+      join_body(s, step, next, m_n, tv, ids);
+    }
     if (--pq_ck == 0) {
       pq_ck = 500;
-      if (steps > 0 && (double)(ub / kBinT) / (double)ave0 > 2.0 && threadIdx.x == 0) s.stats[3] += 1;
+      if (steps > 0 && (double)(ub / kBinT) / (double)ave0 > 2.0 && rank == 0 && threadIdx.x == 0) s.stats[3] += 1;
     }
     --m_n;
     na -= 1;
     ++next;
+    cl.sync();
     if (steps == 0) {
-      cta_rowsums(s);
-      if (threadIdx.x == 0) s.stats[4] += 1;
+      clu_rowsums(s, w0, wstride);
+      if (rank == 0 && threadIdx.x == 0) s.stats[4] += 1;
       watermark = next;
       steps = (m_n < 200) ? INT_MAX : (int)((float)m_n * 0.5f);
       ave0 = (((long long)(m_n - 1) * m_n) / 2) / kBinT;
       ub = ((long long)m_n * (m_n - 1)) / 2;
+      cl.sync();
     } else {
       --steps;
       ub += na - 1;
     }
     cta_refresh(s, sTf, snode);
   }
+  cl.sync();   // no rank leaves while another may still read its shared memory
 }
 
 }  // namespace
 
 struct NJState {
   DevBuf D, T, Tf, slot, node, act, na, g32, cand, win, stats, joins, vd, rmin;
+  DevBuf D2, T2, Tf2, node2, map, desc;   // large-n path: the other half of the compaction buffers
   ~NJState() {
-    for (DevBuf* b : {&D, &T, &Tf, &slot, &node, &act, &na, &g32, &cand, &win, &stats, &joins, &vd, &rmin}) b->release();
+    for (DevBuf* b : {&D, &T, &Tf, &slot, &node, &act, &na, &g32, &cand, &win, &stats, &joins, &vd, &rmin, &D2, &T2,
+                      &Tf2, &node2, &map, &desc})
+      b->release();
   }
 };
+
+// Up to this many taxa one cluster runs the whole join loop (the matrix stays
+// in L2); larger matrices take the full-GPU first pass per join.  The
+// environment variable NWG_NJ_CLUSTER_MAX_N overrides the threshold (both
+// paths give the same joins; the tests run each path on the same inputs).
+int cluster_nj_max_n() {
+  static const int v = [] {
+    const char* e = std::getenv("NWG_NJ_CLUSTER_MAX_N");
+    return e ? std::atoi(e) : 2048;
+  }();
+  return v;
+}
 
 void Ctx::nj_release() {
   delete reinterpret_cast<NJState*>(nj_state);
@@ -748,6 +898,7 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
   if (!nj_state) nj_state = new NJState();
   NJState& S = *reinterpret_cast<NJState*>(nj_state);
   const int nn = 2 * n - 1;
+  const bool big = n > cluster_nj_max_n();
   int rc;
   if ((rc = S.D.ensure(sizeof(float) * (size_t)n * n)) || (rc = S.T.ensure(sizeof(double) * n)) ||
       (rc = S.Tf.ensure(sizeof(float) * n)) || (rc = S.slot.ensure(sizeof(int) * nn)) ||
@@ -756,25 +907,17 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
       (rc = S.cand.ensure(sizeof(Cand) * kCandCap)) || (rc = S.win.ensure(sizeof(Pick))) ||
       (rc = S.stats.ensure(sizeof(unsigned long long) * 5)) ||
       (rc = S.joins.ensure(sizeof(nwg_join) * (n - 1))) || (rc = S.vd.ensure(sizeof(float) * n)) ||
-      (rc = S.rmin.ensure(sizeof(float) * n)))
+      (rc = S.rmin.ensure(sizeof(float) * n)) || (rc = S.desc.ensure(sizeof(NJJob))))
+    return fail(rc, "nj allocation");
+  if (big && ((rc = S.D2.ensure(sizeof(float) * (size_t)n * n)) || (rc = S.T2.ensure(sizeof(double) * n)) ||
+              (rc = S.Tf2.ensure(sizeof(float) * n)) || (rc = S.node2.ensure(sizeof(int) * n)) ||
+              (rc = S.map.ensure(sizeof(int) * n))))
     return fail(rc, "nj allocation");
   cudaStream_t s = stream;
   const cudaMemcpyKind kind = device_D ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   if ((rc = cuda(cudaMemcpy2DAsync(S.D.p, sizeof(float) * n, D, sizeof(float) * ld, sizeof(float) * n, n, kind, s),
                  "nj upload")))
     return rc;
-  std::vector<int> slot0(nn, -1), act0(n + 1, 0), node0(n);
-  for (int k = 0; k < n; ++k) slot0[k] = k, act0[k] = k, node0[k] = k;
-  const int na0 = n;
-  const int g0[4] = {0x7F7FFFFF, 0, 0, 0};
-  if ((rc = cuda(cudaMemcpyAsync(S.slot.p, slot0.data(), sizeof(int) * nn, cudaMemcpyHostToDevice, s), "nj upload")) ||
-      (rc = cuda(cudaMemcpyAsync(S.node.p, node0.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s), "nj upload")) ||
-      (rc = cuda(cudaMemcpyAsync(S.act.p, act0.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s), "nj upload")) ||
-      (rc = cuda(cudaMemcpyAsync(S.na.p, &na0, sizeof(int), cudaMemcpyHostToDevice, s), "nj upload")) ||
-      (rc = cuda(cudaMemcpyAsync(S.g32.p, g0, sizeof(g0), cudaMemcpyHostToDevice, s), "nj upload")) ||
-      (rc = cuda(cudaMemsetAsync(S.stats.p, 0, sizeof(unsigned long long) * 5, s), "nj upload")))
-    return rc;
-  if ((rc = cuda(cudaStreamSynchronize(s), "nj upload"))) return rc;   // host vectors above are local
   NJDev d{};
   d.D = (float*)S.D.p;
   d.T = (double*)S.T.p;
@@ -792,52 +935,85 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
   d.rmin = (float*)S.rmin.p;
   d.n0 = n;
   d.cand_cap = kCandCap;
-  const size_t join_smem = 2 * sizeof(float) * (size_t)n;
-  if ((rc = cuda(cudaFuncSetAttribute(join_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)join_smem),
-                 "nj smem")))
-    return rc;
-  if (st) cudaEventRecord(ev0, s);
-  rowsum_kernel<<<(n + 7) / 8, 256, 0, s>>>(d);
-  ++launches;
-  // host-side schedule (deterministic in n, as the reference's)
-  const int kBinT = 30 * 31 / 2;
-  int steps = std::max((int)((float)n * 0.5f), 200);
-  int pq_ck = 500;
-  long long ave0 = (((long long)(n - 1) * n) / 2) / kBinT;
-  long long ub = ((long long)n * (n - 1)) / 2;
-  int watermark = n, next = n, m_n = n, na = n;
-  for (int step = 0; step < n - 1; ++step) {
-    const double nm2 = (double)(m_n - 2);
-    pass_min_kernel<<<na, 256, 0, s>>>(d, (float)(m_n - 2));
-    pass_cand_kernel<<<na, 256, 0, s>>>(d, (float)(m_n - 2), nm2, watermark);
-    pick_kernel<<<1, 1024, 0, s>>>(d);
-    join_kernel<<<1, 1024, join_smem, s>>>(d, step, next, m_n);
-    launches += 4;
-    if (--pq_ck == 0) {
-      pq_ck = 500;
-      if (steps > 0) {
-        const double r = (double)(ub / kBinT) / (double)ave0;
-        if (r > 2.0) ++stats.pq_trigger_open;
+  if (!big) {
+    NJJob J{};
+    J.s = d;
+    J.n = n;
+    // the descriptor travels in the stream (a pageable copy is staged at once)
+    if ((rc = cuda(cudaMemcpyAsync(S.desc.p, &J, sizeof(J), cudaMemcpyHostToDevice, s), "nj upload"))) return rc;
+    if (st) cudaEventRecord(ev0, s);
+    if ((rc = cuda(launch_nj_cluster(S.desc.p, 1, n, nj_cluster_size(), s), "nj launch"))) return rc;
+    ++launches;
+  } else {
+    std::vector<int> slot0(nn, -1), act0(n + 1, 0);
+    for (int k = 0; k < n; ++k) slot0[k] = k, act0[k] = k;
+    const int na0 = n;
+    const int g0[4] = {0x7F7FFFFF, 0, 0, 0};
+    if ((rc = cuda(cudaMemcpyAsync(S.slot.p, slot0.data(), sizeof(int) * nn, cudaMemcpyHostToDevice, s), "nj upload")) ||
+        (rc = cuda(cudaMemcpyAsync(S.node.p, act0.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s), "nj upload")) ||
+        (rc = cuda(cudaMemcpyAsync(S.act.p, act0.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s), "nj upload")) ||
+        (rc = cuda(cudaMemcpyAsync(S.na.p, &na0, sizeof(int), cudaMemcpyHostToDevice, s), "nj upload")) ||
+        (rc = cuda(cudaMemcpyAsync(S.g32.p, g0, sizeof(g0), cudaMemcpyHostToDevice, s), "nj upload")) ||
+        (rc = cuda(cudaMemsetAsync(S.stats.p, 0, sizeof(unsigned long long) * 5, s), "nj upload")) ||
+        (rc = cuda(cudaStreamSynchronize(s), "nj upload")))   // the host vectors above are local
+      return rc;
+    const size_t step_smem = 2 * sizeof(float) * (size_t)n;
+    if ((rc = cuda(cudaFuncSetAttribute(step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)step_smem),
+                   "nj smem")))
+      return rc;
+    float* Dalt = (float*)S.D2.p;
+    double* Talt = (double*)S.T2.p;
+    float* Tfalt = (float*)S.Tf2.p;
+    int* nodealt = (int*)S.node2.p;
+    if (st) cudaEventRecord(ev0, s);
+    rowsum_kernel<<<(n + 7) / 8, 256, 0, s>>>(d);
+    ++launches;
+    // host-side schedule (deterministic in n, as the reference's)
+    const int kBinT = 30 * 31 / 2;
+    int steps = std::max((int)((float)n * 0.5f), 200);
+    int pq_ck = 500;
+    long long ave0 = (((long long)(n - 1) * n) / 2) / kBinT;
+    long long ub = ((long long)n * (n - 1)) / 2;
+    int watermark = n, next = n, m_n = n, na = n;
+    for (int step = 0; step < n - 1; ++step) {
+      pass_min_kernel<<<na, 256, 0, s>>>(d, (float)(m_n - 2));
+      step_kernel<<<1, 1024, step_smem, s>>>(d, step, next, m_n, watermark);
+      launches += 2;
+      if (--pq_ck == 0) {
+        pq_ck = 500;
+        if (steps > 0) {
+          const double r = (double)(ub / kBinT) / (double)ave0;
+          if (r > 2.0) ++stats.pq_trigger_open;
+        }
       }
+      --m_n;
+      na -= 1;
+      ++next;
+      if (steps == 0) {
+        rowsum_kernel<<<(na + 7) / 8, 256, 0, s>>>(d);
+        // compaction to the live slots, in slot order
+        compact_map_kernel<<<1, 1024, 0, s>>>(d, (int*)S.map.p, Talt, Tfalt, nodealt, nn);
+        compact_copy_kernel<<<d.n0, 256, 0, s>>>(d, (const int*)S.map.p, Dalt, na);
+        launches += 3;
+        std::swap(d.D, Dalt);
+        std::swap(d.T, Talt);
+        std::swap(d.Tf, Tfalt);
+        std::swap(d.node, nodealt);
+        d.n0 = na;
+        ++stats.rebuilds;
+        watermark = next;
+        steps = (m_n < 200) ? INT_MAX : (int)((float)m_n * 0.5f);
+        ave0 = (((long long)(m_n - 1) * m_n) / 2) / kBinT;
+        ub = ((long long)m_n * (m_n - 1)) / 2;
+      } else {
+        --steps;
+        ub += na - 1;
+      }
+      if ((rc = cuda(cudaGetLastError(), "nj launch"))) return rc;
     }
-    --m_n;
-    na -= 1;
-    ++next;
-    if (steps == 0) {
-      rowsum_kernel<<<(na + 7) / 8, 256, 0, s>>>(d);
-      ++launches;
-      ++stats.rebuilds;
-      watermark = next;
-      steps = (m_n < 200) ? INT_MAX : (int)((float)m_n * 0.5f);
-      ave0 = (((long long)(m_n - 1) * m_n) / 2) / kBinT;
-      ub = ((long long)m_n * (m_n - 1)) / 2;
-    } else {
-      --steps;
-      ub += na - 1;
-    }
-    if ((rc = cuda(cudaGetLastError(), "nj launch"))) return rc;
   }
-  unsigned long long dst[3] = {0, 0, 0};
+  if (st) cudaEventRecord(ev1, s);
+  unsigned long long dst[5] = {0, 0, 0, 0, 0};
   if ((rc = cuda(cudaMemcpyAsync(joins, S.joins.p, sizeof(nwg_join) * (n - 1), cudaMemcpyDeviceToHost, s), "nj download")) ||
       (rc = cuda(cudaMemcpyAsync(dst, S.stats.p, sizeof(dst), cudaMemcpyDeviceToHost, s), "nj download")) ||
       (rc = cuda(cudaStreamSynchronize(s), "nj sync")))
@@ -845,9 +1021,11 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
   if (dst[2]) return fail(NWG_ERR_CUDA, "neighbor joining candidate list empty or overflowing");
   stats.ambiguous_steps = (int64_t)dst[0];
   stats.tie_steps = (int64_t)dst[1];
+  if (!big) {
+    stats.pq_trigger_open = (int64_t)dst[3];
+    stats.rebuilds = (int64_t)dst[4];
+  }
   if (st) {
-    cudaEventRecord(ev1, s);
-    cudaEventSynchronize(ev1);
     float ms = 0;
     cudaEventElapsedTime(&ms, ev0, ev1);
     stats.device_ms = ms;
@@ -899,12 +1077,56 @@ void nj_job_setup(void* job_out, float* D, int n, char* base, nwg_join** joins, 
 }
 
 size_t nj_job_desc_bytes() { return sizeof(NJJob); }
-int nj_cta_max_n() { return kCtaMaxN; }
 
-cudaError_t launch_nj_jobs(const void* d_jobs, int njobs, cudaStream_t s) {
+// One job per cluster of C CTAs (C = 1, 8 or 16); nmax: the largest n of the
+// jobs (dynamic shared memory of 5 arrays of nmax 4-byte words).
+cudaError_t launch_nj_cluster(const void* d_jobs, int njobs, int nmax, int C, cudaStream_t s) {
   if (njobs <= 0) return cudaSuccess;
-  nj_cta_kernel<<<njobs, 1024, 0, s>>>(reinterpret_cast<const NJJob*>(d_jobs), njobs);
-  return cudaGetLastError();
+  const size_t smem = (size_t)5 * sizeof(float) * (size_t)std::max(nmax, 1);
+  const NJJob* jobs = reinterpret_cast<const NJJob*>(d_jobs);
+  auto go = [&](auto kern, int c) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    if (c > 8 && (e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1)) != cudaSuccess)
+      return e;
+    kern<<<njobs * c, 1024, smem, s>>>(jobs, njobs, nmax);
+    return cudaGetLastError();
+  };
+  if (C == 16) return go(nj_cluster_kernel<16>, 16);
+  if (C == 8) return go(nj_cluster_kernel<8>, 8);
+  return go(nj_cluster_kernel<1>, 1);
+}
+
+// The largest cluster (16, else 8) that the device schedules with the join
+// loop's shared memory for the largest supported n.
+int nj_cluster_size() {
+  static int best = 0;
+  if (best) return best;
+  const size_t smem = (size_t)5 * sizeof(float) * kNJMaxN;
+  best = 8;
+  for (int c : {16, 8}) {
+    const void* fn = c == 16 ? (const void*)nj_cluster_kernel<16> : (const void*)nj_cluster_kernel<8>;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) continue;
+    if (c > 8 && cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) continue;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(c);
+    cfg.blockDim = dim3(1024);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute at;
+    at.id = cudaLaunchAttributeClusterDimension;
+    at.val.clusterDim.x = c;
+    at.val.clusterDim.y = 1;
+    at.val.clusterDim.z = 1;
+    cfg.attrs = &at;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, fn, &cfg) == cudaSuccess && clusters > 0) {
+      best = c;
+      break;
+    }
+  }
+  cudaGetLastError();
+  return best;
 }
 
 }  // namespace nwg

@@ -151,12 +151,13 @@ bool wave_exists(int R, int P, int V, int W);
 inline int wave_x_per_front(int V) { return V == 5 ? 2 : 1; }
 cudaError_t launch_plain(const PlainArgs& a, cudaStream_t s);
 cudaError_t launch_rerun(const WaveArgs& a, int2* scratch, int64_t nthreads, cudaStream_t s);
-// per-CTA neighbor joining for many small jobs (nj.cu)
+// neighbor joining of many jobs in one launch, one thread-block cluster per job (nj.cu)
 size_t nj_job_workspace(int n);
 void nj_job_setup(void* job_out, float* D, int n, char* base, nwg_join** joins, unsigned long long** stats);
 size_t nj_job_desc_bytes();
-int nj_cta_max_n();
-cudaError_t launch_nj_jobs(const void* d_jobs, int njobs, cudaStream_t s);
+cudaError_t launch_nj_cluster(const void* d_jobs, int njobs, int nmax, int C, cudaStream_t s);
+int nj_cluster_size();
+constexpr int kServeMaxN = 8192;   // largest job of the serving loop (neighbor joining on the device)
 cudaError_t launch_dpx_peak(int P, int form, int cols, int grid, uint32_t* sink, int go, int ge, cudaStream_t s);
 int dpx_peak_ctas_per_sm(int P, int form);
 cudaError_t launch_pairlist(const PairListArgs& a, int64_t count, cudaStream_t s);

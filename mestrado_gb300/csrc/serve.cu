@@ -34,6 +34,10 @@ namespace nwg {
 
 namespace {
 
+// CTAs per job in the join-loop launch: the O(n^2) passes of one join split
+// over 8 SMs (jobs of one batch run side by side).
+constexpr int kNJClusterServe = 8;
+
 double clock_ms() {
   using clk = std::chrono::steady_clock;
   return std::chrono::duration<double, std::milli>(clk::now().time_since_epoch()).count();
@@ -306,15 +310,10 @@ int Server::launch_batch(Slot& S) {
   }
   if ((rc = c.cuda(cudaMemcpyAsync(S.h_D.p, S.D.p, sizeof(float) * total_D, cudaMemcpyDeviceToHost, st), "serve")))
     return rc;
-  // join loops: small jobs one CTA each, larger ones through the context path
-  std::vector<int> small;
-  for (int k = 0; k < nj; ++k)
-    if (S.batch[k]->n <= nj_cta_max_n()) small.push_back(k);
-  if ((int)small.size() == nj) {
-    if ((rc = c.cuda(launch_nj_jobs(S.njdesc.p, nj, st), "serve nj launch"))) return rc;
-  } else {
-    return NWG_ERR_INVALID;   // submit() rejects such jobs
-  }
+  // join loops: one cluster of kNJClusterServe CTAs per job, all jobs in one launch
+  int nmax = 1;
+  for (ServeJob* J : S.batch) nmax = std::max(nmax, J->n);
+  if ((rc = c.cuda(launch_nj_cluster(S.njdesc.p, nj, nmax, kNJClusterServe, st), "serve nj launch"))) return rc;
   char* hj = (char*)S.h_joins.p;
   size_t jo = 0;
   for (int k = 0; k < nj; ++k) {
@@ -452,7 +451,7 @@ int nwg_server_create(int gap_open, int gap_ext, int64_t hbm_budget_bytes, int m
 int nwg_server_submit(nwg_server* srv, const char* ascii, const int64_t* offsets, int n, uint64_t* job_id) {
   if (!srv || !ascii || !offsets || n < 1 || !job_id) return NWG_ERR_INVALID;
   Server* s = reinterpret_cast<Server*>(srv);
-  if (n > nwg::nj_cta_max_n()) return NWG_ERR_INVALID;
+  if (n > nwg::kServeMaxN) return NWG_ERR_INVALID;
   auto* J = new nwg::ServeJob();
   J->n = n;
   J->off.assign(offsets, offsets + n + 1);

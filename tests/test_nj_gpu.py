@@ -70,3 +70,29 @@ def test_device_nj_ties_and_duplicates(ctx):
     for a, b in zip(joins, oj):
         assert (a["i"], a["j"], a["len_i"], a["len_j"]) == (b["i"], b["j"], b["len_i"], b["len_j"])
     assert st["ambiguous_steps"] == ost["ambiguous_steps"]
+
+
+@pytest.mark.parametrize("path", ["cluster", "full_gpu"])
+def test_both_nj_paths_match_oracle(path):
+    # the large-matrix path (full-GPU first pass, compaction at the rebuild
+    # steps) and the one-cluster path give the oracle's joins; run in a child
+    # process so that the path threshold applies from the library's first use
+    import subprocess
+    import sys
+    env = dict(os.environ, NWG_NJ_CLUSTER_MAX_N="0" if path == "full_gpu" else "100000")
+    code = (
+        "import sys, numpy as np; sys.path.insert(0, 'tests'); import oracle_py as O\n"
+        "from mestrado_gb300 import Context, synth\n"
+        "c = Context(10, 2)\n"
+        "for seed, n in ((11, 450), (12, 640)):\n"
+        "    D = c.score_all(synth.family(n, 90, ps=0.1, pi=0.01, seed=seed))\n"
+        "    j, st = c.nj(D, stats=True)\n"
+        "    oj, ost = O.nj(D)\n"
+        "    assert st['rebuilds'] == ost['rebuilds'] and st['tie_steps'] == ost['tie_steps']\n"
+        "    for a, b in zip(j, oj):\n"
+        "        assert (a['i'], a['j'], a['node'], a['len_i'], a['len_j'], a['q']) == "
+        "(b['i'], b['j'], b['node'], b['len_i'], b['len_j'], b['q'])\n"
+        "print('ok')\n")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", code], cwd=root, env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and r.stdout.strip().endswith("ok"), r.stdout + r.stderr

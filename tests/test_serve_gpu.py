@@ -110,7 +110,7 @@ def test_serving_concurrent_submitters(ctx):
 def test_serving_rejects():
     with Server(hbm_budget=1 << 20) as srv:
         with pytest.raises(NWGError) as e:
-            srv.submit(synth.family(1100, 20, seed=1))
+            srv.submit(synth.family(8200, 5, seed=1))
         assert e.value.status == NWG_ERR_INVALID
         with pytest.raises(NWGError) as e:
             srv.submit(synth.family(600, 20, seed=1))   # 1.4 MB matrix > 1 MB budget
