@@ -84,6 +84,20 @@ int nwg_parse_wire(const char* wire, int n, int8_t* codes, int64_t* offsets);
 /* Encode and reverse n ASCII sequences laid end to end (offsets[n+1]). */
 int nwg_encode(const char* ascii, const int64_t* offsets, int n, int8_t* codes);
 
+/* The same on the device: d_ascii and d_codes are device buffers, offsets a
+ * host array.  Bytes outside the alphabet become -1 as in the reference's
+ * table; their count goes to *bad_count (may be NULL) and the call returns
+ * NWG_ERR_BAD_RESIDUE.  Synchronizes the context stream. */
+int nwg_encode_dev(nwg_ctx* ctx, const char* d_ascii, const int64_t* offsets, int n, int8_t* d_codes,
+                   int64_t* bad_count);
+
+/* nwg_parse_wire with the residues encoded on the device: the headers are
+ * read from the host copy `wire`, the residues from `d_wire`, a device copy of
+ * the same block; offsets (n+1, host) are filled; d_codes may be NULL (offsets
+ * only). */
+int nwg_parse_wire_dev(nwg_ctx* ctx, const char* wire, const char* d_wire, int n, int8_t* d_codes,
+                       int64_t* offsets, int64_t* bad_count);
+
 /* ---- all-pairs distance matrix ----------------------------------------- */
 
 /* Replaces AlignmentScore::loadDB + computeDistanceMtx on one rank
@@ -310,7 +324,10 @@ typedef struct {
 
 int nwg_server_create(int gap_open, int gap_ext, int64_t hbm_budget_bytes, int max_batch_jobs,
                       nwg_server** out);
-/* Copies the job's sequences (ASCII, offsets[0..n]); returns at once. */
+/* Copies the job's sequences (ASCII, offsets[0..n]; empty sequences are
+ * refused here) and returns at once; the residues are encoded on the device
+ * with the batch, so a byte outside the alphabet makes the job's status
+ * NWG_ERR_BAD_RESIDUE at nwg_server_wait. */
 int nwg_server_submit(nwg_server* srv, const char* ascii, const int64_t* offsets, int n, uint64_t* job_id);
 /* Waits up to timeout_ms (< 0: no limit; NWG_ERR_TIMEOUT when it runs out, the
  * job stays queryable) for the job, copies its n*n matrix to D and its n-1

@@ -8,7 +8,8 @@
 // footprint (n^2 matrix, NJ workspace, codes) fits the budget left by the jobs
 // in flight.  A batch is queued on one of two pipeline slots (own stream,
 // device arenas, pinned staging):
-//   codes in -> one multi-job plan: every job's Y groups in shared
+//   residues in (ASCII; encoded and reversed on the device) -> one
+//   multi-job plan: every job's Y groups in shared
 //   length buckets, so one persistent launch per bucket interleaves pairs of
 //   different jobs -> matrices out -> one launch of the per-CTA join loop
 //   (one CTA per job) -> join lists out.
@@ -69,7 +70,7 @@ struct HostBuf {
 struct ServeJob {
   uint64_t id = 0;
   int n = 0;
-  std::vector<int8_t> codes;
+  std::vector<char> ascii;    // the job's residues as submitted (encoded on the device)
   std::vector<int64_t> off;
   size_t footprint = 0;
   double t_submit = 0, t_admit = 0, t_done = 0;
@@ -80,19 +81,20 @@ struct ServeJob {
   std::vector<nwg_join> joins;
   unsigned long long njst[5] = {0, 0, 0, 0, 0};
   // placement in its batch
-  size_t d_off = 0, nj_off = 0, codes_off = 0, desc_idx = 0;
+  size_t d_off = 0, nj_off = 0, codes_off = 0, desc_idx = 0, seq_base = 0;
 };
 
 struct Slot {
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
-  DevBuf codes, start, len, orig, gy, gy2, gx, gxb, gdofs, gld, jobsbuf, counters, scratch, D, njws, njdesc;
+  DevBuf ascii, codes, bad, start, len, orig, gy, gy2, gx, gxb, gdofs, gld, jobsbuf, counters, scratch, D, njws, njdesc;
   HostBuf h_codes, h_plan, h_D, h_joins;
   std::vector<ServeJob*> batch;
   bool busy = false;
   size_t plan_bytes = 0;
   ~Slot() {
-    for (DevBuf* b : {&codes, &start, &len, &orig, &gy, &gy2, &gx, &gxb, &gdofs, &gld, &jobsbuf, &counters, &scratch,
+    for (DevBuf* b : {&ascii, &codes, &bad, &start, &len, &orig, &gy, &gy2, &gx, &gxb, &gdofs, &gld, &jobsbuf, &counters,
+                      &scratch,
                       &D, &njws, &njdesc})
       b->release();
     if (done) cudaEventDestroy(done);
@@ -133,7 +135,8 @@ int Server::launch_batch(Slot& S) {
   int64_t total_codes = 0, total_seqs = 0, total_D = 0, total_ws = 0;
   for (ServeJob* J : S.batch) {
     J->codes_off = (size_t)total_codes;
-    total_codes += (int64_t)J->codes.size();
+    J->seq_base = (size_t)total_seqs;
+    total_codes += (int64_t)J->ascii.size();
     total_seqs += J->n;
     J->d_off = (size_t)total_D;
     total_D += (int64_t)J->n * J->n;
@@ -219,6 +222,7 @@ int Server::launch_batch(Slot& S) {
   int rc;
   const size_t desc = nj_job_desc_bytes();
   if ((rc = S.codes.ensure((size_t)std::max<int64_t>(total_codes, 1))) ||
+      (rc = S.ascii.ensure((size_t)std::max<int64_t>(total_codes, 1))) || (rc = S.bad.ensure(sizeof(int) * total_seqs)) ||
       (rc = S.start.ensure(sizeof(int64_t) * total_seqs)) || (rc = S.len.ensure(sizeof(int32_t) * total_seqs)) ||
       (rc = S.orig.ensure(sizeof(int32_t) * total_seqs)) || (rc = S.gy.ensure(sizeof(int32_t) * ng)) ||
       (rc = S.gy2.ensure(sizeof(int32_t) * ng)) || (rc = S.gx.ensure(sizeof(int32_t) * ng)) ||
@@ -259,17 +263,18 @@ int Server::launch_batch(Slot& S) {
   for (auto& pc : pieces) staged += (pc.bytes + 15) / 16 * 16;
   if ((rc = S.h_codes.ensure((size_t)std::max<int64_t>(total_codes, 1))) || (rc = S.h_plan.ensure(staged)) ||
       (rc = S.h_D.ensure(sizeof(float) * total_D)) ||
-      (rc = S.h_joins.ensure((sizeof(nwg_join) * (size_t)total_seqs) + sizeof(unsigned long long) * 5 * nj)))
+      (rc = S.h_joins.ensure((sizeof(nwg_join) * (size_t)total_seqs) + sizeof(unsigned long long) * 5 * nj +
+                             sizeof(int) * total_seqs)))
     return rc;
   for (ServeJob* J : S.batch)
-    std::memcpy((char*)S.h_codes.p + J->codes_off, J->codes.data(), J->codes.size());
+    std::memcpy((char*)S.h_codes.p + J->codes_off, J->ascii.data(), J->ascii.size());
   size_t o = 0;
   for (auto& pc : pieces) {
     std::memcpy((char*)S.h_plan.p + o, pc.src, pc.bytes);
     o += (pc.bytes + 15) / 16 * 16;
   }
   cudaStream_t st = S.stream;
-  if ((rc = c.cuda(cudaMemcpyAsync(S.codes.p, S.h_codes.p, (size_t)total_codes, cudaMemcpyHostToDevice, st), "serve")))
+  if ((rc = c.cuda(cudaMemcpyAsync(S.ascii.p, S.h_codes.p, (size_t)total_codes, cudaMemcpyHostToDevice, st), "serve")))
     return rc;
   o = 0;
   for (auto& pc : pieces) {
@@ -277,6 +282,11 @@ int Server::launch_batch(Slot& S) {
       return rc;
     o += (pc.bytes + 15) / 16 * 16;
   }
+  // codes: every sequence encoded and reversed in place of its ASCII (same offsets)
+  if ((rc = c.cuda(launch_encode((const char*)S.ascii.p, (const int64_t*)S.start.p, (const int64_t*)S.start.p,
+                                 (const int32_t*)S.len.p, (int)total_seqs, (int8_t*)S.codes.p, (int*)S.bad.p, st),
+                   "serve encode")))
+    return rc;
   if ((rc = c.cuda(cudaMemsetAsync(S.counters.p, 0, sizeof(unsigned long long) * (buckets.size() + 1), st), "serve")))
     return rc;
   WaveArgs a{};
@@ -328,6 +338,8 @@ int Server::launch_batch(Slot& S) {
       return rc;
     jo += sizeof(unsigned long long) * 5;
   }
+  if ((rc = c.cuda(cudaMemcpyAsync(hj + jo, S.bad.p, sizeof(int) * total_seqs, cudaMemcpyDeviceToHost, st), "serve")))
+    return rc;
   return c.cuda(cudaEventRecord(S.done, st), "serve event");
 }
 
@@ -403,8 +415,16 @@ void Server::completer_loop() {
     for (ServeJob* J : S.batch) {
       std::memcpy(J->njst, hj + jo, sizeof(J->njst));
       jo += sizeof(J->njst);
+    }
+    const int* badseq = reinterpret_cast<const int*>(hj + jo);
+    for (ServeJob* J : S.batch) {
+      int nbad = 0;
+      for (int k = 0; k < J->n; ++k) nbad += badseq[J->seq_base + k];
       J->D.assign((const float*)S.h_D.p + J->d_off, (const float*)S.h_D.p + J->d_off + (size_t)J->n * J->n);
-      J->status = e == cudaSuccess ? (J->njst[2] ? NWG_ERR_CUDA : NWG_OK) : NWG_ERR_CUDA;
+      J->status = e != cudaSuccess ? NWG_ERR_CUDA
+                  : nbad           ? NWG_ERR_BAD_RESIDUE
+                  : J->njst[2]     ? NWG_ERR_CUDA
+                                   : NWG_OK;
       J->t_done = now;
       J->done = true;
       in_use -= (int64_t)J->footprint;
@@ -456,12 +476,13 @@ int nwg_server_submit(nwg_server* srv, const char* ascii, const int64_t* offsets
   J->n = n;
   J->off.assign(offsets, offsets + n + 1);
   for (int k = 0; k <= n; ++k) J->off[k] -= offsets[0];
-  J->codes.resize((size_t)std::max<int64_t>(J->off[n], 1));
-  const int rc = nwg_encode(ascii + offsets[0], J->off.data(), n, J->codes.data());
-  if (rc != NWG_OK) {
-    delete J;
-    return rc;
-  }
+  for (int k = 0; k < n; ++k)
+    if (J->off[k + 1] <= J->off[k]) {
+      delete J;
+      return NWG_ERR_EMPTY_SEQ;
+    }
+  J->ascii.assign(ascii + offsets[0], ascii + offsets[n]);
+  if (J->ascii.empty()) J->ascii.push_back(0);
   J->footprint = s->footprint(n);
   if ((int64_t)J->footprint > s->budget) {
     delete J;

@@ -228,6 +228,7 @@ void Ctx::extra_release() {
   delete reinterpret_cast<TraceState*>(trace_state);
   trace_state = nullptr;
   nj_release();
+  ingest_release();
 }
 
 int Ctx::align_pairs(const int8_t* codes, const int64_t* offsets, int n, const int32_t* px, const int32_t* py,

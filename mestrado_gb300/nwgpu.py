@@ -225,6 +225,30 @@ class Context:
         joins = joins[: max(n - 1, 0)]
         return (joins, st.as_dict()) if stats else joins
 
+    def encode_dev(self, d_ascii: int, offsets, d_codes: int):
+        """Encode and reverse on the device (device pointers, host offsets);
+        returns the count of bytes outside the alphabet (codes -1 there)."""
+        from ._native import NWG_ERR_BAD_RESIDUE
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        bad = np.zeros(1, dtype=np.int64)
+        st = self._lib.nwg_encode_dev(self.h, ctypes.c_void_p(d_ascii), _p(offsets, c_i64p), len(offsets) - 1,
+                                      ctypes.c_void_p(d_codes), _p(bad, c_i64p))
+        if st != NWG_ERR_BAD_RESIDUE:
+            self._check(st)
+        return int(bad[0])
+
+    def parse_wire_dev(self, wire: bytes, d_wire: int, n: int, d_codes: int):
+        """Offsets of the wire block's sequences and their codes on the device
+        (d_wire: device copy of `wire`); returns (offsets, bad count)."""
+        from ._native import NWG_ERR_BAD_RESIDUE
+        off = np.zeros(n + 1, dtype=np.int64)
+        bad = np.zeros(1, dtype=np.int64)
+        st = self._lib.nwg_parse_wire_dev(self.h, wire, ctypes.c_void_p(d_wire), n, ctypes.c_void_p(d_codes),
+                                          _p(off, c_i64p), _p(bad, c_i64p))
+        if st != NWG_ERR_BAD_RESIDUE:
+            self._check(st)
+        return off, int(bad[0])
+
     def score_pairs(self, codes, offsets, pi, pj):
         """Scores of explicit pairs (int32 lanes, one thread per pair)."""
         pi = np.ascontiguousarray(pi, dtype=np.int32)
