@@ -293,6 +293,23 @@ int nwg_set_tuning(nwg_ctx* ctx, const int32_t* rows_per_lane, const int32_t* va
 int nwg_set_tuning_lanes(nwg_ctx* ctx, const int32_t* rows_per_lane, const int32_t* variant,
                          const int32_t* lanes);
 
+/* ---- progressive alignment ----------------------------------------------------
+ * The multiple alignment along the guide tree (the reference's
+ * AlignmentMatch::computeMSA, AlignmentMatch.cu:320-434, is an empty loop:
+ * this is the library's own definition, the same as the oracle's nwo_msa).
+ * Internal node n+k joins left[k] (columns) and right[k] (rows), left[k] <
+ * right[k] < n+k -- the (i, j) of nwg_join records.  Profiles are letter
+ * counts per column; a merge is the pairwise recurrence and traceback flags
+ * of nwg_align_pairs with the cell score sum_x sum_y cX[x] cY[y] S[x][y] and
+ * the gap penalties scaled by the product of the two profiles' sequence
+ * counts (64-bit integers); columns a walk leaves are appended opposite gaps.
+ * codes/offsets: reversed codes (nwg_encode).  Returns the alignment length in
+ * *msa_len; nwg_msa_rows then copies the n rows (forward order, '-' for gaps)
+ * to out, row k at out + k*row_stride (row_stride >= length). */
+int nwg_msa(nwg_ctx* ctx, const int8_t* codes, const int64_t* offsets, int n, const int32_t* left,
+            const int32_t* right, int64_t* msa_len, nwg_stats* stats);
+int nwg_msa_rows(nwg_ctx* ctx, char* out, int64_t row_stride);
+
 /* ---- serving loop ------------------------------------------------------------
  * Alignment jobs (one sequence family each: distance matrix + guide tree, the
  * work of SpeciesBlock::buildTree up to the join loop, SpeciesBlock.cpp:242-403

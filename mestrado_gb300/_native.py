@@ -192,6 +192,8 @@ EXTRA_SIGS: dict = {
     "nwg_cherries": ([c_i32p, c_i32p, ctypes.c_int, c_i32p, c_i32p, c_i32p], ctypes.c_int),
     "nwg_dpx_peak": ([ctypes.c_void_p, ctypes.c_int, P(ctypes.c_double)], ctypes.c_int),
     "nwg_dpx_peak_form": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int, P(ctypes.c_double)], ctypes.c_int),
+    "nwg_msa": ([ctypes.c_void_p, c_i8p, c_i64p, ctypes.c_int, c_i32p, c_i32p, c_i64p, P(Stats)], ctypes.c_int),
+    "nwg_msa_rows": ([ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int64], ctypes.c_int),
     "nwg_encode_dev": ([ctypes.c_void_p, ctypes.c_void_p, c_i64p, ctypes.c_int, ctypes.c_void_p, c_i64p],
                        ctypes.c_int),
     "nwg_parse_wire_dev": ([ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, c_i64p,

@@ -107,9 +107,14 @@ struct Ctx {
   void* trace_state = nullptr;
   void* nj_state = nullptr;
   void* ingest_state = nullptr;
+  void* msa_state = nullptr;
   void extra_release();
   void nj_release();
   void ingest_release();
+  void msa_release();
+  int msa(const int8_t* codes, const int64_t* offsets, int n, const int32_t* left, const int32_t* right,
+          int64_t* msa_len, nwg_stats* st);
+  int msa_rows(char* out, int64_t stride);
   int nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, nwg_nj_stats* st);
   int align_pairs(const int8_t* codes, const int64_t* offsets, int n, const int32_t* px, const int32_t* py,
                   int npairs, char* outx, char* outy, int64_t stride, int32_t* outlen, int32_t* score,

@@ -229,6 +229,7 @@ void Ctx::extra_release() {
   trace_state = nullptr;
   nj_release();
   ingest_release();
+  msa_release();
 }
 
 int Ctx::align_pairs(const int8_t* codes, const int64_t* offsets, int n, const int32_t* px, const int32_t* py,

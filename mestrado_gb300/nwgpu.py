@@ -225,6 +225,26 @@ class Context:
         joins = joins[: max(n - 1, 0)]
         return (joins, st.as_dict()) if stats else joins
 
+    def msa(self, seqs=None, left=None, right=None, *, codes=None, offsets=None, stats: bool = False):
+        """Progressive alignment along the guide tree (node n+k joins left[k],
+        right[k], e.g. the i and j of the nj() records): list of n gapped
+        rows in forward order."""
+        if codes is None:
+            codes, offsets = encode(seqs)
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        n = len(offsets) - 1
+        left = np.ascontiguousarray(left if left is not None else [], dtype=np.int32)
+        right = np.ascontiguousarray(right if right is not None else [], dtype=np.int32)
+        L = ctypes.c_int64()
+        st = Stats()
+        self._check(self._lib.nwg_msa(self.h, _p(codes, c_i8p), _p(offsets, c_i64p), n, _p(left, c_i32p),
+                                      _p(right, c_i32p), ctypes.byref(L), ctypes.byref(st)))
+        buf = ctypes.create_string_buffer(max(n * L.value, 1))
+        self._check(self._lib.nwg_msa_rows(self.h, buf, L.value))
+        raw = buf.raw
+        rows = [raw[k * L.value:(k + 1) * L.value] for k in range(n)]
+        return (rows, st.as_dict()) if stats else rows
+
     def encode_dev(self, d_ascii: int, offsets, d_codes: int):
         """Encode and reverse on the device (device pointers, host offsets);
         returns the count of bytes outside the alphabet (codes -1 there)."""

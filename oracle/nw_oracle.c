@@ -479,3 +479,162 @@ void nwo_nj(float* D, int n, nwo_join* joins, nwo_nj_stats* stats) {
   if (stats) *stats = st;
   free(slot); free(act); free(T); free(vd);
 }
+
+
+/* ---- progressive alignment (nwo_msa) ----------------------------------- */
+
+typedef struct {
+  int len;          /* columns                                   */
+  int k;            /* sequences                                 */
+  int32_t* cnt;     /* len x NWO_LETTERS letter counts, reversed  */
+  int32_t* mapx;    /* merge: X column -> new column (reversed)   */
+  int32_t* mapy;    /* merge: Y column -> new column (reversed)   */
+  int left, right;  /* children (internal nodes), -1 for leaves   */
+} nwo_prof;
+
+static int64_t i64max(int64_t a, int64_t b) { return a > b ? a : b; }
+
+/* Merge X (columns) and Y (rows) into a new profile; fills the maps. */
+static int msa_merge(const nwo_prof* X, const nwo_prof* Y, int go, int ge, const int8_t* sub, nwo_prof* out,
+                     int32_t* mapx, int32_t* mapy) {
+  const int lx = X->len, ly = Y->len;
+  const int64_t kk = (int64_t)X->k * Y->k;
+  const int64_t GO = go * kk, GE = ge * kk;
+  const int64_t kSent = -(((int64_t)1) << 60);
+  /* W[y][x] = sum_b cY[y][b] S[x][b]: the row's score against letter x */
+  int64_t* W = (int64_t*)malloc(sizeof(int64_t) * (size_t)ly * NWO_LETTERS);
+  for (int r = 0; r < ly; ++r)
+    for (int x = 0; x < NWO_LETTERS; ++x) {
+      int64_t w = 0;
+      for (int b = 0; b < NWO_LETTERS; ++b) w += (int64_t)Y->cnt[(size_t)r * NWO_LETTERS + b] * sub[b * NWO_LETTERS + x];
+      W[(size_t)r * NWO_LETTERS + x] = w;
+    }
+  uint8_t* nib = (uint8_t*)malloc((size_t)lx * ly + 1);
+  int64_t* Hrow = (int64_t*)malloc(sizeof(int64_t) * (size_t)lx);
+  int64_t* Frow = (int64_t*)malloc(sizeof(int64_t) * (size_t)lx);
+  for (int c = 0; c < lx; ++c) { Hrow[c] = -GE * (c + 1); Frow[c] = kSent; }
+  for (int r = 0; r < ly; ++r) {
+    int64_t hleft = -GE * (r + 1), eleft = kSent, diag = (r == 0) ? 0 : -GE * r;
+    const int64_t* w = W + (size_t)r * NWO_LETTERS;
+    for (int c = 0; c < lx; ++c) {
+      const int32_t* cx = X->cnt + (size_t)c * NWO_LETTERS;
+      int64_t s = 0;
+      for (int x = 0; x < NWO_LETTERS; ++x) s += (int64_t)cx[x] * w[x];
+      const int64_t hup = Hrow[c], fup = Frow[c];
+      const int64_t f = i64max(fup - GE, hup - GO);
+      const int cu = (f == fup - GE);
+      const int64_t e = i64max(eleft - GE, hleft - GO);
+      const int cl = (e == eleft - GE);
+      const int64_t sim = diag + s;
+      const int64_t h = i64max(i64max(e, f), sim);
+      const int L = ((h == e) && (h != f)) || (h == sim);
+      const int U = (h == f) || (h == sim);
+      nib[(size_t)r * lx + c] = (uint8_t)((L << 3) | (U << 2) | (cu << 1) | cl);
+      diag = hup;
+      Hrow[c] = h;
+      Frow[c] = f;
+      hleft = h;
+      eleft = e;
+    }
+  }
+  /* walk: ops in forward order; 12 = both columns, 8 = X only, 4 = Y only */
+  uint8_t* ops = (uint8_t*)malloc((size_t)lx + ly + 1);
+  int px = lx - 1, py = ly - 1, k = 0;
+  unsigned prev = 12u;
+#define NIB(xx, yy) ((yy) < 0 ? ((xx) < 0 ? 0u : 9u) : ((xx) < 0 ? 6u : (unsigned)nib[(size_t)(yy) * lx + (xx)]))
+  unsigned cell = NIB(px, py);
+  while ((cell & 12u) && k < lx + ly) {
+    unsigned todo;
+    if (((prev & 12u) == 4u) && (prev & 2u)) todo = 4u;
+    else if (((prev & 12u) == 8u) && (prev & 1u)) todo = 8u;
+    else if ((cell & 12u) == 4u) todo = 4u;
+    else if ((cell & 12u) == 8u) todo = 8u;
+    else todo = 12u;
+    if ((todo != 4u && px < 0) || (todo != 8u && py < 0)) break;
+    int stop = 0;
+    ops[k++] = (uint8_t)todo;
+    if (todo == 8u) --px;
+    else if (todo == 4u) { --py; stop = py < 0; }
+    else { --px; --py; }
+    prev = todo | (cell & 3u);
+    cell = stop ? 0u : NIB(px, py);
+  }
+#undef NIB
+  while (px >= 0) { ops[k++] = 8u; --px; }   /* columns the walk left */
+  while (py >= 0) { ops[k++] = 4u; --py; }
+  /* merged profile: op j (forward) is new column k-1-j (reversed) */
+  out->len = k;
+  out->k = X->k + Y->k;
+  out->cnt = (int32_t*)calloc((size_t)k * NWO_LETTERS + 1, sizeof(int32_t));
+  int ix = lx - 1, iy = ly - 1;
+  for (int j = 0; j < k; ++j) {
+    const int col = k - 1 - j;
+    int32_t* o = out->cnt + (size_t)col * NWO_LETTERS;
+    if (ops[j] & 8u) {
+      for (int x = 0; x < NWO_LETTERS; ++x) o[x] += X->cnt[(size_t)ix * NWO_LETTERS + x];
+      mapx[ix--] = col;
+    }
+    if (ops[j] & 4u) {
+      for (int x = 0; x < NWO_LETTERS; ++x) o[x] += Y->cnt[(size_t)iy * NWO_LETTERS + x];
+      mapy[iy--] = col;
+    }
+  }
+  free(W); free(nib); free(Hrow); free(Frow); free(ops);
+  return k;
+}
+
+int64_t nwo_msa(const int8_t* codes, const int64_t* offsets, int n, const int32_t* left, const int32_t* right,
+                int go, int ge, const int8_t* sub, char* out, int64_t cap) {
+  if (n < 1) return -1;
+  const int nn = 2 * n - 1;
+  nwo_prof* P = (nwo_prof*)calloc((size_t)nn, sizeof(nwo_prof));
+  for (int v = 0; v < n; ++v) {
+    const int L = (int)(offsets[v + 1] - offsets[v]);
+    P[v].len = L;
+    P[v].k = 1;
+    P[v].left = P[v].right = -1;
+    P[v].cnt = (int32_t*)calloc((size_t)L * NWO_LETTERS + 1, sizeof(int32_t));
+    for (int c = 0; c < L; ++c) {
+      int x = codes[offsets[v] + c];
+      if (x < 0 || x >= NWO_LETTERS) x = NWO_LETTERS - 1;
+      P[v].cnt[(size_t)c * NWO_LETTERS + x] = 1;
+    }
+  }
+  for (int k = 0; k < n - 1; ++k) {
+    const int a = left[k], b = right[k], v = n + k;
+    if (a < 0 || b < 0 || a >= v || b >= v || a >= b || P[a].cnt == NULL || P[b].cnt == NULL) return -1;
+    P[a].mapx = (int32_t*)malloc(sizeof(int32_t) * (size_t)P[a].len + 4);
+    P[b].mapy = (int32_t*)malloc(sizeof(int32_t) * (size_t)P[b].len + 4);
+    msa_merge(&P[a], &P[b], go, ge, sub, &P[v], P[a].mapx, P[b].mapy);
+    P[v].left = a;
+    P[v].right = b;
+  }
+  const int root = nn - 1;
+  const int64_t L = P[root].len;
+  if (out && cap >= (int64_t)n * L) {
+    /* final forward position of every column, parents before children */
+    int32_t** pos = (int32_t**)calloc((size_t)nn, sizeof(int32_t*));
+    pos[root] = (int32_t*)malloc(sizeof(int32_t) * (size_t)L + 4);
+    for (int c = 0; c < L; ++c) pos[root][c] = (int32_t)(L - 1 - c);
+    for (int v = root; v >= n; --v) {
+      const int a = P[v].left, b = P[v].right;
+      pos[a] = (int32_t*)malloc(sizeof(int32_t) * (size_t)P[a].len + 4);
+      pos[b] = (int32_t*)malloc(sizeof(int32_t) * (size_t)P[b].len + 4);
+      for (int c = 0; c < P[a].len; ++c) pos[a][c] = pos[v][P[a].mapx[c]];
+      for (int c = 0; c < P[b].len; ++c) pos[b][c] = pos[v][P[b].mapy[c]];
+    }
+    static const char kDec[NWO_LETTERS + 1] = "ARNDCQEGHILKMFPSTWYVBZX*";
+    memset(out, '-', (size_t)n * L);
+    for (int v = 0; v < n; ++v)
+      for (int c = 0; c < P[v].len; ++c) {
+        int x = codes[offsets[v] + c];
+        if (x < 0 || x >= NWO_LETTERS) x = NWO_LETTERS - 1;
+        out[(size_t)v * L + pos[v][c]] = kDec[x];
+      }
+    for (int v = 0; v < nn; ++v) free(pos[v]);
+    free(pos);
+  }
+  for (int v = 0; v < nn; ++v) { free(P[v].cnt); free(P[v].mapx); free(P[v].mapy); }
+  free(P);
+  return L;
+}

@@ -92,6 +92,22 @@ typedef struct {
  * modified in place.  joins must hold n-1 records. */
 void nwo_nj(float* D, int n, nwo_join* joins, nwo_nj_stats* stats);
 
+/* Progressive alignment along the guide tree (this build's definition: the
+ * reference's AlignmentMatch::computeMSA, AlignmentMatch.cu:320-434, is an
+ * empty loop -- parity unpinned).  Internal node n+k joins left[k] (X,
+ * columns) and right[k] (Y, rows), left[k] < right[k].  A profile is its
+ * columns' letter counts, in reversed column order like the codes; a merge
+ * aligns two profiles with the pairwise recurrence and flags of
+ * nwo_traceback, generalised: the cell score is the sum over residue pairs
+ * sum_x sum_y cX[x] cY[y] S[x][y], the gap penalties are go*kX*kY and
+ * ge*kX*kY (k = sequences in a profile), all in 64-bit integers.  The walk
+ * follows nwo_traceback's rules; columns it leaves (an up move out of row 0)
+ * are appended opposite gaps.  Writes n rows of L characters (row k =
+ * sequence k in forward order, '-' for gaps) to out when cap >= n*L; returns
+ * L (or -1 on a malformed tree). */
+int64_t nwo_msa(const int8_t* codes, const int64_t* offsets, int n, const int32_t* left, const int32_t* right,
+                int go, int ge, const int8_t* sub, char* out, int64_t cap);
+
 #ifdef __cplusplus
 }
 #endif

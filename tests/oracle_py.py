@@ -62,6 +62,9 @@ def lib():
                                     ctypes.c_char_p, P(ctypes.c_int)]
         L.nwo_traceback.restype = ctypes.c_int
         L.nwo_nj.argtypes = [P(ctypes.c_float), ctypes.c_int, P(Join), P(NJStats)]
+        L.nwo_msa.argtypes = [P(ctypes.c_int8), P(ctypes.c_int64), ctypes.c_int, P(ctypes.c_int32), P(ctypes.c_int32),
+                              ctypes.c_int, ctypes.c_int, P(ctypes.c_int8), ctypes.c_char_p, ctypes.c_int64]
+        L.nwo_msa.restype = ctypes.c_int64
         _LIB = L
     return _LIB
 
@@ -132,6 +135,25 @@ def traceback(x: bytes, y: bytes, go: int = 10, ge: int = 2):
     lib().nwo_traceback(_p(cx, ctypes.c_int8), len(x), _p(cy, ctypes.c_int8), len(y), go, ge,
                         _p(sub, ctypes.c_int8), bx, by, ctypes.byref(sc))
     return bx.value, by.value, sc.value
+
+
+def msa(seqset, left, right, go: int = 10, ge: int = 2, sub=None):
+    """Progressive alignment along the guide tree (internal node n+k joins
+    left[k], right[k]): list of n gapped rows, forward order."""
+    codes, off = encode(seqset)
+    n = len(off) - 1
+    left = np.ascontiguousarray(left, dtype=np.int32)
+    right = np.ascontiguousarray(right, dtype=np.int32)
+    sub = blosum() if sub is None else np.ascontiguousarray(sub, dtype=np.int8).reshape(576)
+    L = lib().nwo_msa(_p(codes, ctypes.c_int8), _p(off, ctypes.c_int64), n, _p(left, ctypes.c_int32),
+                      _p(right, ctypes.c_int32), go, ge, _p(sub, ctypes.c_int8), None, 0)
+    if L < 0:
+        raise ValueError("malformed tree")
+    buf = ctypes.create_string_buffer(int(n * L) + 1)
+    lib().nwo_msa(_p(codes, ctypes.c_int8), _p(off, ctypes.c_int64), n, _p(left, ctypes.c_int32),
+                  _p(right, ctypes.c_int32), go, ge, _p(sub, ctypes.c_int8), buf, n * L)
+    raw = buf.raw
+    return [raw[k * L:(k + 1) * L] for k in range(n)]
 
 
 def nj(D: np.ndarray):
