@@ -91,6 +91,7 @@ struct NJDev {
   nwg_join* joins;
   float* vd;           // per slot, new row values
   float* rmin;         // per slot: smallest float q of the row's pairs (c > r) in this join
+  float* rmax;         // per slot: largest magnitude of those pairs' terms (large-n path)
   int n0;
   int cand_cap;        // candidate list capacity
 };
@@ -230,11 +231,8 @@ __global__ void __launch_bounds__(256) pass_min_kernel(NJDev s, float nm2f) {
       qmin = fminf(qmin, sq[w]);
       mmax = fmaxf(mmax, sm[w]);
     }
-    s.rmin[r] = qmin;
-    if (qmin < FLT_MAX) {
-      atomicMin(&s.g32[0], ford(qmin));
-      atomicMax(&s.g32[1], ford(mmax));
-    }
+    s.rmin[r] = qmin;   // the step kernel reduces these (no contended atomics here)
+    s.rmax[r] = mmax;
   }
 }
 
@@ -519,11 +517,40 @@ __global__ void __launch_bounds__(1024) step_kernel(NJDev s, int step, int next,
   __shared__ int nrows;
   const double nm2 = (double)(m_n - 2);
   const float nm2f = (float)(m_n - 2);
-  const float qmin = iord(s.g32[0]);
-  const float mmax = iord(s.g32[1]);
-  const float thr = qmin + 3.f * (8.f * 5.9604645e-8f * mmax) + 1e-30f;
+  __shared__ float red_q[32], red_m[32];
+  // the global minimum and magnitude from the rows' values
+  float qmin = FLT_MAX, mmax = 0.f;
+  for (int p = threadIdx.x; p < s.n0; p += blockDim.x) {
+    if (s.node[p] >= 0) {
+      qmin = fminf(qmin, s.rmin[p]);
+      mmax = fmaxf(mmax, s.rmax[p]);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    qmin = fminf(qmin, __shfl_xor_sync(0xffffffffu, qmin, o));
+    mmax = fmaxf(mmax, __shfl_xor_sync(0xffffffffu, mmax, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red_q[threadIdx.x >> 5] = qmin;
+    red_m[threadIdx.x >> 5] = mmax;
+  }
   if (threadIdx.x == 0) nrows = 0;
   __syncthreads();
+  if (threadIdx.x < 32) {
+    const int nw = (int)(blockDim.x >> 5);
+    qmin = threadIdx.x < nw ? red_q[threadIdx.x] : FLT_MAX;
+    mmax = threadIdx.x < nw ? red_m[threadIdx.x] : 0.f;
+    for (int o = 16; o > 0; o >>= 1) {
+      qmin = fminf(qmin, __shfl_xor_sync(0xffffffffu, qmin, o));
+      mmax = fmaxf(mmax, __shfl_xor_sync(0xffffffffu, mmax, o));
+    }
+    if (threadIdx.x == 0) {
+      red_q[0] = qmin;
+      red_m[0] = mmax;
+    }
+  }
+  __syncthreads();
+  const float thr = red_q[0] + 3.f * (8.f * 5.9604645e-8f * red_m[0]) + 1e-30f;
   // live slots whose row minimum is within the threshold (usually one or two)
   for (int p = threadIdx.x; p < s.n0; p += blockDim.x) {
     if (s.node[p] >= 0 && s.rmin[p] <= thr) {
@@ -861,10 +888,10 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_cluster_
 
 struct NJState {
   DevBuf D, T, Tf, slot, node, act, na, g32, cand, win, stats, joins, vd, rmin;
-  DevBuf D2, T2, Tf2, node2, map, desc;   // large-n path: the other half of the compaction buffers
+  DevBuf D2, T2, Tf2, node2, map, desc, rmax;   // large-n path: compaction buffers, row magnitudes
   ~NJState() {
     for (DevBuf* b : {&D, &T, &Tf, &slot, &node, &act, &na, &g32, &cand, &win, &stats, &joins, &vd, &rmin, &D2, &T2,
-                      &Tf2, &node2, &map, &desc})
+                      &Tf2, &node2, &map, &desc, &rmax})
       b->release();
   }
 };
@@ -911,7 +938,7 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
     return fail(rc, "nj allocation");
   if (big && ((rc = S.D2.ensure(sizeof(float) * (size_t)n * n)) || (rc = S.T2.ensure(sizeof(double) * n)) ||
               (rc = S.Tf2.ensure(sizeof(float) * n)) || (rc = S.node2.ensure(sizeof(int) * n)) ||
-              (rc = S.map.ensure(sizeof(int) * n))))
+              (rc = S.map.ensure(sizeof(int) * n)) || (rc = S.rmax.ensure(sizeof(float) * n))))
     return fail(rc, "nj allocation");
   cudaStream_t s = stream;
   const cudaMemcpyKind kind = device_D ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
@@ -933,6 +960,7 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
   d.joins = (nwg_join*)S.joins.p;
   d.vd = (float*)S.vd.p;
   d.rmin = (float*)S.rmin.p;
+  d.rmax = big ? (float*)S.rmax.p : nullptr;
   d.n0 = n;
   d.cand_cap = kCandCap;
   if (!big) {

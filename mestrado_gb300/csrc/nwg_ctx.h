@@ -101,6 +101,7 @@ struct Ctx {
   cudaEvent_t fork_ev = nullptr;
   std::vector<cudaEvent_t> join_ev;
   int autotune(bool force, nwg_tune_result* out);
+  bool tune_from_cache(nwg_tune_result* res);
   int batched(const int8_t* d_codes, const int64_t* xoff, int nx, const int64_t* yoff, int ny, bool triangle,
               float* d_D, int64_t ld, int64_t col0, int mode, nwg_stats* st);
   // traceback / neighbor joining state (trace.cu, nj.cu)

@@ -453,6 +453,7 @@ int nwg_server_create(int gap_open, int gap_ext, int64_t hbm_budget_bytes, int m
   s->budget = hbm_budget_bytes;
   s->max_batch = max_batch_jobs;
   cudaGetDevice(&s->device);
+  s->ctx->tune_from_cache(nullptr);   // the device's autotuned table when one is cached
   for (auto& S : s->slots) {
     if (cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&S.done, cudaEventDisableTiming) != cudaSuccess) {

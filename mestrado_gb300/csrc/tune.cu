@@ -52,45 +52,52 @@ const char kCacheTag[] = "nwgpu-tune-3";
 
 }  // namespace
 
+// The cached table of this device, if one exists (no tuning run).
+bool Ctx::tune_from_cache(nwg_tune_result* res) {
+  const std::string path = cache_path(device);
+  FILE* f = std::fopen(path.c_str(), "r");
+  if (!f) return false;
+  int ok = 0;
+  TuneChoice t[kTuneClasses];
+  double g[kTuneClasses];
+  char tag[32] = {0};
+  if (std::fscanf(f, "%31s", tag) == 1 && std::strcmp(tag, kCacheTag) == 0) {
+    for (int k = 0; k < kTuneClasses; ++k) {
+      int kk, R, V, W;
+      double gc;
+      if (std::fscanf(f, "%d %d %d %d %lf", &kk, &R, &V, &W, &gc) == 5 && kk == k && wave_exists(R, 2, V, W)) {
+        t[k] = {R, V, W};
+        g[k] = gc;
+        ++ok;
+      }
+    }
+  }
+  std::fclose(f);
+  if (ok != kTuneClasses) return false;
+  for (int k = 0; k < kTuneClasses; ++k) {
+    tune[k] = t[k];
+    if (res) {
+      res->rows_per_lane[k] = t[k].R;
+      res->variant[k] = t[k].V;
+      res->lanes[k] = t[k].W;
+      res->gcups[k] = g[k];
+    }
+  }
+  ++tune_version;
+  tuned = true;
+  if (res) res->from_cache = 1;
+  return true;
+}
+
 int Ctx::autotune(bool force, nwg_tune_result* out) {
   const std::string path = cache_path(device);
   nwg_tune_result res;
   std::memset(&res, 0, sizeof(res));
   res.classes = kTuneClasses;
   for (int k = 0; k < kTuneClasses; ++k) res.max_rows[k] = kClassRows[k] > 1000000 ? 0x7fffffff : kClassRows[k];
-  if (!force) {
-    if (FILE* f = std::fopen(path.c_str(), "r")) {
-      int ok = 0;
-      TuneChoice t[kTuneClasses];
-      double g[kTuneClasses];
-      char tag[32] = {0};
-      if (std::fscanf(f, "%31s", tag) == 1 && std::strcmp(tag, kCacheTag) == 0) {
-        for (int k = 0; k < kTuneClasses; ++k) {
-          int kk, R, V, W;
-          double gc;
-          if (std::fscanf(f, "%d %d %d %d %lf", &kk, &R, &V, &W, &gc) == 5 && kk == k && wave_exists(R, 2, V, W)) {
-            t[k] = {R, V, W};
-            g[k] = gc;
-            ++ok;
-          }
-        }
-      }
-      std::fclose(f);
-      if (ok == kTuneClasses) {
-        for (int k = 0; k < kTuneClasses; ++k) {
-          tune[k] = t[k];
-          res.rows_per_lane[k] = t[k].R;
-          res.variant[k] = t[k].V;
-          res.lanes[k] = t[k].W;
-          res.gcups[k] = g[k];
-        }
-        ++tune_version;
-        tuned = true;
-        res.from_cache = 1;
-        if (out) *out = res;
-        return NWG_OK;
-      }
-    }
+  if (!force && tune_from_cache(&res)) {
+    if (out) *out = res;
+    return NWG_OK;
   }
   const auto t0 = std::chrono::steady_clock::now();
   const bool saved_graphs = use_graphs;
