@@ -207,6 +207,7 @@ __global__ void __launch_bounds__(256) pass_min_kernel(NJDev s, float nm2f) {
   const float tr = s.Tf[r];
   const float* row = s.D + (size_t)r * s.n0;
   float qmin = FLT_MAX, mmax = 0.f;
+#pragma unroll 8
   for (int c = r + 1 + threadIdx.x; c < s.n0; c += blockDim.x) {
     if (s.node[c] < 0) continue;
     const float d = row[c];
@@ -305,19 +306,18 @@ __device__ void pick_body(const NJDev& s) {
 // The join: record, modifyMatrix, active list.  One CTA; tv and ids are
 // shared-memory arrays of n0 entries.
 __device__ void join_body(const NJDev& s, int step, int next, int m_n, float* tv, int* ids) {
-  __shared__ int s_pos[1024 / 32 + 1];
   __shared__ int s_skip[2];
   __shared__ long long s_isum[32], s_iabs[32];
   __shared__ int s_low[33], s_top[33];
   const Pick w = *s.win;
-  if (w.b < 0) return;                 // counted as an internal error by pick_kernel
+  if (w.b < 0) return;                 // counted as an internal error by the pick
   const int i = w.a, j = w.b;          // i < j
   const int si = s.slot[i], sj = s.slot[j];
   const int n0 = s.n0;
   const int na = *s.na;
   const float dmin = s.D[(size_t)si * n0 + sj];
   if (threadIdx.x == 0) {
-    // TreeNode::join with left = min id, right = max id
+    // TreeNode::join with left = min id, right = max id (overlaps the loop below)
     const double Ti = s.T[si], Tj = s.T[sj];
     double li, lj;
     const double half = 0.5;
@@ -348,10 +348,15 @@ __device__ void join_body(const NJDev& s, int step, int next, int m_n, float* tv
     J.len_i = li;
     J.len_j = lj;
   }
-  __syncthreads();
-  // new row values and T updates over active k != i, j (SpeciesBlock.cpp:787-817)
+  // One pass over the active nodes k != i, j (SpeciesBlock.cpp:787-841):
+  // tmp = ((Dik + Djk) - d) / 2 in float, T[k] += (float)(tmp - (Dik + Djk)),
+  // the new row and column of slot si (its diagonal keeps i's old value), the
+  // old active list copied for the compaction, and the exponent range of tmp.
+  // Each thread reads and writes only its own k's entries of row si.
+  int lowexp = INT_MAX, topexp = INT_MIN;
   for (int k = threadIdx.x; k < na; k += blockDim.x) {
     const int v = s.act[k];
+    ids[k] = v;
     if (v == i || v == j) {
       s_skip[v == i ? 0 : 1] = k;
       tv[k] = 0.f;
@@ -362,69 +367,65 @@ __device__ void join_body(const NJDev& s, int step, int next, int m_n, float* tv
     const float Djk = s.D[(size_t)sj * n0 + sk];
     const float sumf = __fadd_rn(Dik, Djk);
     const float tmp = __fmul_rn(__fsub_rn(sumf, dmin), 0.5f);
-    s.vd[sk] = tmp;
     tv[k] = tmp;
     const double t = __dadd_rn(s.T[sk], (double)__fsub_rn(tmp, sumf));
     s.T[sk] = t;
     s.Tf[sk] = (float)t;
+    s.D[(size_t)sk * n0 + si] = tmp;
+    s.D[(size_t)si * n0 + sk] = tmp;
+    lowexp = min(lowexp, low_bit_exp(tmp));
+    topexp = max(topexp, top_bit_exp(tmp));
+  }
+  // the new node's sum in ascending id order (SpeciesBlock.cpp:799, :818):
+  // the exact sum in 64-bit integers of 2^e (e = the lowest set bit of any
+  // term) when it proves every partial sum of the sequential loop exact, else
+  // the sequential loop itself
+  for (int o = 16; o > 0; o >>= 1) {
+    lowexp = min(lowexp, __shfl_xor_sync(0xffffffffu, lowexp, o));
+    topexp = max(topexp, __shfl_xor_sync(0xffffffffu, topexp, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    s_low[threadIdx.x >> 5] = lowexp;
+    s_top[threadIdx.x >> 5] = topexp;
   }
   __syncthreads();
-  // sum of tmp in ascending id order (SpeciesBlock.cpp:799, :818): the exact
-  // sum, taken in 64-bit integers of 2^e (e = the lowest set bit of any term),
-  // when it proves that every partial sum of the sequential loop is exact,
-  // else the sequential loop itself
-  {
-    int lowexp = INT_MAX, topexp = INT_MIN;
-    for (int k = threadIdx.x; k < na; k += blockDim.x) {
-      const float x = tv[k];            // 0 at i and j
-      lowexp = min(lowexp, low_bit_exp(x));
-      topexp = max(topexp, top_bit_exp(x));
-    }
+  if (threadIdx.x < 32) {
+    const int nw = (int)(blockDim.x >> 5);
+    lowexp = threadIdx.x < nw ? s_low[threadIdx.x] : INT_MAX;
+    topexp = threadIdx.x < nw ? s_top[threadIdx.x] : INT_MIN;
     for (int o = 16; o > 0; o >>= 1) {
       lowexp = min(lowexp, __shfl_xor_sync(0xffffffffu, lowexp, o));
       topexp = max(topexp, __shfl_xor_sync(0xffffffffu, topexp, o));
     }
+    if (threadIdx.x == 0) {
+      s_low[32] = lowexp;
+      s_top[32] = topexp;
+    }
+  }
+  __syncthreads();
+  lowexp = s_low[32];
+  topexp = s_top[32];
+  // every term below 2^49 units of 2^e: sums of up to 8192 terms stay below 2^62
+  const bool fits = lowexp == INT_MAX || topexp - lowexp < 48;
+  long long isum = 0, iabs = 0;
+  if (fits && lowexp != INT_MAX) {
+    for (int k = threadIdx.x; k < na; k += blockDim.x) {
+      const long long v = float_units(tv[k], lowexp);
+      isum += v;
+      iabs += v < 0 ? -v : v;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      isum += __shfl_xor_sync(0xffffffffu, isum, o);
+      iabs += __shfl_xor_sync(0xffffffffu, iabs, o);
+    }
     if ((threadIdx.x & 31) == 0) {
-      s_low[threadIdx.x >> 5] = lowexp;
-      s_top[threadIdx.x >> 5] = topexp;
+      s_isum[threadIdx.x >> 5] = isum;
+      s_iabs[threadIdx.x >> 5] = iabs;
     }
-    __syncthreads();
-    if (threadIdx.x < 32) {
-      const int nw = (int)(blockDim.x >> 5);
-      lowexp = threadIdx.x < nw ? s_low[threadIdx.x] : INT_MAX;
-      topexp = threadIdx.x < nw ? s_top[threadIdx.x] : INT_MIN;
-      for (int o = 16; o > 0; o >>= 1) {
-        lowexp = min(lowexp, __shfl_xor_sync(0xffffffffu, lowexp, o));
-        topexp = max(topexp, __shfl_xor_sync(0xffffffffu, topexp, o));
-      }
-      if (threadIdx.x == 0) {
-        s_low[32] = lowexp;
-        s_top[32] = topexp;
-      }
-    }
-    __syncthreads();
-    lowexp = s_low[32];
-    topexp = s_top[32];
-    // every term below 2^49 units of 2^e: sums of up to 8192 terms stay below 2^62
-    const bool fits = lowexp == INT_MAX || topexp - lowexp < 48;
-    long long isum = 0, iabs = 0;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
     if (fits && lowexp != INT_MAX) {
-      for (int k = threadIdx.x; k < na; k += blockDim.x) {
-        const long long v = float_units(tv[k], lowexp);
-        isum += v;
-        iabs += v < 0 ? -v : v;
-      }
-      for (int o = 16; o > 0; o >>= 1) {
-        isum += __shfl_xor_sync(0xffffffffu, isum, o);
-        iabs += __shfl_xor_sync(0xffffffffu, iabs, o);
-      }
-      if ((threadIdx.x & 31) == 0) {
-        s_isum[threadIdx.x >> 5] = isum;
-        s_iabs[threadIdx.x >> 5] = iabs;
-      }
-    }
-    __syncthreads();
-    if (threadIdx.x < 32 && fits && lowexp != INT_MAX) {
       const int nw = (int)(blockDim.x >> 5);
       isum = threadIdx.x < nw ? s_isum[threadIdx.x] : 0;
       iabs = threadIdx.x < nw ? s_iabs[threadIdx.x] : 0;
@@ -449,47 +450,15 @@ __device__ void join_body(const NJDev& s, int step, int next, int m_n, float* tv
       s.Tf[si] = (float)sum;
     }
   }
-  // D row and column of slot si (:820-841; the diagonal keeps i's old value)
-  for (int k = threadIdx.x; k < na; k += blockDim.x) {
-    const int v = s.act[k];
-    if (v == i || v == j) continue;
-    const int sk = s.slot[v];
-    const float t = s.vd[sk];
-    s.D[(size_t)sk * n0 + si] = t;
-    s.D[(size_t)si * n0 + sk] = t;
+  // compacted active list: ascending ids without i (at ki) and j (at kj > ki),
+  // plus next at the end -- a shift of the old list
+  {
+    const int ki = s_skip[0], kj = s_skip[1];
+    for (int k = threadIdx.x; k < na - 2; k += blockDim.x) s.act[k] = ids[k < ki ? k : (k < kj - 1 ? k + 1 : k + 2)];
   }
-  // compacted active list: ascending ids without i, j, plus next at the end
-  const int chunk = (na + blockDim.x - 1) / blockDim.x;
-  const int k0 = threadIdx.x * chunk;
-  int keep = 0;
-  for (int k = k0; k < k0 + chunk && k < na; ++k) keep += (s.act[k] != i && s.act[k] != j);
-  int incl = keep;
-  for (int o = 1; o < 32; o <<= 1) {
-    const int y = __shfl_up_sync(0xffffffffu, incl, o);
-    if ((threadIdx.x & 31) >= o) incl += y;
-  }
-  if ((threadIdx.x & 31) == 31) s_pos[threadIdx.x >> 5] = incl;
-  __syncthreads();
   if (threadIdx.x == 0) {
-    int acc = 0;
-    for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2) {
-      const int t = s_pos[w2];
-      s_pos[w2] = acc;
-      acc += t;
-    }
-    s_pos[blockDim.x >> 5] = acc;
-  }
-  __syncthreads();
-  int pos = s_pos[threadIdx.x >> 5] + incl - keep;
-  for (int k = k0; k < k0 + chunk && k < na; ++k)
-    if (s.act[k] != i && s.act[k] != j) ids[pos++] = s.act[k];
-  __syncthreads();
-  const int cnt = s_pos[blockDim.x >> 5];
-  for (int k = threadIdx.x; k < cnt; k += blockDim.x) s.act[k] = ids[k];
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    s.act[cnt] = next;
-    *s.na = cnt + 1;
+    s.act[na - 2] = next;
+    *s.na = na - 1;
     s.slot[j] = -1;
     s.slot[i] = -1;
     s.slot[next] = si;
@@ -498,7 +467,6 @@ __device__ void join_body(const NJDev& s, int step, int next, int m_n, float* tv
   }
   __syncthreads();
 }
-
 
 // ---- large n: full-GPU first pass, one CTA for the rest of the join --------
 // Per join: pass_min_kernel (one block per live row, every SM) writes the row
@@ -656,11 +624,13 @@ struct NJJob {
   int n;
 };
 
-// Shared-memory copies of the float row sums and the slot -> node map.
-__device__ void cta_refresh(const NJDev& s, float* sTf, int* snode) {
+// Shared-memory copies of the float row sums and the slot -> node map; the
+// row minima of the next pass start at +inf (ordered-int encoding).
+__device__ void cta_refresh(const NJDev& s, float* sTf, int* snode, int* srmin) {
   for (int k = threadIdx.x; k < s.n0; k += blockDim.x) {
     sTf[k] = s.Tf[k];
     snode[k] = s.node[k];
+    srmin[k] = 0x7F7FFFFF;
   }
   __syncthreads();
 }
@@ -705,21 +675,64 @@ __device__ void clu_rowsums(const NJDev& s, int w0, int wstride) {
   }
 }
 
+// Rows are dealt to the cluster's warps as folded slot pairs (p, n0-1-p):
+// row r has n0-1-r entries right of the diagonal, so every pair holds about
+// n0 of them.  With fewer pairs than warps, a pair is split over f warps of
+// one CTA (f a power of two, at most 32), each taking every f-th group of 32
+// columns of both rows; the row minima then meet in the CTA's shared memory.
+// Dead slots are skipped.  fn(row, first column offset, column stride).
+struct RowSplit {
+  int f;        // warps per pair
+  int unit;     // this warp's first unit (pair * f + share)
+  int ustride;  // units between this warp's units
+  int npairs;
+};
+
+__device__ __forceinline__ RowSplit row_split(int n0, int C) {
+  const int nw = C * (int)(blockDim.x >> 5);
+  const int npairs = (n0 + 1) >> 1;
+  int f = 1;
+  while (f < 32 && npairs * (f * 2) <= nw) f *= 2;
+  RowSplit rs;
+  rs.f = f;
+  rs.npairs = npairs;
+  // warp g of the cluster (rank-major) owns units g, g + nw, ...; the f units
+  // of a pair are consecutive warps of one CTA
+  rs.unit = (int)cooperative_groups::this_cluster().block_rank() * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5);
+  rs.ustride = nw;
+  return rs;
+}
+
+template <class Fn>
+__device__ __forceinline__ void for_my_rows(int n0, const int* __restrict__ snode, const RowSplit& rs, Fn&& fn) {
+  for (int u = rs.unit; u < rs.npairs * rs.f; u += rs.ustride) {
+    const int p = u / rs.f, share = u - p * rs.f;
+    if (snode[p] >= 0) fn(p, share * 32, rs.f * 32);
+    const int q = n0 - 1 - p;
+    if (q != p && snode[q] >= 0) fn(q, share * 32, rs.f * 32);
+  }
+}
+
+__device__ __forceinline__ int ford_s(float f) {
+  const int b = __float_as_int(f);
+  return b >= 0 ? b : b ^ 0x7FFFFFFF;
+}
+__device__ __forceinline__ float iord_s(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7FFFFFFF); }
+
 // This CTA's rows: the smallest float q and the largest magnitude, reduced
-// over the block into part[0], part[1]; srmin[r] = the row's smallest q.
+// over the block into part[0], part[1]; srmin[r] (ordered int, set to the
+// encoding of FLT_MAX beforehand) = the row's smallest q.
 __device__ void clu_pass_min(const NJDev& s, float nm2f, const float* __restrict__ sTf, const int* __restrict__ snode,
-                             float* __restrict__ srmin, int w0, int wstride, float* part) {
+                             int* __restrict__ srmin, const RowSplit& rs, float* part) {
   __shared__ float sq[32], sm[32];
-  const int na = *s.na;
   const int lane = threadIdx.x & 31;
   float qmin = FLT_MAX, mmax = 0.f;
-  for (int k = w0; k < na; k += wstride) {
-    const int r = s.slot[s.act[k]];
+  for_my_rows(s.n0, snode, rs, [&](int r, int c0, int cstride) {
     const float tr = sTf[r];
     const float* __restrict__ row = s.D + (size_t)r * s.n0;
     float rq = FLT_MAX;
 #pragma unroll 4
-    for (int c = r + 1 + lane; c < s.n0; c += 32) {
+    for (int c = r + 1 + c0 + lane; c < s.n0; c += cstride) {
       // branch-free: a dead slot's (finite, stale) entries are masked out
       const float d = row[c];
       const bool live = snode[c] >= 0;
@@ -731,9 +744,12 @@ __device__ void clu_pass_min(const NJDev& s, float nm2f, const float* __restrict
       mmax = fmaxf(mmax, live ? mag : 0.f);
     }
     for (int o = 16; o > 0; o >>= 1) rq = fminf(rq, __shfl_xor_sync(0xffffffffu, rq, o));
-    if (lane == 0) srmin[r] = rq;
+    if (lane == 0) {
+      if (rs.f == 1) srmin[r] = ford_s(rq);
+      else atomicMin(&srmin[r], ford_s(rq));
+    }
     qmin = fminf(qmin, rq);
-  }
+  });
   for (int o = 16; o > 0; o >>= 1) mmax = fmaxf(mmax, __shfl_xor_sync(0xffffffffu, mmax, o));
   if (lane == 0) {
     sq[threadIdx.x >> 5] = qmin;
@@ -757,17 +773,14 @@ __device__ void clu_pass_min(const NJDev& s, float nm2f, const float* __restrict
 
 __device__ void clu_pass_cand(const NJDev& s, float nm2f, double nm2, int watermark, float thr,
                               const float* __restrict__ sTf, const int* __restrict__ snode,
-                              const float* __restrict__ srmin, int w0, int wstride) {
-  const int na = *s.na;
+                              const int* __restrict__ srmin, const RowSplit& rs) {
   const int lane = threadIdx.x & 31;
-  for (int k = w0; k < na; k += wstride) {
-    const int ur = s.act[k];
-    const int r = s.slot[ur];
-    if (srmin[r] > thr) continue;   // no pair of this row is a candidate
+  for_my_rows(s.n0, snode, rs, [&](int r, int c0, int cstride) {
+    if (iord_s(srmin[r]) > thr) return;   // no pair of this row is a candidate
+    const int ur = snode[r];
     const float tr = sTf[r];
     const float* __restrict__ row = s.D + (size_t)r * s.n0;
-#pragma unroll 4
-    for (int c = r + 1 + lane; c < s.n0; c += 32) {
+    for (int c = r + 1 + c0 + lane; c < s.n0; c += cstride) {
       const float d = row[c];
       const int uc = snode[c];
       if (uc < 0) continue;
@@ -782,7 +795,7 @@ __device__ void clu_pass_cand(const NJDev& s, float nm2f, double nm2, int waterm
       const int idx = atomicAdd(&s.g32[2], 1);
       if (idx < s.cand_cap) s.cand[idx] = cd;
     }
-  }
+  });
 }
 
 template <int C>
@@ -794,7 +807,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_cluster_
   int* ids = reinterpret_cast<int*>(tv + nmax);
   float* sTf = reinterpret_cast<float*>(ids + nmax);
   int* snode = reinterpret_cast<int*>(sTf + nmax);
-  float* srmin = reinterpret_cast<float*>(snode + nmax);
+  int* srmin = snode + nmax;   // per slot, ordered-int row minimum
   __shared__ float part[2];   // this CTA's pass-1 partial (read by the other ranks)
   __shared__ float glob[2];   // the cluster's minimum and magnitude
   cg::cluster_group cl = cg::this_cluster();
@@ -806,6 +819,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_cluster_
   const int n = J.n;
   const int w0 = rank * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5);
   const int wstride = C * (int)(blockDim.x >> 5);
+  const RowSplit rs = row_split(n, C);
   if (rank == 0) {
     for (int k = threadIdx.x; k < 2 * n - 1; k += blockDim.x) s.slot[k] = k < n ? k : -1;
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
@@ -822,7 +836,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_cluster_
   if (n < 2) return;
   clu_rowsums(s, w0, wstride);
   cl.sync();
-  cta_refresh(s, sTf, snode);
+  cta_refresh(s, sTf, snode, srmin);
   const int kBinT = 30 * 31 / 2;
   int steps = max((int)((float)n * 0.5f), 200);
   int pq_ck = 500;
@@ -832,7 +846,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_cluster_
   for (int step = 0; step < n - 1; ++step) {
     const double nm2 = (double)(m_n - 2);
     const float nm2f = (float)(m_n - 2);
-    clu_pass_min(s, nm2f, sTf, snode, srmin, w0, wstride, part);
+    clu_pass_min(s, nm2f, sTf, snode, srmin, rs, part);
     cl.sync();
     if (threadIdx.x < 32) {
       const int l = threadIdx.x;
@@ -853,7 +867,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_cluster_
     }
     __syncthreads();
     const float thr = glob[0] + 3.f * (8.f * 5.9604645e-8f * glob[1]) + 1e-30f;
-    clu_pass_cand(s, nm2f, nm2, watermark, thr, sTf, snode, srmin, w0, wstride);
+    clu_pass_cand(s, nm2f, nm2, watermark, thr, sTf, snode, srmin, rs);
     cl.sync();
     if (rank == 0) {
       pick_body(s);
@@ -879,7 +893,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_cluster_
       --steps;
       ub += na - 1;
     }
-    cta_refresh(s, sTf, snode);
+    cta_refresh(s, sTf, snode, srmin);
   }
   cl.sync();   // no rank leaves while another may still read its shared memory
 }

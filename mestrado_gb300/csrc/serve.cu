@@ -38,6 +38,7 @@ namespace {
 // CTAs per job in the join-loop launch: the O(n^2) passes of one join split
 // over 8 SMs (jobs of one batch run side by side).
 constexpr int kNJClusterServe = 8;
+constexpr int kNJWideN = 256;   // from this job size on, the widest cluster
 
 double clock_ms() {
   using clk = std::chrono::steady_clock;
@@ -320,10 +321,12 @@ int Server::launch_batch(Slot& S) {
   }
   if ((rc = c.cuda(cudaMemcpyAsync(S.h_D.p, S.D.p, sizeof(float) * total_D, cudaMemcpyDeviceToHost, st), "serve")))
     return rc;
-  // join loops: one cluster of kNJClusterServe CTAs per job, all jobs in one launch
+  // join loops: one cluster per job, all jobs in one launch; batches with a
+  // large job take the device's largest cluster (the passes split wider)
   int nmax = 1;
   for (ServeJob* J : S.batch) nmax = std::max(nmax, J->n);
-  if ((rc = c.cuda(launch_nj_cluster(S.njdesc.p, nj, nmax, kNJClusterServe, st), "serve nj launch"))) return rc;
+  const int csize = nmax >= kNJWideN ? nj_cluster_size() : kNJClusterServe;
+  if ((rc = c.cuda(launch_nj_cluster(S.njdesc.p, nj, nmax, csize, st), "serve nj launch"))) return rc;
   char* hj = (char*)S.h_joins.p;
   size_t jo = 0;
   for (int k = 0; k < nj; ++k) {
