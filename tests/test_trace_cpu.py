@@ -37,3 +37,19 @@ def test_reference_cherry_list_is_a_prefix():
         # every internal node whose children are leaves is listed once
         all_cherries = {(n + k) for k in range(n - 1) if left[k] < n and right[k] < n}
         assert set(node.tolist()) == all_cherries
+
+
+def test_oracle_alignments_rescore_to_their_score():
+    # every traceback reproduces its own DP score under the recurrence's model
+    import numpy as np
+    import oracle_py as O
+    from rescore import rescore
+    rng = np.random.default_rng(4)
+    letters = np.frombuffer(b"ARNDCQEGHILKMFPSTWYV", dtype=np.uint8)
+    sub = O.blosum()
+    for _ in range(60):
+        x = letters[rng.integers(0, 20, rng.integers(1, 150))].tobytes()
+        y = letters[rng.integers(0, 20, rng.integers(1, 150))].tobytes()
+        ax, ay, sc = O.traceback(x, y)
+        assert ax.replace(b"-", b"") == x and ay.replace(b"-", b"") == y
+        assert rescore(ax, ay, sub) == sc

@@ -50,3 +50,19 @@ def test_cherries_of_reference_tree(ctx, case):
     right = np.array([int(r[2]) for r in rows], dtype=np.int32)
     node, l, r = cherries(left, right, len(seqs))
     _check(ctx, seqs, l, r)
+
+
+def test_device_alignments_rescore_to_their_score(ctx):
+    # independent of the flag rules: the path found reproduces the DP score
+    from rescore import rescore
+    from mestrado_gb300 import encode
+    rng = np.random.default_rng(12)
+    letters = np.frombuffer(b"ARNDCQEGHILKMFPSTWYV", dtype=np.uint8)
+    seqs = [letters[rng.integers(0, 20, rng.integers(1, 700))].tobytes() for _ in range(80)]
+    codes, off = encode(seqs)
+    px = np.arange(0, 80, 2, dtype=np.int32)
+    py = np.arange(1, 80, 2, dtype=np.int32)
+    sub = O.blosum()
+    for (ax, ay, sc), i, j in zip(ctx.align_pairs(codes, off, px, py), px, py):
+        assert ax.replace(b"-", b"") == seqs[i] and ay.replace(b"-", b"") == seqs[j]
+        assert rescore(ax, ay, sub) == sc
