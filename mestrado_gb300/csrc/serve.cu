@@ -14,9 +14,10 @@
 //   different jobs -> matrices out -> one launch of the per-CTA join loop
 //   (one CTA per job) -> join lists out.
 // While one slot's batch is on the device the next batch is formed and queued
-// on the other slot, so arrivals overlap the work in flight.  A completion
-// thread waits for each slot's event, hands results to their jobs and frees
-// their footprint.  Nothing waits on the device except those host-side event
+// on another free slot (four slots), so arrivals overlap the work in flight.
+// Each slot has its own completion thread that waits for that slot's event,
+// hands results to their jobs and frees their footprint, so a short batch
+// is returned without waiting for a longer one launched before it.  Nothing waits on the device except those host-side event
 // waits.
 #include <algorithm>
 #include <chrono>
@@ -91,7 +92,8 @@ struct Slot {
   DevBuf ascii, codes, bad, start, len, orig, gy, gy2, gx, gxb, gdofs, gld, jobsbuf, counters, scratch, D, njws, njdesc;
   HostBuf h_codes, h_plan, h_D, h_joins;
   std::vector<ServeJob*> batch;
-  bool busy = false;
+  bool busy = false;       // holds a batch (from admission to completion)
+  bool launched = false;   // its work is queued on the device
   size_t plan_bytes = 0;
   ~Slot() {
     for (DevBuf* b : {&ascii, &codes, &bad, &start, &len, &orig, &gy, &gy2, &gx, &gxb, &gdofs, &gld, &jobsbuf, &counters,
@@ -111,12 +113,12 @@ struct Server {
   uint64_t next_id = 1;
   std::mutex mu;
   std::condition_variable cv_work, cv_done, cv_slot;
+  static constexpr int kSlots = 4;   // batches that can be on the device at once
   std::deque<ServeJob*> pending;
   std::unordered_map<uint64_t, ServeJob*> jobs;
-  Slot slots[2];
-  std::deque<int> inflight;   // slot indices in launch order
+  Slot slots[kSlots];
   bool stop = false;
-  std::thread worker, completer;
+  std::thread worker, completer[kSlots];
   int device = 0;
 
   size_t footprint(int n) const {
@@ -125,7 +127,12 @@ struct Server {
 
   int launch_batch(Slot& S);
   void worker_loop();
-  void completer_loop();
+  void completer_loop(int si);
+  int free_slot() const {
+    for (int k = 0; k < kSlots; ++k)
+      if (!slots[k].busy) return k;
+    return -1;
+  }
 };
 
 // Build the multi-job plan of the slot's batch and queue all its work.
@@ -350,10 +357,10 @@ void Server::worker_loop() {
   cudaSetDevice(device);
   std::unique_lock<std::mutex> lk(mu);
   for (;;) {
-    cv_work.wait(lk, [&] { return stop || (!pending.empty() && (!slots[0].busy || !slots[1].busy)); });
+    cv_work.wait(lk, [&] { return stop || (!pending.empty() && free_slot() >= 0); });
     if (stop) return;
-    Slot& S = !slots[0].busy ? slots[0] : slots[1];
-    const int si = &S == &slots[0] ? 0 : 1;
+    const int si = free_slot();
+    Slot& S = slots[si];
     S.batch.clear();
     const double now = clock_ms();
     // first come, first served: stop at the first job that does not fit
@@ -389,24 +396,25 @@ void Server::worker_loop() {
       cv_done.notify_all();
       continue;
     }
-    inflight.push_back(si);
+    S.launched = true;
     cv_slot.notify_all();
   }
 }
 
-void Server::completer_loop() {
+// One completion thread per slot: each waits for its own slot's batch, so a
+// short batch is handed back while a longer one is still on the device.
+void Server::completer_loop(int si) {
   cudaSetDevice(device);
+  Slot& S = slots[si];
   std::unique_lock<std::mutex> lk(mu);
   for (;;) {
-    cv_slot.wait(lk, [&] { return stop || !inflight.empty(); });
-    if (inflight.empty() && stop) return;
-    const int si = inflight.front();
-    Slot& S = slots[si];
+    cv_slot.wait(lk, [&] { return stop || S.launched; });
+    if (!S.launched && stop) return;
     lk.unlock();
     const cudaError_t e = cudaEventSynchronize(S.done);
     const double now = clock_ms();
     lk.lock();
-    inflight.pop_front();
+    S.launched = false;
     const char* hj = (const char*)S.h_joins.p;
     size_t jo = 0;
     for (ServeJob* J : S.batch) {
@@ -467,7 +475,7 @@ int nwg_server_create(int gap_open, int gap_ext, int64_t hbm_budget_bytes, int m
     }
   }
   s->worker = std::thread([s] { s->worker_loop(); });
-  s->completer = std::thread([s] { s->completer_loop(); });
+  for (int k = 0; k < Server::kSlots; ++k) s->completer[k] = std::thread([s, k] { s->completer_loop(k); });
   *out = reinterpret_cast<nwg_server*>(s);
   return NWG_OK;
 }
@@ -551,8 +559,8 @@ int nwg_server_destroy(nwg_server* srv) {
   s->cv_work.notify_all();
   s->cv_slot.notify_all();
   s->worker.join();
-  // let the completion thread drain what is in flight
-  s->completer.join();
+  // the completion threads drain what is in flight
+  for (auto& t : s->completer) t.join();
   for (auto& S : s->slots) cudaStreamSynchronize(S.stream);
   for (auto& kv : s->jobs) delete kv.second;
   nwg_ctx* c = reinterpret_cast<nwg_ctx*>(s->ctx);
