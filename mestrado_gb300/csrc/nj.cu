@@ -91,8 +91,8 @@ struct NJDev {
   nwg_join* joins;
   float* vd;           // per slot, new row values
   float* rmin;         // per slot: smallest float q of the row's pairs (c > r) in this join
-  float* rmax;         // per slot: largest magnitude of those pairs' terms (large-n path)
-  int n0;
+  int n0;              // slots
+  int ld;              // row stride of D (floats)
   int cand_cap;        // candidate list capacity
 };
 
@@ -174,7 +174,7 @@ __global__ void rowsum_kernel(NJDev s) {
   const int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (k >= na) return;
   const int sk = s.slot[s.act[k]];
-  const float* row = s.D + (size_t)sk * s.n0;
+  const float* row = s.D + (size_t)sk * s.ld;
   double part = 0.0, ab = 0.0;
   int lowexp = INT_MAX;
   for (int j = lane; j < na; j += 32) {
@@ -199,104 +199,97 @@ __global__ void rowsum_kernel(NJDev s) {
   }
 }
 
-// Pass 1: minimum float q and largest magnitude over the live triangle
-// (row slot r, column slots c > r).
-__global__ void __launch_bounds__(256) pass_min_kernel(NJDev s, float nm2f) {
-  if ((int)blockIdx.x >= *s.na) return;
-  const int r = s.slot[s.act[blockIdx.x]];
-  const float tr = s.Tf[r];
-  const float* row = s.D + (size_t)r * s.n0;
-  float qmin = FLT_MAX, mmax = 0.f;
-#pragma unroll 8
-  for (int c = r + 1 + threadIdx.x; c < s.n0; c += blockDim.x) {
-    if (s.node[c] < 0) continue;
-    const float d = row[c];
-    const float tc = s.Tf[c];
-    const float x = __fmul_rn(d, nm2f);
-    const float q = __fsub_rn(__fsub_rn(x, tr), tc);
-    qmin = fminf(qmin, q);
-    mmax = fmaxf(mmax, __fadd_rn(__fadd_rn(fabsf(x), fabsf(tr)), fabsf(tc)));
+// Winner among the candidates and the ambiguity / tie counts, by one warp
+// (the list holds a few entries); every lane returns the same result.  The
+// count and the first 32 entries are loaded together.
+struct PickOut {
+  int idx;          // the winner's position in the list
+  unsigned ties, amb;
+  bool error;       // no candidate, or the list overflowed
+};
+
+template <class C>
+__device__ PickOut pick_warp(const C* cand, const int* count, int cap) {
+  const int l = threadIdx.x & 31;
+  const int ncount = *count;
+  C first{};
+  if (l < cap) first = cand[l];
+  const int nc = min(ncount, cap);
+  // the reduction carries the heap rounding q2 of the best entry with it
+  double bq = DBL_MAX, bq2 = DBL_MAX;
+  int ba = INT_MAX, bb = -1, bi = -1;
+  for (int k = l; k < nc; k += 32) {
+    const C c = k == l ? first : cand[k];
+    if (better(c.q1, c.b, c.a, bq, bb, ba)) {
+      bq = c.q1;
+      bq2 = c.q2;
+      ba = c.a;
+      bb = c.b;
+      bi = k;
+    }
   }
   for (int o = 16; o > 0; o >>= 1) {
-    qmin = fminf(qmin, __shfl_down_sync(0xffffffffu, qmin, o));
-    mmax = fmaxf(mmax, __shfl_down_sync(0xffffffffu, mmax, o));
-  }
-  __shared__ float sq[8], sm[8];
-  if ((threadIdx.x & 31) == 0) {
-    sq[threadIdx.x >> 5] = qmin;
-    sm[threadIdx.x >> 5] = mmax;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
-      qmin = fminf(qmin, sq[w]);
-      mmax = fmaxf(mmax, sm[w]);
+    const double q = __shfl_xor_sync(0xffffffffu, bq, o);
+    const double q2 = __shfl_xor_sync(0xffffffffu, bq2, o);
+    const int a2 = __shfl_xor_sync(0xffffffffu, ba, o);
+    const int b2 = __shfl_xor_sync(0xffffffffu, bb, o);
+    const int i2 = __shfl_xor_sync(0xffffffffu, bi, o);
+    if (better(q, b2, a2, bq, bb, ba)) {
+      bq = q;
+      bq2 = q2;
+      ba = a2;
+      bb = b2;
+      bi = i2;
     }
-    s.rmin[r] = qmin;   // the step kernel reduces these (no contended atomics here)
-    s.rmax[r] = mmax;
   }
+  // every lane now holds the winner (the order is total: q, then ids)
+  const double hiw = fmax(bq, bq2);
+  const bool robust_w = bq == bq2;
+  unsigned ties = 0, amb = 0;
+  for (int k = l; k < nc; k += 32) {
+    const C c = k == l ? first : cand[k];
+    const double lo = fmin(c.q1, c.q2);
+    if (lo > hiw) continue;
+    if (c.a == ba && c.b == bb) ++ties;
+    else if (robust_w && c.q1 == c.q2 && c.q1 == bq) ++ties;
+    else ++amb;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    ties += __shfl_xor_sync(0xffffffffu, ties, o);
+    amb += __shfl_xor_sync(0xffffffffu, amb, o);
+  }
+  PickOut r;
+  r.idx = bi;
+  r.ties = ties;
+  r.amb = amb;
+  r.error = bb < 0 || ncount > cap;
+  return r;
 }
 
-// Winner among the candidates, ambiguity and tie count; resets the pass
-// accumulators for the next join.  Warp 0 of the CTA does the work (the list
-// holds a few entries: double-precision work on every warp would only load
-// the FP64 pipe); the other warps wait at the final barrier.
+// The pick's statistics: ambiguous step, tie step or internal error.
+__device__ __forceinline__ void record_pick(const NJDev& s, const PickOut& r) {
+  if (r.error) atomicAdd(&s.stats[2], 1ull);
+  else if (r.amb > 0 || r.ties > 4) atomicAdd(&s.stats[0], 1ull);
+  else if (r.ties > 1) atomicAdd(&s.stats[1], 1ull);
+}
+
+// Per-CTA form: warp 0 picks, records and resets the candidate count; the
+// other warps wait at the final barrier.
 __device__ void pick_body(const NJDev& s) {
   if (threadIdx.x < 32) {
-    const int l = threadIdx.x;
-    const int nc = min(s.g32[2], s.cand_cap);
-    // the reduction carries the heap rounding q2 of the best entry with it
-    double bq = DBL_MAX, bq2 = DBL_MAX;
-    int ba = INT_MAX, bb = -1;
-    for (int k = l; k < nc; k += 32) {
-      const Cand c = s.cand[k];
-      if (better(c.q1, c.b, c.a, bq, bb, ba)) {
-        bq = c.q1;
-        bq2 = c.q2;
-        ba = c.a;
-        bb = c.b;
+    const PickOut r = pick_warp(s.cand, &s.g32[2], s.cand_cap);
+    if (threadIdx.x == 0) {
+      Pick w;
+      w.b = -1;
+      if (!r.error) {
+        const Cand c = s.cand[r.idx];
+        w.q1 = c.q1;
+        w.q2 = c.q2;
+        w.a = c.a;
+        w.b = c.b;
       }
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      const double q = __shfl_xor_sync(0xffffffffu, bq, o);
-      const double q2 = __shfl_xor_sync(0xffffffffu, bq2, o);
-      const int a2 = __shfl_xor_sync(0xffffffffu, ba, o);
-      const int b2 = __shfl_xor_sync(0xffffffffu, bb, o);
-      if (better(q, b2, a2, bq, bb, ba)) {
-        bq = q;
-        bq2 = q2;
-        ba = a2;
-        bb = b2;
-      }
-    }
-    // every lane now holds the winner (the order is total: q, then ids)
-    const double hiw = fmax(bq, bq2);
-    const bool robust_w = bq == bq2;
-    unsigned ties = 0, amb = 0;
-    for (int k = l; k < nc; k += 32) {
-      const Cand c = s.cand[k];
-      const double lo = fmin(c.q1, c.q2);
-      if (lo > hiw) continue;
-      if (c.a == ba && c.b == bb) ++ties;
-      else if (robust_w && c.q1 == c.q2 && c.q1 == bq) ++ties;
-      else ++amb;
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      ties += __shfl_xor_sync(0xffffffffu, ties, o);
-      amb += __shfl_xor_sync(0xffffffffu, amb, o);
-    }
-    if (l == 0) {
-      Pick p;
-      p.q1 = bq;
-      p.q2 = bq2;
-      p.a = ba;
-      p.b = bb;
-      *s.win = p;
-      if (bb < 0 || s.g32[2] > s.cand_cap) atomicAdd(&s.stats[2], 1ull);   // no candidate / list overflow
-      else if (amb > 0 || ties > 4) atomicAdd(&s.stats[0], 1ull);
-      else if (ties > 1) atomicAdd(&s.stats[1], 1ull);
-      s.g32[0] = 0x7F7FFFFF;          // ordered-int of FLT_MAX
-      s.g32[1] = 0;
+      *s.win = w;
+      record_pick(s, r);
       s.g32[2] = 0;
     }
   }
@@ -315,7 +308,7 @@ __device__ void join_body(const NJDev& s, int step, int next, int m_n, float* tv
   const int si = s.slot[i], sj = s.slot[j];
   const int n0 = s.n0;
   const int na = *s.na;
-  const float dmin = s.D[(size_t)si * n0 + sj];
+  const float dmin = s.D[(size_t)si * s.ld + sj];
   if (threadIdx.x == 0) {
     // TreeNode::join with left = min id, right = max id (overlaps the loop below)
     const double Ti = s.T[si], Tj = s.T[sj];
@@ -363,16 +356,16 @@ __device__ void join_body(const NJDev& s, int step, int next, int m_n, float* tv
       continue;
     }
     const int sk = s.slot[v];
-    const float Dik = s.D[(size_t)si * n0 + sk];
-    const float Djk = s.D[(size_t)sj * n0 + sk];
+    const float Dik = s.D[(size_t)si * s.ld + sk];
+    const float Djk = s.D[(size_t)sj * s.ld + sk];
     const float sumf = __fadd_rn(Dik, Djk);
     const float tmp = __fmul_rn(__fsub_rn(sumf, dmin), 0.5f);
     tv[k] = tmp;
     const double t = __dadd_rn(s.T[sk], (double)__fsub_rn(tmp, sumf));
     s.T[sk] = t;
     s.Tf[sk] = (float)t;
-    s.D[(size_t)sk * n0 + si] = tmp;
-    s.D[(size_t)si * n0 + sk] = tmp;
+    s.D[(size_t)sk * s.ld + si] = tmp;
+    s.D[(size_t)si * s.ld + sk] = tmp;
     lowexp = min(lowexp, low_bit_exp(tmp));
     topexp = max(topexp, top_bit_exp(tmp));
   }
@@ -468,93 +461,491 @@ __device__ void join_body(const NJDev& s, int step, int next, int m_n, float* tv
   __syncthreads();
 }
 
-// ---- large n: full-GPU first pass, one CTA for the rest of the join --------
-// Per join: pass_min_kernel (one block per live row, every SM) writes the row
-// minima and the global minimum and magnitude; step_kernel (one CTA) scans only
-// the rows whose minimum is within the candidate threshold, picks the winner
-// and applies the join.  At the rebuild steps the matrix is compacted to its
-// live rows and columns, in slot order (so every slot comparison of the
-// record-order rounding is unchanged), after the row sums.
+// ---- large n: one cooperative launch over the whole GPU per rebuild segment --
+// Every CTA takes part in every phase of every join; three grid barriers per
+// join separate the phases:
+//  P  the live triangle, rows dealt to all warps of the grid as folded slot
+//     pairs (16-byte loads: rows are padded to a multiple of 4 floats and the
+//     padding's float row sums are NaN); per row its smallest float q
+//     (grmin), per CTA the smallest q and the largest magnitude (part);
+//  S  every CTA reduces the CTA partials to the candidate threshold, finds the
+//     rows whose minimum is within it and scans its own slice of their
+//     columns; a candidate carries its slots, d and both T values;
+//  J  every CTA takes the same winner from the list and applies the join to
+//     its own share of the slots (T, the new row and column, the new row's
+//     values with their exponent range and integer sum) and of the active
+//     list (shifted into the other list).
+// At the start of the next join (or at the end of the segment) every CTA
+// combines the shares into the new node's row sum and writes it, with the
+// dead slot's NaN and the slot -> node map, itself -- the same values in
+// every CTA, so each CTA reads its own writes; CTA 0 keeps the join record and
+// the id -> slot map.  A dead slot's float row sum is NaN, so its pairs drop
+// out of fminf / fmaxf in P.  Rebuilds (row sums, compaction) run between
+// segments as separate launches.
 
-__global__ void __launch_bounds__(1024) step_kernel(NJDev s, int step, int next, int m_n, int watermark) {
-  extern __shared__ __align__(16) unsigned char st_smem[];
-  float* tv = reinterpret_cast<float*>(st_smem);
-  int* ids = reinterpret_cast<int*>(tv + s.n0);
-  constexpr int kRows = 1024;
-  __shared__ int rows[kRows];
-  __shared__ int nrows;
-  const double nm2 = (double)(m_n - 2);
-  const float nm2f = (float)(m_n - 2);
-  __shared__ float red_q[32], red_m[32];
-  // the global minimum and magnitude from the rows' values
+struct GCand {
+  double q1, q2;   // record-order and heap rounding of q
+  double ta, tb;   // T of the slots of a and b
+  int a, b;        // node ids, a < b
+  int sa, sb;      // their slots
+  float d;
+  int pad;
+};
+
+struct GridNJ {
+  unsigned* bar;        // [0] barrier arrivals (counts up from 0 per launch)
+  int* abort;           // set when a barrier wait gave up; every CTA then leaves
+  int* act2;            // the other active list (the join writes the shifted list there)
+  int* grmin;           // per slot: smallest float q of the row's pairs (ordered int)
+  float* tv;            // per slot: the new row's value
+  float* part;          // [2 * grid]: per CTA smallest q and largest magnitude
+  long long* jsum;      // [2 * grid]: per CTA integer sum and sum of magnitudes (units of 2^jexp)
+  int* jexp;            // [2 * grid]: per CTA lowest and highest exponent of its values
+  GCand* cand;
+};
+
+constexpr long long kBarrierSpinCycles = 4000000000ll;   // about two seconds: no phase takes a millisecond
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void red_release_add(unsigned* p, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Grid barrier of a cooperative launch (all CTAs resident): arrivals count up,
+// the k-th barrier waits for k * gridDim.x arrivals.  A wait that exceeds the
+// spin limit, or sees another CTA's abort, sets the abort flag and returns
+// false; the caller then leaves the kernel.
+__device__ bool grid_barrier(const GridNJ& g, unsigned& target) {
+  __shared__ int s_ok;
+  __syncthreads();
+  target += gridDim.x;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    red_release_add(&g.bar[0], 1u);
+    int ok = 1;
+    const long long t0 = clock64();
+    while ((int)(ld_acquire_u32(&g.bar[0]) - target) < 0) {
+      if (*(volatile int*)g.abort) {
+        ok = 0;
+        break;
+      }
+      if (clock64() - t0 > kBarrierSpinCycles) {
+        atomicExch(g.abort, 1);
+        ok = 0;
+        break;
+      }
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+__device__ __forceinline__ void pass_elem(float d, float tc, float tr, float nm2f, float& rq, float& mmax) {
+  const float x = __fmul_rn(d, nm2f);
+  const float q = __fsub_rn(__fsub_rn(x, tr), tc);   // NaN at a dead or padding slot: drops out
+  rq = fminf(rq, q);
+  mmax = fmaxf(mmax, __fadd_rn(__fadd_rn(fabsf(x), fabsf(tr)), fabsf(tc)));
+}
+
+// P.  Warps are numbered across CTAs first, so consecutive pairs land on
+// different SMs; with fewer pairs than warps a pair is split over f warps,
+// each taking every f-th group of 32 vectors (the row minimum then meets in
+// grmin by atomicMin).
+__device__ void grid_pass(const NJDev& s, const GridNJ& g, float nm2f) {
+  __shared__ float sq[32], sm[32];
+  const int lane = threadIdx.x & 31;
+  const int n0 = s.n0, nv = s.ld >> 2;
+  const int nw = (int)gridDim.x * (int)(blockDim.x >> 5);
+  const int npairs = (n0 + 1) >> 1;
+  int f = 1;
+  while (f < 32 && npairs * (f * 2) <= nw) f *= 2;
+  const int gw = (int)(threadIdx.x >> 5) * (int)gridDim.x + (int)blockIdx.x;
+  const float4* Tf4 = reinterpret_cast<const float4*>(s.Tf);
   float qmin = FLT_MAX, mmax = 0.f;
-  for (int p = threadIdx.x; p < s.n0; p += blockDim.x) {
-    if (s.node[p] >= 0) {
-      qmin = fminf(qmin, s.rmin[p]);
-      mmax = fmaxf(mmax, s.rmax[p]);
+  for (int u = gw; u < npairs * f; u += nw) {
+    const int p = u / f, share = u - p * f;
+    for (int h = 0; h < 2; ++h) {
+      const int r = h ? n0 - 1 - p : p;
+      if (h && r == p) break;
+      const float tr = s.Tf[r];
+      if (tr != tr) continue;   // dead slot
+      const float* row = s.D + (size_t)r * s.ld;
+      float rq = FLT_MAX;
+      const int c0 = r + 1, v0 = (c0 + 3) >> 2;
+      // columns c0 .. 4*v0-1 (at most three) one by one
+      if (share == 0 && lane < 4 * v0 - c0 && c0 + lane < n0) pass_elem(row[c0 + lane], s.Tf[c0 + lane], tr, nm2f, rq, mmax);
+      const float4* row4 = reinterpret_cast<const float4*>(row);
+#pragma unroll 4
+      for (int v = v0 + share * 32 + lane; v < nv; v += f * 32) {
+        const float4 d = row4[v];
+        const float4 tc = Tf4[v];
+        pass_elem(d.x, tc.x, tr, nm2f, rq, mmax);
+        pass_elem(d.y, tc.y, tr, nm2f, rq, mmax);
+        pass_elem(d.z, tc.z, tr, nm2f, rq, mmax);
+        pass_elem(d.w, tc.w, tr, nm2f, rq, mmax);
+      }
+      for (int o = 16; o > 0; o >>= 1) rq = fminf(rq, __shfl_xor_sync(0xffffffffu, rq, o));
+      if (lane == 0) {
+        if (f == 1) g.grmin[r] = ford(rq);
+        else atomicMin(&g.grmin[r], ford(rq));
+      }
+      qmin = fminf(qmin, rq);
     }
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    qmin = fminf(qmin, __shfl_xor_sync(0xffffffffu, qmin, o));
-    mmax = fmaxf(mmax, __shfl_xor_sync(0xffffffffu, mmax, o));
+  for (int o = 16; o > 0; o >>= 1) mmax = fmaxf(mmax, __shfl_xor_sync(0xffffffffu, mmax, o));
+  if (lane == 0) {
+    sq[threadIdx.x >> 5] = qmin;
+    sm[threadIdx.x >> 5] = mmax;
   }
-  if ((threadIdx.x & 31) == 0) {
-    red_q[threadIdx.x >> 5] = qmin;
-    red_m[threadIdx.x >> 5] = mmax;
-  }
-  if (threadIdx.x == 0) nrows = 0;
   __syncthreads();
   if (threadIdx.x < 32) {
-    const int nw = (int)(blockDim.x >> 5);
-    qmin = threadIdx.x < nw ? red_q[threadIdx.x] : FLT_MAX;
-    mmax = threadIdx.x < nw ? red_m[threadIdx.x] : 0.f;
+    const int nwb = (int)(blockDim.x >> 5);
+    qmin = lane < nwb ? sq[lane] : FLT_MAX;
+    mmax = lane < nwb ? sm[lane] : 0.f;
     for (int o = 16; o > 0; o >>= 1) {
       qmin = fminf(qmin, __shfl_xor_sync(0xffffffffu, qmin, o));
       mmax = fmaxf(mmax, __shfl_xor_sync(0xffffffffu, mmax, o));
     }
-    if (threadIdx.x == 0) {
-      red_q[0] = qmin;
-      red_m[0] = mmax;
+    if (lane == 0) {
+      g.part[2 * blockIdx.x] = qmin;
+      g.part[2 * blockIdx.x + 1] = mmax;
+    }
+  }
+}
+
+// S: the threshold from the CTA partials, the rows within it, and this CTA's
+// slice of their columns into the candidate list.
+__device__ void grid_cand(const NJDev& s, const GridNJ& g, float nm2f, double nm2, int watermark) {
+  constexpr int kRows = 512;
+  __shared__ int rows[kRows];
+  __shared__ int nrows;
+  __shared__ float sthr;
+  const int n0 = s.n0;
+  if (threadIdx.x < 32) {
+    const int l = threadIdx.x;
+    float q = FLT_MAX, m = 0.f;
+    for (int b = l; b < (int)gridDim.x; b += 32) {
+      q = fminf(q, g.part[2 * b]);
+      m = fmaxf(m, g.part[2 * b + 1]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      q = fminf(q, __shfl_xor_sync(0xffffffffu, q, o));
+      m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    }
+    if (l == 0) {
+      sthr = q + 3.f * (8.f * 5.9604645e-8f * m) + 1e-30f;
+      nrows = 0;
     }
   }
   __syncthreads();
-  const float thr = red_q[0] + 3.f * (8.f * 5.9604645e-8f * red_m[0]) + 1e-30f;
-  // live slots whose row minimum is within the threshold (usually one or two)
-  for (int p = threadIdx.x; p < s.n0; p += blockDim.x) {
-    if (s.node[p] >= 0 && s.rmin[p] <= thr) {
+  const float thr = sthr;
+  const int othr = ford(thr);
+  for (int p = threadIdx.x; p < n0; p += blockDim.x) {
+    if (g.grmin[p] <= othr) {
       const int t = atomicAdd(&nrows, 1);
       if (t < kRows) rows[t] = p;
     }
   }
   __syncthreads();
-  const bool all = nrows > kRows;   // more near-minimal rows than the list holds: every live row
-  const int nr = all ? s.n0 : nrows;
-  // each selected row scanned by the whole CTA
+  const bool all = nrows > kRows;   // more near-minimal rows than the list holds: every row
+  const int nr = all ? n0 : nrows;
+  const int cstride = (int)gridDim.x * (int)blockDim.x;
   for (int t = 0; t < nr; ++t) {
     const int r = all ? t : rows[t];
     const int ur = s.node[r];
-    if (ur < 0 || s.rmin[r] > thr) continue;
     const float tr = s.Tf[r];
-    const float* row = s.D + (size_t)r * s.n0;
-    for (int c = r + 1 + (int)threadIdx.x; c < s.n0; c += blockDim.x) {
+    const double Tr = s.T[r];
+    if (ur < 0 || g.grmin[r] > othr) continue;
+    const float* row = s.D + (size_t)r * s.ld;
+    for (int c = r + 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x); c < n0; c += cstride) {
       const int uc = s.node[c];
-      if (uc < 0) continue;
       const float d = row[c];
-      const float q = __fsub_rn(__fsub_rn(__fmul_rn(d, nm2f), tr), s.Tf[c]);
+      const float tcf = s.Tf[c];
+      const double Tc = s.T[c];
+      if (uc < 0) continue;
+      const float q = __fsub_rn(__fsub_rn(__fmul_rn(d, nm2f), tr), tcf);
       if (q > thr) continue;
-      const int a = min(ur, uc), b = max(ur, uc);
-      Cand cd;
-      cd.q1 = q_record(s, d, a, b, watermark, nm2);
-      cd.q2 = q_heap(s, d, a, b, nm2);
-      cd.a = a;
-      cd.b = b;
+      GCand cd;
+      const bool rfirst = ur < uc;
+      cd.a = rfirst ? ur : uc;
+      cd.b = rfirst ? uc : ur;
+      cd.sa = rfirst ? r : c;
+      cd.sb = rfirst ? c : r;
+      cd.ta = rfirst ? Tr : Tc;
+      cd.tb = rfirst ? Tc : Tr;
+      cd.d = d;
+      cd.pad = 0;
+      // record order (SpeciesBlock.cpp:1051): node-id order, except for a
+      // record made when the newer node was inserted (row-slot order)
+      const bool swap = cd.b >= watermark && cd.sb < cd.sa;
+      const double nmd = __dmul_rn((double)d, nm2);
+      cd.q1 = swap ? __dsub_rn(__dsub_rn(nmd, cd.tb), cd.ta) : __dsub_rn(__dsub_rn(nmd, cd.ta), cd.tb);
+      cd.q2 = __dsub_rn(nmd, __dadd_rn(cd.ta, cd.tb));   // heap rounding (:1119-1121)
       const int idx = atomicAdd(&s.g32[2], 1);
-      if (idx < s.cand_cap) s.cand[idx] = cd;
+      if (idx < s.cand_cap) g.cand[idx] = cd;
+    }
+  }
+}
+
+// Block-wide min / max of two ints (every thread gets the result).
+__device__ __forceinline__ void block_minmax(int& lo, int& hi, int* slo, int* shi) {
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    slo[threadIdx.x >> 5] = lo;
+    shi[threadIdx.x >> 5] = hi;
+  }
+  __syncthreads();
+  lo = INT_MAX;
+  hi = INT_MIN;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+    lo = min(lo, slo[w]);
+    hi = max(hi, shi[w]);
+  }
+  __syncthreads();
+}
+
+// J: this CTA's share of the slots (SpeciesBlock.cpp:787-841: tmp = ((Dik +
+// Djk) - d) / 2 in float, T[k] += (float)(tmp - (Dik + Djk)), the new row and
+// column of slot si, whose diagonal keeps i's old value) and of the active
+// list; the share's exponent range and integer sum go to jexp / jsum.
+__device__ void grid_join_share(const NJDev& s, const GridNJ& g, const GCand& w, int na, const int* act, int* act2) {
+  __shared__ int slo[32], shi[32];
+  __shared__ long long ssum[32], sabs[32];
+  const int i = w.a, j = w.b, si = w.sa, sj = w.sb;
+  const float dmin = w.d;
+  const int n0 = s.n0;
+  const size_t ld = (size_t)s.ld;
+  const int per = (n0 + (int)gridDim.x - 1) / (int)gridDim.x;
+  const int p0 = (int)blockIdx.x * per, p1 = min(n0, p0 + per);
+  int lowexp = INT_MAX, topexp = INT_MIN;
+  for (int p = p0 + (int)threadIdx.x; p < p1; p += blockDim.x) {
+    g.grmin[p] = 0x7F7FFFFF;   // the next join's row minima start at +inf (S has read them)
+    const int v = s.node[p];
+    const float Dik = s.D[(size_t)si * ld + p];
+    const float Djk = s.D[(size_t)sj * ld + p];
+    const double Tk = s.T[p];
+    if (v < 0 || p == si || p == sj) continue;
+    const float sumf = __fadd_rn(Dik, Djk);
+    const float tmp = __fmul_rn(__fsub_rn(sumf, dmin), 0.5f);
+    const double t = __dadd_rn(Tk, (double)__fsub_rn(tmp, sumf));
+    s.T[p] = t;
+    s.Tf[p] = (float)t;
+    s.D[(size_t)p * ld + si] = tmp;
+    s.D[(size_t)si * ld + p] = tmp;
+    g.tv[p] = tmp;
+    lowexp = min(lowexp, low_bit_exp(tmp));
+    topexp = max(topexp, top_bit_exp(tmp));
+  }
+  // the active list without i and j (ascending ids), shifted into act2
+  const int kper = (na + (int)gridDim.x - 1) / (int)gridDim.x;
+  const int k0 = (int)blockIdx.x * kper, k1 = min(na, k0 + kper);
+  for (int k = k0 + (int)threadIdx.x; k < k1; k += blockDim.x) {
+    const int v = act[k];
+    if (v != i && v != j) act2[k - (v > i) - (v > j)] = v;
+  }
+  block_minmax(lowexp, topexp, slo, shi);
+  // this share's integer sum in units of its own lowest exponent (used only
+  // when the whole row's range is below 48 bits, so only then needed exact)
+  long long isum = 0, iabs = 0;
+  if (lowexp != INT_MAX && topexp - lowexp < 48) {
+    for (int p = p0 + (int)threadIdx.x; p < p1; p += blockDim.x) {
+      if (s.node[p] < 0 || p == si || p == sj) continue;
+      const long long v = float_units(g.tv[p], lowexp);
+      isum += v;
+      iabs += v < 0 ? -v : v;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    isum += __shfl_xor_sync(0xffffffffu, isum, o);
+    iabs += __shfl_xor_sync(0xffffffffu, iabs, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    ssum[threadIdx.x >> 5] = isum;
+    sabs[threadIdx.x >> 5] = iabs;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    isum = iabs = 0;
+    for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2) {
+      isum += ssum[w2];
+      iabs += sabs[w2];
+    }
+    g.jsum[2 * blockIdx.x] = isum;
+    g.jsum[2 * blockIdx.x + 1] = iabs;
+    g.jexp[2 * blockIdx.x] = lowexp;
+    g.jexp[2 * blockIdx.x + 1] = topexp;
+  }
+}
+
+// After the barrier that ends join `step`: the new node's row sum
+// (SpeciesBlock.cpp:799, :818 -- the sequential double sum in ascending id
+// order, taken as the exact integer sum of the shares when that provably
+// equals it), written by every CTA for itself; CTA 0 also writes the join
+// record (TreeNode::join) and the id -> slot map.  When the integer sum cannot
+// be used, CTA 0 runs the sequential loop and one more grid barrier follows.
+__device__ bool grid_join_apply(const NJDev& s, const GridNJ& g, const GCand& w, const PickOut& pk, int step, int n,
+                                const int* act_old, int* act_new, unsigned& target) {
+  __shared__ double s_sum;
+  __shared__ int s_exact;
+  const int i = w.a, j = w.b, si = w.sa, sj = w.sb;
+  const int m_n = n - step, next = n + step;
+  if (threadIdx.x < 32) {
+    const int l = threadIdx.x;
+    int lowexp = INT_MAX, topexp = INT_MIN;
+    for (int b = l; b < (int)gridDim.x; b += 32) {
+      lowexp = min(lowexp, g.jexp[2 * b]);
+      topexp = max(topexp, g.jexp[2 * b + 1]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      lowexp = min(lowexp, __shfl_xor_sync(0xffffffffu, lowexp, o));
+      topexp = max(topexp, __shfl_xor_sync(0xffffffffu, topexp, o));
+    }
+    // every value below 2^49 units of 2^lowexp: a share's sum (at most 8192
+    // values) moved to those units stays below 2^62
+    const bool fits = lowexp == INT_MAX || topexp - lowexp < 48;
+    long long isum = 0, iabs = 0;
+    if (fits && lowexp != INT_MAX) {
+      for (int b = l; b < (int)gridDim.x; b += 32) {
+        const int e = g.jexp[2 * b];
+        if (e == INT_MAX) continue;   // a share without values
+        const long long m = 1ll << (e - lowexp);
+        isum += g.jsum[2 * b] * m;
+        iabs += g.jsum[2 * b + 1] * m;
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        isum += __shfl_xor_sync(0xffffffffu, isum, o);
+        iabs += __shfl_xor_sync(0xffffffffu, iabs, o);
+      }
+    }
+    if (l == 0) {
+      if (lowexp == INT_MAX) {
+        s_sum = 0.0;                                 // every value is zero
+        s_exact = 1;
+      } else if (fits && iabs < (1ll << 53)) {
+        s_sum = ldexp((double)isum, lowexp);         // exact: |isum| < 2^53
+        s_exact = 1;
+      } else {
+        s_exact = 0;
+      }
     }
   }
   __syncthreads();
-  pick_body(s);
-  join_body(s, step, next, m_n, tv, ids);
+  const bool exact = s_exact != 0;
+  if (threadIdx.x == 0) {
+    if (exact) {
+      s.T[si] = s_sum;
+      s.Tf[si] = (float)s_sum;
+    } else if (blockIdx.x == 0) {
+      double sum = 0.0;   // the reference's loop: active ids ascending, i and j skipped
+      for (int k = 0; k < m_n; ++k) {
+        const int v = act_old[k];
+        if (v != i && v != j) sum = __dadd_rn(sum, (double)g.tv[s.slot[v]]);
+      }
+      s.T[si] = sum;
+      s.Tf[si] = (float)sum;
+    }
+    s.Tf[sj] = __int_as_float(0x7FC00000);   // dead: NaN
+    s.node[sj] = -1;
+    s.node[si] = next;
+    if (blockIdx.x == 0) {
+      const float dmin = w.d;
+      const double Ti = w.ta, Tj = w.tb;
+      double li, lj;
+      const double half = 0.5;
+      if (m_n == 2) {
+        li = lj = __dmul_rn((double)dmin, half);
+      } else {
+        const double nm2 = (double)(m_n - 2);
+        li = __dmul_rn(half, __dadd_rn((double)dmin, __ddiv_rn(__dsub_rn(Ti, Tj), nm2)));
+        lj = __dmul_rn(half, __dadd_rn((double)dmin, __ddiv_rn(__dsub_rn(Tj, Ti), nm2)));
+      }
+      if (li < 0.0) {
+        lj = __dsub_rn(lj, li);
+        li = 0.0;
+      } else if (lj < 0.0) {
+        li = __dsub_rn(li, lj);
+        lj = 0.0;
+      }
+      nwg_join& J = s.joins[step];
+      J.i = i;
+      J.j = j;
+      J.node = next;
+      J.n = m_n;
+      J.d = dmin;
+      J.pad = 0.f;
+      J.q = w.q1;
+      J.ti = Ti;
+      J.tj = Tj;
+      J.len_i = li;
+      J.len_j = lj;
+      act_new[m_n - 2] = next;
+      *s.na = m_n - 1;
+      s.slot[j] = -1;
+      s.slot[i] = -1;
+      s.slot[next] = si;
+      s.g32[2] = 0;   // every CTA took its pick before the barrier
+      record_pick(s, pk);
+    }
+  }
+  if (!exact) return grid_barrier(g, target);   // T[si] from CTA 0
+  __syncthreads();
+  return true;
+}
+
+// Joins step0 .. step1-1 of an n-taxon job (no rebuild among them; the
+// active count before join t is n - t).
+__global__ void __launch_bounds__(1024, 1) nj_grid_kernel(NJDev s, GridNJ g, int step0, int step1, int n,
+                                                         int watermark) {
+  __shared__ PickOut spick;
+  __shared__ GCand swin;
+  unsigned target = 0;
+  for (int p = (int)(blockIdx.x * blockDim.x + threadIdx.x); p < s.n0; p += (int)(gridDim.x * blockDim.x))
+    g.grmin[p] = 0x7F7FFFFF;   // ordered int of FLT_MAX
+  if (blockIdx.x == 0 && threadIdx.x == 0) s.g32[2] = 0;
+  if (!grid_barrier(g, target)) return;
+  int* act = s.act;
+  int* act2 = g.act2;
+  for (int step = step0; step < step1; ++step) {
+    if (step > step0) {
+      // the previous join's new list is act (swapped below), its old one act2
+      if (!grid_join_apply(s, g, swin, spick, step - 1, n, act2, act, target)) return;
+    }
+    const int m_n = n - step;
+    const float nm2f = (float)(m_n - 2);
+    const double nm2 = (double)(m_n - 2);
+    grid_pass(s, g, nm2f);
+    if (!grid_barrier(g, target)) return;
+    grid_cand(s, g, nm2f, nm2, watermark);
+    if (!grid_barrier(g, target)) return;
+    if (threadIdx.x < 32) {
+      const PickOut r = pick_warp(g.cand, &s.g32[2], s.cand_cap);
+      if (threadIdx.x == 0) {
+        spick = r;
+        if (!r.error) swin = g.cand[r.idx];
+      }
+    }
+    __syncthreads();
+    if (spick.error) {   // the same in every CTA
+      if (blockIdx.x == 0 && threadIdx.x == 0) record_pick(s, spick);
+      return;
+    }
+    grid_join_share(s, g, swin, m_n, act, act2);
+    int* t = act;
+    act = act2;
+    act2 = t;
+    if (!grid_barrier(g, target)) return;
+  }
+  if (step1 > step0) grid_join_apply(s, g, swin, spick, step1 - 1, n, act2, act, target);
 }
 
 // Compaction, part 1 (one CTA): map[p] = new slot of live slot p (ascending),
@@ -605,12 +996,12 @@ __global__ void __launch_bounds__(1024) compact_map_kernel(NJDev s, int* map, do
 }
 
 // Compaction, part 2: D2[map[p]][map[c]] = D[p][c] for live p, c (one block per old row).
-__global__ void __launch_bounds__(256) compact_copy_kernel(NJDev s, const int* map, float* D2, int n2) {
+__global__ void __launch_bounds__(256) compact_copy_kernel(NJDev s, const int* map, float* D2, int ld2) {
   const int p = blockIdx.x;
   const int np = map[p];
   if (np < 0) return;
-  const float* row = s.D + (size_t)p * s.n0;
-  float* out = D2 + (size_t)np * n2;
+  const float* row = s.D + (size_t)p * s.ld;
+  float* out = D2 + (size_t)np * ld2;
   for (int c = threadIdx.x; c < s.n0; c += blockDim.x) {
     const int nc = map[c];
     if (nc >= 0) out[nc] = row[c];
@@ -649,7 +1040,7 @@ __device__ void clu_rowsums(const NJDev& s, int w0, int wstride) {
   const int lane = threadIdx.x & 31;
   for (int k = w0; k < na; k += wstride) {
     const int sk = s.slot[s.act[k]];
-    const float* row = s.D + (size_t)sk * s.n0;
+    const float* row = s.D + (size_t)sk * s.ld;
     double part = 0.0, ab = 0.0;
     int lowexp = INT_MAX;
     for (int j = lane; j < na; j += 32) {
@@ -729,7 +1120,7 @@ __device__ void clu_pass_min(const NJDev& s, float nm2f, const float* __restrict
   float qmin = FLT_MAX, mmax = 0.f;
   for_my_rows(s.n0, snode, rs, [&](int r, int c0, int cstride) {
     const float tr = sTf[r];
-    const float* __restrict__ row = s.D + (size_t)r * s.n0;
+    const float* row = s.D + (size_t)r * s.ld;
     float rq = FLT_MAX;
 #pragma unroll 4
     for (int c = r + 1 + c0 + lane; c < s.n0; c += cstride) {
@@ -779,7 +1170,7 @@ __device__ void clu_pass_cand(const NJDev& s, float nm2f, double nm2, int waterm
     if (iord_s(srmin[r]) > thr) return;   // no pair of this row is a candidate
     const int ur = snode[r];
     const float tr = sTf[r];
-    const float* __restrict__ row = s.D + (size_t)r * s.n0;
+    const float* row = s.D + (size_t)r * s.ld;
     for (int c = r + 1 + c0 + lane; c < s.n0; c += cstride) {
       const float d = row[c];
       const int uc = snode[c];
@@ -901,11 +1292,12 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_cluster_
 }  // namespace
 
 struct NJState {
-  DevBuf D, T, Tf, slot, node, act, na, g32, cand, win, stats, joins, vd, rmin;
-  DevBuf D2, T2, Tf2, node2, map, desc, rmax;   // large-n path: compaction buffers, row magnitudes
+  DevBuf D, T, Tf, slot, node, act, na, g32, cand, win, stats, joins, vd, rmin, desc;
+  // large-n path: compaction buffers, second active list, grid partials and barrier words
+  DevBuf D2, T2, Tf2, node2, map, act2, part, jsum, jexp, gbar;
   ~NJState() {
-    for (DevBuf* b : {&D, &T, &Tf, &slot, &node, &act, &na, &g32, &cand, &win, &stats, &joins, &vd, &rmin, &D2, &T2,
-                      &Tf2, &node2, &map, &desc, &rmax})
+    for (DevBuf* b : {&D, &T, &Tf, &slot, &node, &act, &na, &g32, &cand, &win, &stats, &joins, &vd, &rmin, &desc, &D2,
+                      &T2, &Tf2, &node2, &map, &act2, &part, &jsum, &jexp, &gbar})
       b->release();
   }
 };
@@ -941,22 +1333,27 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
   const int nn = 2 * n - 1;
   const bool big = n > cluster_nj_max_n();
   int rc;
-  if ((rc = S.D.ensure(sizeof(float) * (size_t)n * n)) || (rc = S.T.ensure(sizeof(double) * n)) ||
-      (rc = S.Tf.ensure(sizeof(float) * n)) || (rc = S.slot.ensure(sizeof(int) * nn)) ||
+  // the large-n path pads rows to a multiple of 4 floats (16-byte loads)
+  const int ldd = big ? (n + 3) & ~3 : n;
+  if ((rc = S.D.ensure(sizeof(float) * (size_t)n * ldd)) || (rc = S.T.ensure(sizeof(double) * n)) ||
+      (rc = S.Tf.ensure(sizeof(float) * ldd)) || (rc = S.slot.ensure(sizeof(int) * nn)) ||
       (rc = S.node.ensure(sizeof(int) * n)) || (rc = S.act.ensure(sizeof(int) * (n + 1))) ||
       (rc = S.na.ensure(sizeof(int))) || (rc = S.g32.ensure(sizeof(int) * 4)) ||
-      (rc = S.cand.ensure(sizeof(Cand) * kCandCap)) || (rc = S.win.ensure(sizeof(Pick))) ||
+      (rc = S.cand.ensure(std::max(sizeof(Cand), sizeof(GCand)) * kCandCap)) || (rc = S.win.ensure(sizeof(Pick))) ||
       (rc = S.stats.ensure(sizeof(unsigned long long) * 5)) ||
       (rc = S.joins.ensure(sizeof(nwg_join) * (n - 1))) || (rc = S.vd.ensure(sizeof(float) * n)) ||
       (rc = S.rmin.ensure(sizeof(float) * n)) || (rc = S.desc.ensure(sizeof(NJJob))))
     return fail(rc, "nj allocation");
-  if (big && ((rc = S.D2.ensure(sizeof(float) * (size_t)n * n)) || (rc = S.T2.ensure(sizeof(double) * n)) ||
-              (rc = S.Tf2.ensure(sizeof(float) * n)) || (rc = S.node2.ensure(sizeof(int) * n)) ||
-              (rc = S.map.ensure(sizeof(int) * n)) || (rc = S.rmax.ensure(sizeof(float) * n))))
+  const int grid = sms;   // one CTA of 1024 threads per SM (cooperative launch)
+  if (big && ((rc = S.D2.ensure(sizeof(float) * (size_t)n * ldd)) || (rc = S.T2.ensure(sizeof(double) * n)) ||
+              (rc = S.Tf2.ensure(sizeof(float) * ldd)) || (rc = S.node2.ensure(sizeof(int) * n)) ||
+              (rc = S.map.ensure(sizeof(int) * n)) || (rc = S.act2.ensure(sizeof(int) * (n + 1))) ||
+              (rc = S.part.ensure(sizeof(float) * 2 * grid)) || (rc = S.jsum.ensure(sizeof(long long) * 2 * grid)) ||
+              (rc = S.jexp.ensure(sizeof(int) * 2 * grid)) || (rc = S.gbar.ensure(sizeof(int) * 4))))
     return fail(rc, "nj allocation");
   cudaStream_t s = stream;
   const cudaMemcpyKind kind = device_D ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-  if ((rc = cuda(cudaMemcpy2DAsync(S.D.p, sizeof(float) * n, D, sizeof(float) * ld, sizeof(float) * n, n, kind, s),
+  if ((rc = cuda(cudaMemcpy2DAsync(S.D.p, sizeof(float) * ldd, D, sizeof(float) * ld, sizeof(float) * n, n, kind, s),
                  "nj upload")))
     return rc;
   NJDev d{};
@@ -974,8 +1371,8 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
   d.joins = (nwg_join*)S.joins.p;
   d.vd = (float*)S.vd.p;
   d.rmin = (float*)S.rmin.p;
-  d.rmax = big ? (float*)S.rmax.p : nullptr;
   d.n0 = n;
+  d.ld = ldd;
   d.cand_cap = kCandCap;
   if (!big) {
     NJJob J{};
@@ -999,57 +1396,93 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
         (rc = cuda(cudaMemsetAsync(S.stats.p, 0, sizeof(unsigned long long) * 5, s), "nj upload")) ||
         (rc = cuda(cudaStreamSynchronize(s), "nj upload")))   // the host vectors above are local
       return rc;
-    const size_t step_smem = 2 * sizeof(float) * (size_t)n;
-    if ((rc = cuda(cudaFuncSetAttribute(step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)step_smem),
-                   "nj smem")))
+    int blocks_per_sm = 0;
+    if ((rc = cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, nj_grid_kernel, 1024, 0),
+                   "nj occupancy")))
       return rc;
+    if (blocks_per_sm < 1) return fail(NWG_ERR_CUDA, "neighbor-joining grid kernel does not fit an SM");
     float* Dalt = (float*)S.D2.p;
     double* Talt = (double*)S.T2.p;
     float* Tfalt = (float*)S.Tf2.p;
     int* nodealt = (int*)S.node2.p;
+    GridNJ g{};
+    g.bar = (unsigned*)S.gbar.p;
+    g.abort = (int*)S.gbar.p + 2;
+    g.act2 = (int*)S.act2.p;
+    g.grmin = (int*)S.rmin.p;
+    g.tv = (float*)S.vd.p;
+    g.part = (float*)S.part.p;
+    g.jsum = (long long*)S.jsum.p;
+    g.jexp = (int*)S.jexp.p;
+    g.cand = (GCand*)S.cand.p;
+    // NaN (all bits set) float row sums at the padding slots; rowsum_kernel
+    // fills the live ones
+    if ((rc = cuda(cudaMemsetAsync(S.gbar.p, 0, sizeof(int) * 4, s), "nj upload")) ||
+        (rc = cuda(cudaMemsetAsync(S.Tf.p, 0xFF, sizeof(float) * ldd, s), "nj upload")))
+      return rc;
     if (st) cudaEventRecord(ev0, s);
     rowsum_kernel<<<(n + 7) / 8, 256, 0, s>>>(d);
     ++launches;
-    // host-side schedule (deterministic in n, as the reference's)
+    // The reference's schedule (deterministic in n): rebuild after
+    // max(n*0.5, 200) joins, then every m*0.5 joins, none below 200 active
+    // nodes; the joins between two rebuilds are one cooperative launch.
     const int kBinT = 30 * 31 / 2;
     int steps = std::max((int)((float)n * 0.5f), 200);
     int pq_ck = 500;
     long long ave0 = (((long long)(n - 1) * n) / 2) / kBinT;
     long long ub = ((long long)n * (n - 1)) / 2;
-    int watermark = n, next = n, m_n = n, na = n;
-    for (int step = 0; step < n - 1; ++step) {
-      pass_min_kernel<<<na, 256, 0, s>>>(d, (float)(m_n - 2));
-      step_kernel<<<1, 1024, step_smem, s>>>(d, step, next, m_n, watermark);
-      launches += 2;
-      if (--pq_ck == 0) {
-        pq_ck = 500;
-        if (steps > 0) {
-          const double r = (double)(ub / kBinT) / (double)ave0;
-          if (r > 2.0) ++stats.pq_trigger_open;
+    int watermark = n, m_n = n;
+    int step = 0;
+    while (step < n - 1) {
+      // the segment ends with the join after which the countdown reaches 0
+      const int seg_end = steps == INT_MAX ? n - 1 : std::min(n - 1, step + steps + 1);
+      if ((rc = cuda(cudaMemsetAsync(S.gbar.p, 0, sizeof(unsigned) * 2, s), "nj launch"))) return rc;
+      {
+        int a0 = step, a1 = seg_end, an = n, aw = watermark;
+        void* args[] = {&d, &g, &a0, &a1, &an, &aw};
+        if ((rc = cuda(cudaLaunchCooperativeKernel((const void*)nj_grid_kernel, dim3(grid), dim3(1024), args, 0, s),
+                       "nj launch")))
+          return rc;
+        ++launches;
+      }
+      if ((seg_end - step) & 1) std::swap(d.act, g.act2);   // each join writes the other list
+      bool rebuild = false;
+      for (; step < seg_end; ++step) {
+        if (--pq_ck == 0) {
+          pq_ck = 500;
+          if (steps > 0) {
+            const double r = (double)(ub / kBinT) / (double)ave0;
+            if (r > 2.0) ++stats.pq_trigger_open;
+          }
+        }
+        --m_n;
+        if (steps == 0) {
+          rebuild = true;
+        } else {
+          if (steps != INT_MAX) --steps;
+          ub += m_n - 1;
         }
       }
-      --m_n;
-      na -= 1;
-      ++next;
-      if (steps == 0) {
+      if (rebuild) {
+        const int na = m_n;
         rowsum_kernel<<<(na + 7) / 8, 256, 0, s>>>(d);
         // compaction to the live slots, in slot order
+        const int ld2 = (na + 3) & ~3;
+        if ((rc = cuda(cudaMemsetAsync(Tfalt, 0xFF, sizeof(float) * ld2, s), "nj launch"))) return rc;
         compact_map_kernel<<<1, 1024, 0, s>>>(d, (int*)S.map.p, Talt, Tfalt, nodealt, nn);
-        compact_copy_kernel<<<d.n0, 256, 0, s>>>(d, (const int*)S.map.p, Dalt, na);
+        compact_copy_kernel<<<d.n0, 256, 0, s>>>(d, (const int*)S.map.p, Dalt, ld2);
         launches += 3;
         std::swap(d.D, Dalt);
         std::swap(d.T, Talt);
         std::swap(d.Tf, Tfalt);
         std::swap(d.node, nodealt);
         d.n0 = na;
+        d.ld = ld2;
         ++stats.rebuilds;
-        watermark = next;
+        watermark = n + step;
         steps = (m_n < 200) ? INT_MAX : (int)((float)m_n * 0.5f);
         ave0 = (((long long)(m_n - 1) * m_n) / 2) / kBinT;
         ub = ((long long)m_n * (m_n - 1)) / 2;
-      } else {
-        --steps;
-        ub += na - 1;
       }
       if ((rc = cuda(cudaGetLastError(), "nj launch"))) return rc;
     }
@@ -1061,6 +1494,11 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
       (rc = cuda(cudaStreamSynchronize(s), "nj sync")))
     return rc;
   if (dst[2]) return fail(NWG_ERR_CUDA, "neighbor joining candidate list empty or overflowing");
+  if (big) {
+    int gb[4];
+    if ((rc = cuda(cudaMemcpy(gb, S.gbar.p, sizeof(gb), cudaMemcpyDeviceToHost), "nj download"))) return rc;
+    if (gb[2]) return fail(NWG_ERR_CUDA, "neighbor-joining grid barrier timed out");
+  }
   stats.ambiguous_steps = (int64_t)dst[0];
   stats.tie_steps = (int64_t)dst[1];
   if (!big) {
@@ -1111,6 +1549,7 @@ void nj_job_setup(void* job_out, float* D, int n, char* base, nwg_join** joins, 
   J.s.win = (Pick*)p; p += al(sizeof(Pick));
   J.s.joins = (nwg_join*)p;
   J.s.n0 = n;
+  J.s.ld = n;
   J.s.cand_cap = (int)cap;
   J.n = n;
   *joins = J.s.joins;
