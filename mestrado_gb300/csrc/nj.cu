@@ -461,33 +461,39 @@ __device__ void join_body(const NJDev& s, int step, int next, int m_n, float* tv
   __syncthreads();
 }
 
-// ---- large n: one cooperative launch over the whole GPU per rebuild segment --
-// Every CTA takes part in every phase of every join; three grid barriers per
-// join separate the phases:
-//  P  the live triangle, rows dealt to all warps of the grid as folded slot
-//     pairs (16-byte loads: rows are padded to a multiple of 4 floats and the
-//     padding's float row sums are NaN); per row its smallest float q
-//     (grmin), per CTA the smallest q and the largest magnitude (part);
-//  S  every CTA reduces the CTA partials to the candidate threshold, finds the
-//     rows whose minimum is within it and scans its own slice of their
-//     columns; a candidate carries its slots, d and both T values;
-//  J  every CTA takes the same winner from the list and applies the join to
-//     its own share of the slots (T, the new row and column, the new row's
-//     values with their exponent range and integer sum) and of the active
-//     list (shifted into the other list).
+// ---- large n: one cooperative launch over the whole GPU per segment ---------
+// Every CTA takes part in every phase of every join, with two grid barriers
+// per join in the usual case:
+//  P  the live triangle, one row pair (p, n0-1-p) per warp, warps numbered
+//     across CTAs first; 16-byte loads (rows are padded to a multiple of 4
+//     floats and the padding's float row sums are NaN).  Per row its two
+//     smallest float q and the column of the smallest (grmin, grec); per CTA
+//     the smallest q and the largest magnitude (part).
+//  -- barrier --
+//  K  every CTA reduces the CTA partials to the candidate threshold and finds
+//     the rows whose minimum is within it.  When each such row's second
+//     smallest q is beyond the threshold, the candidates are exactly those
+//     rows' minima: every CTA evaluates them (exact q in both roundings) and
+//     takes the same winner.  Otherwise (ties, close pairs) every CTA scans
+//     its slice of the selected rows into a global list and, after one more
+//     barrier, picks from it.
+//  J  every CTA applies the join to its own share of the slots (T, the new
+//     row and column, the new row's values with their exponent range and
+//     integer sum) and of the active list (shifted into the other list).
+//  -- barrier --
 // At the start of the next join (or at the end of the segment) every CTA
 // combines the shares into the new node's row sum and writes it, with the
 // dead slot's NaN and the slot -> node map, itself -- the same values in
-// every CTA, so each CTA reads its own writes; CTA 0 keeps the join record and
-// the id -> slot map.  A dead slot's float row sum is NaN, so its pairs drop
-// out of fminf / fmaxf in P.  Rebuilds (row sums, compaction) run between
-// segments as separate launches.
+// every CTA, so each CTA reads its own writes; CTA 0 keeps the join record
+// (branch lengths are filled in after the loop) and the id -> slot map.
+// Rebuilds (row sums) and compactions run between segments.
 
 struct GCand {
-  double q1, q2;   // record-order and heap rounding of q
-  double ta, tb;   // T of the slots of a and b
-  int a, b;        // node ids, a < b
-  int sa, sb;      // their slots
+  long long k1, k2;   // order-preserving integer keys of q1 and q2
+  double q1;          // record-order rounding of q (SpeciesBlock.cpp:1051)
+  double ta, tb;      // T of the slots of a and b
+  int a, b;           // node ids, a < b
+  int sa, sb;         // their slots
   float d;
   int pad;
 };
@@ -497,14 +503,17 @@ struct GridNJ {
   int* abort;           // set when a barrier wait gave up; every CTA then leaves
   int* act2;            // the other active list (the join writes the shifted list there)
   int* grmin;           // per slot: smallest float q of the row's pairs (ordered int)
+  int2* grec;           // per slot: second smallest q (ordered int), column of the smallest
   float* tv;            // per slot: the new row's value
   float* part;          // [2 * grid]: per CTA smallest q and largest magnitude
   long long* jsum;      // [2 * grid]: per CTA integer sum and sum of magnitudes (units of 2^jexp)
   int* jexp;            // [2 * grid]: per CTA lowest and highest exponent of its values
-  GCand* cand;
+  GCand* cand;          // the candidate list of the fallback scan
 };
 
 constexpr long long kBarrierSpinCycles = 4000000000ll;   // about two seconds: no phase takes a millisecond
+constexpr int kFastRows = 32;                             // candidate rows the direct pick evaluates
+constexpr int kGridMax = 256;                             // CTAs of the cooperative launch, at most
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
   unsigned v;
@@ -547,59 +556,89 @@ __device__ bool grid_barrier(const GridNJ& g, unsigned& target) {
   return s_ok != 0;
 }
 
-__device__ __forceinline__ void pass_elem(float d, float tc, float tr, float nm2f, float& rq, float& mmax) {
-  const float x = __fmul_rn(d, nm2f);
-  const float q = __fsub_rn(__fsub_rn(x, tr), tc);   // NaN at a dead or padding slot: drops out
-  rq = fminf(rq, q);
-  mmax = fmaxf(mmax, __fadd_rn(__fadd_rn(fabsf(x), fabsf(tr)), fabsf(tc)));
+// Order-preserving map double -> int64 (finite values; -0 and +0 map alike).
+__device__ __forceinline__ long long dkey(double q) {
+  long long b = __double_as_longlong(q);
+  if ((b & 0x7FFFFFFFFFFFFFFFll) == 0) b = 0;
+  return b >= 0 ? b : b ^ 0x7FFFFFFFFFFFFFFFll;
 }
 
-// P.  Warps are numbered across CTAs first, so consecutive pairs land on
-// different SMs; with fewer pairs than warps a pair is split over f warps,
-// each taking every f-th group of 32 vectors (the row minimum then meets in
-// grmin by atomicMin).
+// Exact double of u * 2^e (|u| < 2^53, the result a normal double).
+__device__ __forceinline__ double units_to_double(long long u, int e) {
+  if (u == 0) return 0.0;
+  const unsigned long long m = (unsigned long long)(u < 0 ? -u : u);
+  const int msb = 63 - __clzll((long long)m);
+  const unsigned long long bits = ((unsigned long long)(msb + e + 1023) << 52) |
+                                  ((m << (52 - msb)) & 0xFFFFFFFFFFFFFull) | (u < 0 ? (1ull << 63) : 0ull);
+  return __longlong_as_double(bits);
+}
+
+// One element of P: q, the row's two smallest (with the column of the
+// smallest) and the magnitude |x| + |tc| (the row's |tr| is added per row).
+// At a dead or padding slot tc is NaN: q and the magnitude are NaN and drop
+// out (comparisons with NaN are false; fmaxf ignores NaN).
+__device__ __forceinline__ void pass_elem(float d, float tc, int c, float tr, float nm2f, float& m1, float& m2,
+                                          int& c1, float& mag) {
+  const float x = __fmul_rn(d, nm2f);
+  const float q = __fsub_rn(__fsub_rn(x, tr), tc);
+  const bool lt = q < m1;
+  m2 = lt ? m1 : fminf(m2, q);
+  c1 = lt ? c : c1;
+  m1 = lt ? q : m1;
+  mag = fmaxf(mag, __fadd_rn(fabsf(x), fabsf(tc)));
+}
+
 __device__ void grid_pass(const NJDev& s, const GridNJ& g, float nm2f) {
   __shared__ float sq[32], sm[32];
   const int lane = threadIdx.x & 31;
   const int n0 = s.n0, nv = s.ld >> 2;
   const int nw = (int)gridDim.x * (int)(blockDim.x >> 5);
   const int npairs = (n0 + 1) >> 1;
-  int f = 1;
-  while (f < 32 && npairs * (f * 2) <= nw) f *= 2;
-  const int gw = (int)(threadIdx.x >> 5) * (int)gridDim.x + (int)blockIdx.x;
   const float4* Tf4 = reinterpret_cast<const float4*>(s.Tf);
   float qmin = FLT_MAX, mmax = 0.f;
-  for (int u = gw; u < npairs * f; u += nw) {
-    const int p = u / f, share = u - p * f;
+  for (int p = (int)(threadIdx.x >> 5) * (int)gridDim.x + (int)blockIdx.x; p < npairs; p += nw) {
     for (int h = 0; h < 2; ++h) {
       const int r = h ? n0 - 1 - p : p;
       if (h && r == p) break;
       const float tr = s.Tf[r];
       if (tr != tr) continue;   // dead slot
       const float* row = s.D + (size_t)r * s.ld;
-      float rq = FLT_MAX;
+      float m1 = FLT_MAX, m2 = FLT_MAX, mag = 0.f;
+      int c1 = -1;
       const int c0 = r + 1, v0 = (c0 + 3) >> 2;
       // columns c0 .. 4*v0-1 (at most three) one by one
-      if (share == 0 && lane < 4 * v0 - c0 && c0 + lane < n0) pass_elem(row[c0 + lane], s.Tf[c0 + lane], tr, nm2f, rq, mmax);
+      if (lane < 4 * v0 - c0 && c0 + lane < n0)
+        pass_elem(row[c0 + lane], s.Tf[c0 + lane], c0 + lane, tr, nm2f, m1, m2, c1, mag);
       const float4* row4 = reinterpret_cast<const float4*>(row);
 #pragma unroll 4
-      for (int v = v0 + share * 32 + lane; v < nv; v += f * 32) {
+      for (int v = v0 + lane; v < nv; v += 32) {
         const float4 d = row4[v];
         const float4 tc = Tf4[v];
-        pass_elem(d.x, tc.x, tr, nm2f, rq, mmax);
-        pass_elem(d.y, tc.y, tr, nm2f, rq, mmax);
-        pass_elem(d.z, tc.z, tr, nm2f, rq, mmax);
-        pass_elem(d.w, tc.w, tr, nm2f, rq, mmax);
+        pass_elem(d.x, tc.x, 4 * v, tr, nm2f, m1, m2, c1, mag);
+        pass_elem(d.y, tc.y, 4 * v + 1, tr, nm2f, m1, m2, c1, mag);
+        pass_elem(d.z, tc.z, 4 * v + 2, tr, nm2f, m1, m2, c1, mag);
+        pass_elem(d.w, tc.w, 4 * v + 3, tr, nm2f, m1, m2, c1, mag);
       }
-      for (int o = 16; o > 0; o >>= 1) rq = fminf(rq, __shfl_xor_sync(0xffffffffu, rq, o));
+      // the row's two smallest over the warp (an equal pair makes m2 = m1)
+      for (int o = 16; o > 0; o >>= 1) {
+        const float om1 = __shfl_xor_sync(0xffffffffu, m1, o);
+        const float om2 = __shfl_xor_sync(0xffffffffu, m2, o);
+        const int oc1 = __shfl_xor_sync(0xffffffffu, c1, o);
+        const bool take = om1 < m1 || (om1 == m1 && oc1 < c1);
+        const float lo = take ? om1 : m1, hi = take ? m1 : om1;
+        m2 = fminf(hi, fminf(m2, om2));
+        m1 = lo;
+        c1 = take ? oc1 : c1;
+        mag = fmaxf(mag, __shfl_xor_sync(0xffffffffu, mag, o));
+      }
       if (lane == 0) {
-        if (f == 1) g.grmin[r] = ford(rq);
-        else atomicMin(&g.grmin[r], ford(rq));
+        g.grmin[r] = ford(m1);
+        g.grec[r] = make_int2(ford(m2), c1);
       }
-      qmin = fminf(qmin, rq);
+      qmin = fminf(qmin, m1);
+      mmax = fmaxf(mmax, __fadd_rn(mag, fabsf(tr)));
     }
   }
-  for (int o = 16; o > 0; o >>= 1) mmax = fmaxf(mmax, __shfl_xor_sync(0xffffffffu, mmax, o));
   if (lane == 0) {
     sq[threadIdx.x >> 5] = qmin;
     sm[threadIdx.x >> 5] = mmax;
@@ -620,13 +659,91 @@ __device__ void grid_pass(const NJDev& s, const GridNJ& g, float nm2f) {
   }
 }
 
-// S: the threshold from the CTA partials, the rows within it, and this CTA's
-// slice of their columns into the candidate list.
-__device__ void grid_cand(const NJDev& s, const GridNJ& g, float nm2f, double nm2, int watermark) {
-  constexpr int kRows = 512;
-  __shared__ int rows[kRows];
-  __shared__ int nrows;
-  __shared__ float sthr;
+// A candidate from its pair: slots r, c with their node ids, T and d.
+__device__ __forceinline__ GCand make_cand(int r, int c, int ur, int uc, double Tr, double Tc, float d, double nm2,
+                                           int watermark) {
+  GCand cd;
+  const bool rfirst = ur < uc;
+  cd.a = rfirst ? ur : uc;
+  cd.b = rfirst ? uc : ur;
+  cd.sa = rfirst ? r : c;
+  cd.sb = rfirst ? c : r;
+  cd.ta = rfirst ? Tr : Tc;
+  cd.tb = rfirst ? Tc : Tr;
+  cd.d = d;
+  cd.pad = 0;
+  // record order (SpeciesBlock.cpp:1051): node-id order, except for a record
+  // made when the newer node was inserted (row-slot order)
+  const bool swap = cd.b >= watermark && cd.sb < cd.sa;
+  const double nmd = __dmul_rn((double)d, nm2);
+  cd.q1 = swap ? __dsub_rn(__dsub_rn(nmd, cd.tb), cd.ta) : __dsub_rn(__dsub_rn(nmd, cd.ta), cd.tb);
+  cd.k1 = dkey(cd.q1);
+  cd.k2 = dkey(__dsub_rn(nmd, __dadd_rn(cd.ta, cd.tb)));   // heap rounding (:1119-1121)
+  return cd;
+}
+
+// Winner (smallest q1, then larger b, then larger a) and the ambiguity / tie
+// counts over nc candidates, by one warp; load(k) gives candidate k.
+template <class Load>
+__device__ PickOut pick_keys(int nc, Load&& load) {
+  const int l = threadIdx.x & 31;
+  long long bk = LLONG_MAX, bk2 = LLONG_MAX;
+  int ba = INT_MAX, bb = -1, bi = -1;
+  for (int k = l; k < nc; k += 32) {
+    const GCand c = load(k);
+    if (c.k1 < bk || (c.k1 == bk && (c.b > bb || (c.b == bb && c.a > ba)))) {
+      bk = c.k1;
+      bk2 = c.k2;
+      ba = c.a;
+      bb = c.b;
+      bi = k;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const long long q = __shfl_xor_sync(0xffffffffu, bk, o);
+    const long long q2 = __shfl_xor_sync(0xffffffffu, bk2, o);
+    const int a2 = __shfl_xor_sync(0xffffffffu, ba, o);
+    const int b2 = __shfl_xor_sync(0xffffffffu, bb, o);
+    const int i2 = __shfl_xor_sync(0xffffffffu, bi, o);
+    if (q < bk || (q == bk && (b2 > bb || (b2 == bb && a2 > ba)))) {
+      bk = q;
+      bk2 = q2;
+      ba = a2;
+      bb = b2;
+      bi = i2;
+    }
+  }
+  // every lane holds the winner; any other candidate whose smaller rounding
+  // reaches the winner's larger one could have been picked by the reference
+  const long long hiw = max(bk, bk2);
+  const bool robust_w = bk == bk2;
+  unsigned ties = 0, amb = 0;
+  for (int k = l; k < nc; k += 32) {
+    const GCand c = load(k);
+    if (min(c.k1, c.k2) > hiw) continue;
+    if (c.a == ba && c.b == bb) ++ties;
+    else if (robust_w && c.k1 == c.k2 && c.k1 == bk) ++ties;
+    else ++amb;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    ties += __shfl_xor_sync(0xffffffffu, ties, o);
+    amb += __shfl_xor_sync(0xffffffffu, amb, o);
+  }
+  PickOut r;
+  r.idx = bi;
+  r.ties = ties;
+  r.amb = amb;
+  r.error = bb < 0;
+  return r;
+}
+
+// K.  Returns 1 when the winner is in *win, 0 when the fallback scan is
+// needed (the same in every CTA).
+__device__ int grid_pick_direct(const NJDev& s, const GridNJ& g, double nm2, float nm2f, int watermark, GCand* win,
+                                PickOut* pk, float* sthr) {
+  __shared__ int rows[kFastRows];
+  __shared__ GCand fc[kFastRows];
+  __shared__ int nrows, s_ok;
   const int n0 = s.n0;
   if (threadIdx.x < 32) {
     const int l = threadIdx.x;
@@ -640,13 +757,63 @@ __device__ void grid_cand(const NJDev& s, const GridNJ& g, float nm2f, double nm
       m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
     }
     if (l == 0) {
-      sthr = q + 3.f * (8.f * 5.9604645e-8f * m) + 1e-30f;
+      *sthr = q + 3.f * (8.f * 5.9604645e-8f * m) + 1e-30f;
       nrows = 0;
     }
   }
   __syncthreads();
-  const float thr = sthr;
+  const float thr = *sthr;
   const int othr = ford(thr);
+  for (int p = threadIdx.x; p < n0; p += blockDim.x) {
+    if (g.grmin[p] <= othr) {
+      const int t = atomicAdd(&nrows, 1);
+      if (t < kFastRows) rows[t] = p;
+    }
+  }
+  __syncthreads();
+  const int nr = nrows;
+  if (threadIdx.x < 32) {
+    const int l = threadIdx.x;
+    int ok = nr >= 1 && nr <= kFastRows;
+    if (ok && l < nr) {
+      const int r = rows[l];
+      const int2 rec = g.grec[r];
+      const int c = rec.y;
+      if (rec.x <= othr || c < 0) {
+        ok = 0;   // a second pair of the row within the threshold
+      } else {
+        const int ur = s.node[r], uc = s.node[c];
+        const double Tr = s.T[r], Tc = s.T[c];
+        const float d = s.D[(size_t)r * s.ld + c];
+        fc[l] = make_cand(r, c, ur, uc, Tr, Tc, d, nm2, watermark);
+        if (ur < 0 || uc < 0) ok = 0;
+      }
+    }
+    ok = __all_sync(0xffffffffu, ok);
+    PickOut r{};
+    if (ok) r = pick_keys(nr, [&](int k) { return fc[k]; });
+    if (l == 0) {
+      s_ok = ok;
+      if (ok) {
+        *pk = r;
+        *win = fc[r.idx];
+      }
+    }
+  }
+  __syncthreads();
+  return s_ok;
+}
+
+// K, fallback: this CTA's slice of the columns of every row within the
+// threshold into the candidate list.
+__device__ void grid_cand(const NJDev& s, const GridNJ& g, float nm2f, double nm2, int watermark, float thr) {
+  constexpr int kRows = 512;
+  __shared__ int rows[kRows];
+  __shared__ int nrows;
+  const int n0 = s.n0;
+  const int othr = ford(thr);
+  if (threadIdx.x == 0) nrows = 0;
+  __syncthreads();
   for (int p = threadIdx.x; p < n0; p += blockDim.x) {
     if (g.grmin[p] <= othr) {
       const int t = atomicAdd(&nrows, 1);
@@ -672,24 +839,8 @@ __device__ void grid_cand(const NJDev& s, const GridNJ& g, float nm2f, double nm
       if (uc < 0) continue;
       const float q = __fsub_rn(__fsub_rn(__fmul_rn(d, nm2f), tr), tcf);
       if (q > thr) continue;
-      GCand cd;
-      const bool rfirst = ur < uc;
-      cd.a = rfirst ? ur : uc;
-      cd.b = rfirst ? uc : ur;
-      cd.sa = rfirst ? r : c;
-      cd.sb = rfirst ? c : r;
-      cd.ta = rfirst ? Tr : Tc;
-      cd.tb = rfirst ? Tc : Tr;
-      cd.d = d;
-      cd.pad = 0;
-      // record order (SpeciesBlock.cpp:1051): node-id order, except for a
-      // record made when the newer node was inserted (row-slot order)
-      const bool swap = cd.b >= watermark && cd.sb < cd.sa;
-      const double nmd = __dmul_rn((double)d, nm2);
-      cd.q1 = swap ? __dsub_rn(__dsub_rn(nmd, cd.tb), cd.ta) : __dsub_rn(__dsub_rn(nmd, cd.ta), cd.tb);
-      cd.q2 = __dsub_rn(nmd, __dadd_rn(cd.ta, cd.tb));   // heap rounding (:1119-1121)
       const int idx = atomicAdd(&s.g32[2], 1);
-      if (idx < s.cand_cap) g.cand[idx] = cd;
+      if (idx < s.cand_cap) g.cand[idx] = make_cand(r, c, ur, uc, Tr, Tc, d, nm2, watermark);
     }
   }
 }
@@ -717,7 +868,9 @@ __device__ __forceinline__ void block_minmax(int& lo, int& hi, int* slo, int* sh
 // J: this CTA's share of the slots (SpeciesBlock.cpp:787-841: tmp = ((Dik +
 // Djk) - d) / 2 in float, T[k] += (float)(tmp - (Dik + Djk)), the new row and
 // column of slot si, whose diagonal keeps i's old value) and of the active
-// list; the share's exponent range and integer sum go to jexp / jsum.
+// list; the share's exponent range and integer sum go to jexp / jsum.  The
+// shares hold at most one slot and one list position per thread (the launch
+// has at least n0 / blockDim CTAs).
 __device__ void grid_join_share(const NJDev& s, const GridNJ& g, const GCand& w, int na, const int* act, int* act2) {
   __shared__ int slo[32], shi[32];
   __shared__ long long ssum[32], sabs[32];
@@ -726,30 +879,35 @@ __device__ void grid_join_share(const NJDev& s, const GridNJ& g, const GCand& w,
   const int n0 = s.n0;
   const size_t ld = (size_t)s.ld;
   const int per = (n0 + (int)gridDim.x - 1) / (int)gridDim.x;
-  const int p0 = (int)blockIdx.x * per, p1 = min(n0, p0 + per);
+  const int p = (int)blockIdx.x * per + (int)threadIdx.x;
+  const bool mine = (int)threadIdx.x < per && p < n0;
   int lowexp = INT_MAX, topexp = INT_MIN;
-  for (int p = p0 + (int)threadIdx.x; p < p1; p += blockDim.x) {
-    g.grmin[p] = 0x7F7FFFFF;   // the next join's row minima start at +inf (S has read them)
+  float tmp = 0.f;
+  bool live = false;
+  if (mine) {
+    g.grmin[p] = 0x7F7FFFFF;   // the next join's row minima start at +inf
     const int v = s.node[p];
     const float Dik = s.D[(size_t)si * ld + p];
     const float Djk = s.D[(size_t)sj * ld + p];
     const double Tk = s.T[p];
-    if (v < 0 || p == si || p == sj) continue;
-    const float sumf = __fadd_rn(Dik, Djk);
-    const float tmp = __fmul_rn(__fsub_rn(sumf, dmin), 0.5f);
-    const double t = __dadd_rn(Tk, (double)__fsub_rn(tmp, sumf));
-    s.T[p] = t;
-    s.Tf[p] = (float)t;
-    s.D[(size_t)p * ld + si] = tmp;
-    s.D[(size_t)si * ld + p] = tmp;
-    g.tv[p] = tmp;
-    lowexp = min(lowexp, low_bit_exp(tmp));
-    topexp = max(topexp, top_bit_exp(tmp));
+    live = v >= 0 && p != si && p != sj;
+    if (live) {
+      const float sumf = __fadd_rn(Dik, Djk);
+      tmp = __fmul_rn(__fsub_rn(sumf, dmin), 0.5f);
+      const double t = __dadd_rn(Tk, (double)__fsub_rn(tmp, sumf));
+      s.T[p] = t;
+      s.Tf[p] = (float)t;
+      s.D[(size_t)p * ld + si] = tmp;
+      s.D[(size_t)si * ld + p] = tmp;
+      g.tv[p] = tmp;
+      lowexp = low_bit_exp(tmp);
+      topexp = top_bit_exp(tmp);
+    }
   }
   // the active list without i and j (ascending ids), shifted into act2
   const int kper = (na + (int)gridDim.x - 1) / (int)gridDim.x;
-  const int k0 = (int)blockIdx.x * kper, k1 = min(na, k0 + kper);
-  for (int k = k0 + (int)threadIdx.x; k < k1; k += blockDim.x) {
+  const int k = (int)blockIdx.x * kper + (int)threadIdx.x;
+  if ((int)threadIdx.x < kper && k < na) {
     const int v = act[k];
     if (v != i && v != j) act2[k - (v > i) - (v > j)] = v;
   }
@@ -757,13 +915,9 @@ __device__ void grid_join_share(const NJDev& s, const GridNJ& g, const GCand& w,
   // this share's integer sum in units of its own lowest exponent (used only
   // when the whole row's range is below 48 bits, so only then needed exact)
   long long isum = 0, iabs = 0;
-  if (lowexp != INT_MAX && topexp - lowexp < 48) {
-    for (int p = p0 + (int)threadIdx.x; p < p1; p += blockDim.x) {
-      if (s.node[p] < 0 || p == si || p == sj) continue;
-      const long long v = float_units(g.tv[p], lowexp);
-      isum += v;
-      iabs += v < 0 ? -v : v;
-    }
+  if (live && topexp - lowexp < 48) {
+    isum = float_units(tmp, lowexp);
+    iabs = isum < 0 ? -isum : isum;
   }
   for (int o = 16; o > 0; o >>= 1) {
     isum += __shfl_xor_sync(0xffffffffu, isum, o);
@@ -774,16 +928,20 @@ __device__ void grid_join_share(const NJDev& s, const GridNJ& g, const GCand& w,
     sabs[threadIdx.x >> 5] = iabs;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    isum = iabs = 0;
-    for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2) {
-      isum += ssum[w2];
-      iabs += sabs[w2];
+  if (threadIdx.x < 32) {
+    const int nwb = (int)(blockDim.x >> 5);
+    isum = (int)threadIdx.x < nwb ? ssum[threadIdx.x] : 0;
+    iabs = (int)threadIdx.x < nwb ? sabs[threadIdx.x] : 0;
+    for (int o = 16; o > 0; o >>= 1) {
+      isum += __shfl_xor_sync(0xffffffffu, isum, o);
+      iabs += __shfl_xor_sync(0xffffffffu, iabs, o);
     }
-    g.jsum[2 * blockIdx.x] = isum;
-    g.jsum[2 * blockIdx.x + 1] = iabs;
-    g.jexp[2 * blockIdx.x] = lowexp;
-    g.jexp[2 * blockIdx.x + 1] = topexp;
+    if (threadIdx.x == 0) {
+      g.jsum[2 * blockIdx.x] = isum;
+      g.jsum[2 * blockIdx.x + 1] = iabs;
+      g.jexp[2 * blockIdx.x] = lowexp;
+      g.jexp[2 * blockIdx.x + 1] = topexp;
+    }
   }
 }
 
@@ -791,8 +949,9 @@ __device__ void grid_join_share(const NJDev& s, const GridNJ& g, const GCand& w,
 // (SpeciesBlock.cpp:799, :818 -- the sequential double sum in ascending id
 // order, taken as the exact integer sum of the shares when that provably
 // equals it), written by every CTA for itself; CTA 0 also writes the join
-// record (TreeNode::join) and the id -> slot map.  When the integer sum cannot
-// be used, CTA 0 runs the sequential loop and one more grid barrier follows.
+// record (TreeNode::join's inputs; the lengths follow after the loop) and the
+// id -> slot map.  When the integer sum cannot be used, CTA 0 runs the
+// sequential loop and one more grid barrier follows.
 __device__ bool grid_join_apply(const NJDev& s, const GridNJ& g, const GCand& w, const PickOut& pk, int step, int n,
                                 const int* act_old, int* act_new, unsigned& target) {
   __shared__ double s_sum;
@@ -801,10 +960,23 @@ __device__ bool grid_join_apply(const NJDev& s, const GridNJ& g, const GCand& w,
   const int m_n = n - step, next = n + step;
   if (threadIdx.x < 32) {
     const int l = threadIdx.x;
+    // at most kGridMax CTAs: kGridMax / 32 shares per lane, held in registers
+    constexpr int kPer = kGridMax / 32;
+    int je[kPer];
+    long long jsv[kPer], jav[kPer];
     int lowexp = INT_MAX, topexp = INT_MIN;
-    for (int b = l; b < (int)gridDim.x; b += 32) {
-      lowexp = min(lowexp, g.jexp[2 * b]);
-      topexp = max(topexp, g.jexp[2 * b + 1]);
+#pragma unroll
+    for (int t = 0; t < kPer; ++t) {
+      const int b = l + 32 * t;
+      je[t] = INT_MAX;
+      jsv[t] = jav[t] = 0;
+      if (b < (int)gridDim.x) {
+        je[t] = g.jexp[2 * b];
+        jsv[t] = g.jsum[2 * b];
+        jav[t] = g.jsum[2 * b + 1];
+        topexp = max(topexp, g.jexp[2 * b + 1]);
+      }
+      lowexp = min(lowexp, je[t]);
     }
     for (int o = 16; o > 0; o >>= 1) {
       lowexp = min(lowexp, __shfl_xor_sync(0xffffffffu, lowexp, o));
@@ -815,12 +987,12 @@ __device__ bool grid_join_apply(const NJDev& s, const GridNJ& g, const GCand& w,
     const bool fits = lowexp == INT_MAX || topexp - lowexp < 48;
     long long isum = 0, iabs = 0;
     if (fits && lowexp != INT_MAX) {
-      for (int b = l; b < (int)gridDim.x; b += 32) {
-        const int e = g.jexp[2 * b];
-        if (e == INT_MAX) continue;   // a share without values
-        const long long m = 1ll << (e - lowexp);
-        isum += g.jsum[2 * b] * m;
-        iabs += g.jsum[2 * b + 1] * m;
+#pragma unroll
+      for (int t = 0; t < kPer; ++t) {
+        if (je[t] == INT_MAX) continue;   // a share without values
+        const long long m = 1ll << (je[t] - lowexp);
+        isum += jsv[t] * m;
+        iabs += jav[t] * m;
       }
       for (int o = 16; o > 0; o >>= 1) {
         isum += __shfl_xor_sync(0xffffffffu, isum, o);
@@ -832,7 +1004,7 @@ __device__ bool grid_join_apply(const NJDev& s, const GridNJ& g, const GCand& w,
         s_sum = 0.0;                                 // every value is zero
         s_exact = 1;
       } else if (fits && iabs < (1ll << 53)) {
-        s_sum = ldexp((double)isum, lowexp);         // exact: |isum| < 2^53
+        s_sum = units_to_double(isum, lowexp);       // exact: |isum| < 2^53
         s_exact = 1;
       } else {
         s_exact = 0;
@@ -844,7 +1016,7 @@ __device__ bool grid_join_apply(const NJDev& s, const GridNJ& g, const GCand& w,
   if (threadIdx.x == 0) {
     if (exact) {
       s.T[si] = s_sum;
-      s.Tf[si] = (float)s_sum;
+      s.Tf[si] = __double2float_rn(s_sum);
     } else if (blockIdx.x == 0) {
       double sum = 0.0;   // the reference's loop: active ids ascending, i and j skipped
       for (int k = 0; k < m_n; ++k) {
@@ -852,42 +1024,22 @@ __device__ bool grid_join_apply(const NJDev& s, const GridNJ& g, const GCand& w,
         if (v != i && v != j) sum = __dadd_rn(sum, (double)g.tv[s.slot[v]]);
       }
       s.T[si] = sum;
-      s.Tf[si] = (float)sum;
+      s.Tf[si] = __double2float_rn(sum);
     }
     s.Tf[sj] = __int_as_float(0x7FC00000);   // dead: NaN
     s.node[sj] = -1;
     s.node[si] = next;
     if (blockIdx.x == 0) {
-      const float dmin = w.d;
-      const double Ti = w.ta, Tj = w.tb;
-      double li, lj;
-      const double half = 0.5;
-      if (m_n == 2) {
-        li = lj = __dmul_rn((double)dmin, half);
-      } else {
-        const double nm2 = (double)(m_n - 2);
-        li = __dmul_rn(half, __dadd_rn((double)dmin, __ddiv_rn(__dsub_rn(Ti, Tj), nm2)));
-        lj = __dmul_rn(half, __dadd_rn((double)dmin, __ddiv_rn(__dsub_rn(Tj, Ti), nm2)));
-      }
-      if (li < 0.0) {
-        lj = __dsub_rn(lj, li);
-        li = 0.0;
-      } else if (lj < 0.0) {
-        li = __dsub_rn(li, lj);
-        lj = 0.0;
-      }
       nwg_join& J = s.joins[step];
       J.i = i;
       J.j = j;
       J.node = next;
       J.n = m_n;
-      J.d = dmin;
+      J.d = w.d;
       J.pad = 0.f;
       J.q = w.q1;
-      J.ti = Ti;
-      J.tj = Tj;
-      J.len_i = li;
-      J.len_j = lj;
+      J.ti = w.ta;
+      J.tj = w.tb;
       act_new[m_n - 2] = next;
       *s.na = m_n - 1;
       s.slot[j] = -1;
@@ -902,12 +1054,13 @@ __device__ bool grid_join_apply(const NJDev& s, const GridNJ& g, const GCand& w,
   return true;
 }
 
-// Joins step0 .. step1-1 of an n-taxon job (no rebuild among them; the
-// active count before join t is n - t).
+// Joins step0 .. step1-1 of an n-taxon job (the active count before join t
+// is n - t).
 __global__ void __launch_bounds__(1024, 1) nj_grid_kernel(NJDev s, GridNJ g, int step0, int step1, int n,
                                                          int watermark) {
   __shared__ PickOut spick;
   __shared__ GCand swin;
+  __shared__ float sthr;
   unsigned target = 0;
   for (int p = (int)(blockIdx.x * blockDim.x + threadIdx.x); p < s.n0; p += (int)(gridDim.x * blockDim.x))
     g.grmin[p] = 0x7F7FFFFF;   // ordered int of FLT_MAX
@@ -925,16 +1078,21 @@ __global__ void __launch_bounds__(1024, 1) nj_grid_kernel(NJDev s, GridNJ g, int
     const double nm2 = (double)(m_n - 2);
     grid_pass(s, g, nm2f);
     if (!grid_barrier(g, target)) return;
-    grid_cand(s, g, nm2f, nm2, watermark);
-    if (!grid_barrier(g, target)) return;
-    if (threadIdx.x < 32) {
-      const PickOut r = pick_warp(g.cand, &s.g32[2], s.cand_cap);
-      if (threadIdx.x == 0) {
-        spick = r;
-        if (!r.error) swin = g.cand[r.idx];
+    if (!grid_pick_direct(s, g, nm2, nm2f, watermark, &swin, &spick, &sthr)) {
+      grid_cand(s, g, nm2f, nm2, watermark, sthr);
+      if (!grid_barrier(g, target)) return;
+      if (threadIdx.x < 32) {
+        const int ncount = s.g32[2];
+        const int nc = min(ncount, s.cand_cap);
+        PickOut r = pick_keys(nc, [&](int k) { return g.cand[k]; });
+        r.error = r.error || ncount > s.cand_cap;
+        if (threadIdx.x == 0) {
+          spick = r;
+          if (!r.error) swin = g.cand[r.idx];
+        }
       }
+      __syncthreads();
     }
-    __syncthreads();
     if (spick.error) {   // the same in every CTA
       if (blockIdx.x == 0 && threadIdx.x == 0) record_pick(s, spick);
       return;
@@ -946,6 +1104,33 @@ __global__ void __launch_bounds__(1024, 1) nj_grid_kernel(NJDev s, GridNJ g, int
     if (!grid_barrier(g, target)) return;
   }
   if (step1 > step0) grid_join_apply(s, g, swin, spick, step1 - 1, n, act2, act, target);
+}
+
+// TreeNode::join (TreeNode.cpp:31-58) for the joins the grid kernel recorded:
+// L_i = (d + (T_i - T_j)/(n-2)) / 2, L_j likewise, n = 2 gives d/2 each, a
+// negative side is clamped to 0 and moved to the other.
+__global__ void nj_lengths_kernel(nwg_join* joins, int count) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  nwg_join& J = joins[k];
+  const double half = 0.5;
+  double li, lj;
+  if (J.n == 2) {
+    li = lj = __dmul_rn((double)J.d, half);
+  } else {
+    const double nm2 = (double)(J.n - 2);
+    li = __dmul_rn(half, __dadd_rn((double)J.d, __ddiv_rn(__dsub_rn(J.ti, J.tj), nm2)));
+    lj = __dmul_rn(half, __dadd_rn((double)J.d, __ddiv_rn(__dsub_rn(J.tj, J.ti), nm2)));
+  }
+  if (li < 0.0) {
+    lj = __dsub_rn(lj, li);
+    li = 0.0;
+  } else if (lj < 0.0) {
+    li = __dsub_rn(li, lj);
+    lj = 0.0;
+  }
+  J.len_i = li;
+  J.len_j = lj;
 }
 
 // Compaction, part 1 (one CTA): map[p] = new slot of live slot p (ascending),
@@ -1294,10 +1479,10 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_cluster_
 struct NJState {
   DevBuf D, T, Tf, slot, node, act, na, g32, cand, win, stats, joins, vd, rmin, desc;
   // large-n path: compaction buffers, second active list, grid partials and barrier words
-  DevBuf D2, T2, Tf2, node2, map, act2, part, jsum, jexp, gbar;
+  DevBuf D2, T2, Tf2, node2, map, act2, part, jsum, jexp, gbar, grec;
   ~NJState() {
     for (DevBuf* b : {&D, &T, &Tf, &slot, &node, &act, &na, &g32, &cand, &win, &stats, &joins, &vd, &rmin, &desc, &D2,
-                      &T2, &Tf2, &node2, &map, &act2, &part, &jsum, &jexp, &gbar})
+                      &T2, &Tf2, &node2, &map, &act2, &part, &jsum, &jexp, &gbar, &grec})
       b->release();
   }
 };
@@ -1344,12 +1529,15 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
       (rc = S.joins.ensure(sizeof(nwg_join) * (n - 1))) || (rc = S.vd.ensure(sizeof(float) * n)) ||
       (rc = S.rmin.ensure(sizeof(float) * n)) || (rc = S.desc.ensure(sizeof(NJJob))))
     return fail(rc, "nj allocation");
-  const int grid = sms;   // one CTA of 1024 threads per SM (cooperative launch)
+  // one CTA of 1024 threads per SM (cooperative launch); every join share
+  // then holds at most one slot per thread
+  const int grid = std::min(sms, kGridMax);
   if (big && ((rc = S.D2.ensure(sizeof(float) * (size_t)n * ldd)) || (rc = S.T2.ensure(sizeof(double) * n)) ||
               (rc = S.Tf2.ensure(sizeof(float) * ldd)) || (rc = S.node2.ensure(sizeof(int) * n)) ||
               (rc = S.map.ensure(sizeof(int) * n)) || (rc = S.act2.ensure(sizeof(int) * (n + 1))) ||
               (rc = S.part.ensure(sizeof(float) * 2 * grid)) || (rc = S.jsum.ensure(sizeof(long long) * 2 * grid)) ||
-              (rc = S.jexp.ensure(sizeof(int) * 2 * grid)) || (rc = S.gbar.ensure(sizeof(int) * 4))))
+              (rc = S.jexp.ensure(sizeof(int) * 2 * grid)) || (rc = S.gbar.ensure(sizeof(int) * 4)) ||
+              (rc = S.grec.ensure(sizeof(int2) * n))))
     return fail(rc, "nj allocation");
   cudaStream_t s = stream;
   const cudaMemcpyKind kind = device_D ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
@@ -1400,7 +1588,7 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
     if ((rc = cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, nj_grid_kernel, 1024, 0),
                    "nj occupancy")))
       return rc;
-    if (blocks_per_sm < 1) return fail(NWG_ERR_CUDA, "neighbor-joining grid kernel does not fit an SM");
+    if (blocks_per_sm < 1 || grid * 1024 < n) return fail(NWG_ERR_CUDA, "neighbor-joining grid kernel does not fit");
     float* Dalt = (float*)S.D2.p;
     double* Talt = (double*)S.T2.p;
     float* Tfalt = (float*)S.Tf2.p;
@@ -1410,6 +1598,7 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
     g.abort = (int*)S.gbar.p + 2;
     g.act2 = (int*)S.act2.p;
     g.grmin = (int*)S.rmin.p;
+    g.grec = (int2*)S.grec.p;
     g.tv = (float*)S.vd.p;
     g.part = (float*)S.part.p;
     g.jsum = (long long*)S.jsum.p;
@@ -1486,6 +1675,9 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
       }
       if ((rc = cuda(cudaGetLastError(), "nj launch"))) return rc;
     }
+    nj_lengths_kernel<<<(n - 1 + 255) / 256, 256, 0, s>>>(d.joins, n - 1);
+    ++launches;
+    if ((rc = cuda(cudaGetLastError(), "nj launch"))) return rc;
   }
   if (st) cudaEventRecord(ev1, s);
   unsigned long long dst[5] = {0, 0, 0, 0, 0};
