@@ -72,27 +72,75 @@ def test_device_nj_ties_and_duplicates(ctx):
     assert st["ambiguous_steps"] == ost["ambiguous_steps"]
 
 
+_BOTH_PATHS = """
+import sys, numpy as np; sys.path.insert(0, 'tests'); import oracle_py as O
+from mestrado_gb300 import Context, synth
+c = Context(10, 2)
+
+def check(D, exact_q=True):
+    j, st = c.nj(D, stats=True)
+    oj, ost = O.nj(D)
+    assert len(j) == len(oj)
+    assert st['rebuilds'] == ost['rebuilds'] and st['tie_steps'] == ost['tie_steps']
+    assert st['ambiguous_steps'] == ost['ambiguous_steps']
+    for a, b in zip(j, oj):
+        assert (a['i'], a['j'], a['node'], a['n'], a['len_i'], a['len_j']) == \
+            (b['i'], b['j'], b['node'], b['n'], b['len_i'], b['len_j'])
+        assert not exact_q or (a['q'], a['ti'], a['tj']) == (b['q'], b['ti'], b['tj'])
+
+for seed, n in ((11, 450), (12, 640), (2, 3), (3, 17), (4, 205)):
+    check(c.score_all(synth.family(n, 90, ps=0.1, pi=0.01, seed=seed)))
+# identical sequences (exact ties) and a small integer matrix with many ties:
+# the pick falls back to the candidate scan
+S = synth.family(40, 60, ps=0.02, pi=0.0, seed=9)
+check(c.score_all([S[i] for i in range(len(S))] + [S[0], S[0], S[1]]))
+rng = np.random.default_rng(0)
+M = rng.integers(0, 5, size=(30, 30)).astype(np.float32)
+check(np.triu(M, 1) + np.triu(M, 1).T)
+M = rng.integers(0, 3, size=(300, 300)).astype(np.float32)
+check(np.triu(M, 1) + np.triu(M, 1).T)
+print('ok')
+"""
+
+
 @pytest.mark.parametrize("path", ["cluster", "full_gpu"])
 def test_both_nj_paths_match_oracle(path):
-    # the large-matrix path (full-GPU first pass, compaction at the rebuild
-    # steps) and the one-cluster path give the oracle's joins; run in a child
-    # process so that the path threshold applies from the library's first use
+    # the large-matrix path (one cooperative full-GPU launch per segment,
+    # compaction at the rebuild steps) and the one-cluster path give the
+    # oracle's joins on families, tiny n, duplicates and tie-heavy integer
+    # matrices; run in a child process so that the path threshold applies
+    # from the library's first use
     import subprocess
     import sys
     env = dict(os.environ, NWG_NJ_CLUSTER_MAX_N="0" if path == "full_gpu" else "100000")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", _BOTH_PATHS], cwd=root, env=env, capture_output=True, text=True,
+                       timeout=900)
+    assert r.returncode == 0 and r.stdout.strip().endswith("ok"), r.stdout + r.stderr
+
+
+@pytest.mark.parametrize("case", ["cfg0", "nj300", "nj1200"])
+def test_full_gpu_path_matches_reference_tree(case):
+    # the golden reference trees through the large-matrix path
+    import subprocess
+    import sys
     code = (
-        "import sys, numpy as np; sys.path.insert(0, 'tests'); import oracle_py as O\n"
-        "from mestrado_gb300 import Context, synth\n"
+        "import sys, json, os; sys.path.insert(0, 'tests')\n"
+        "from mestrado_gb300 import Context, newick\n"
+        "from fasta import read_fasta\n"
+        "from test_nj_cpu import golden_joins\n"
+        f"d = os.path.join('tests', 'golden', '{case}')\n"
+        "names, seqs = read_fasta(os.path.join(d, 'input.fasta'))\n"
         "c = Context(10, 2)\n"
-        "for seed, n in ((11, 450), (12, 640)):\n"
-        "    D = c.score_all(synth.family(n, 90, ps=0.1, pi=0.01, seed=seed))\n"
-        "    j, st = c.nj(D, stats=True)\n"
-        "    oj, ost = O.nj(D)\n"
-        "    assert st['rebuilds'] == ost['rebuilds'] and st['tie_steps'] == ost['tie_steps']\n"
-        "    for a, b in zip(j, oj):\n"
-        "        assert (a['i'], a['j'], a['node'], a['len_i'], a['len_j'], a['q']) == "
-        "(b['i'], b['j'], b['node'], b['len_i'], b['len_j'], b['q'])\n"
+        "j, st = c.nj(c.score_all(seqs), stats=True)\n"
+        f"ref = golden_joins('{case}')\n"
+        "assert len(j) == len(ref)\n"
+        "for a, b in zip(j, ref):\n"
+        "    assert (a['node'], a['i'], a['j'], a['len_i'], a['len_j']) == "
+        "(b['node'], b['i'], b['j'], b['len_i'], b['len_j'])\n"
+        "assert newick(j, names) == open(os.path.join(d, 'tree.nwk')).read()\n"
         "print('ok')\n")
+    env = dict(os.environ, NWG_NJ_CLUSTER_MAX_N="0")
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     r = subprocess.run([sys.executable, "-c", code], cwd=root, env=env, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0 and r.stdout.strip().endswith("ok"), r.stdout + r.stderr
