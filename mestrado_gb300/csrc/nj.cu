@@ -534,7 +534,8 @@ __device__ bool grid_barrier(const GridNJ& g, unsigned& target) {
   __syncthreads();
   target += gridDim.x;
   if (threadIdx.x == 0) {
-    __threadfence();
+    // release: this CTA's writes (ordered before by the CTA barrier) are
+    // visible to every CTA that acquires the count
     red_release_add(&g.bar[0], 1u);
     int ok = 1;
     const long long t0 = clock64();
@@ -549,7 +550,6 @@ __device__ bool grid_barrier(const GridNJ& g, unsigned& target) {
         break;
       }
     }
-    __threadfence();
     s_ok = ok;
   }
   __syncthreads();
@@ -588,7 +588,9 @@ __device__ __forceinline__ void pass_elem(float d, float tc, int c, float tr, fl
   mag = fmaxf(mag, __fadd_rn(fabsf(x), fabsf(tc)));
 }
 
-__device__ void grid_pass(const NJDev& s, const GridNJ& g, float nm2f) {
+// Odd joins scan every row backwards: the lines the previous pass read last
+// are still in L2 when the triangle is a little larger than L2.
+__device__ void grid_pass(const NJDev& s, const GridNJ& g, float nm2f, bool rev) {
   __shared__ float sq[32], sm[32];
   const int lane = threadIdx.x & 31;
   const int n0 = s.n0, nv = s.ld >> 2;
@@ -598,8 +600,8 @@ __device__ void grid_pass(const NJDev& s, const GridNJ& g, float nm2f) {
   float qmin = FLT_MAX, mmax = 0.f;
   for (int p = (int)(threadIdx.x >> 5) * (int)gridDim.x + (int)blockIdx.x; p < npairs; p += nw) {
     for (int h = 0; h < 2; ++h) {
-      const int r = h ? n0 - 1 - p : p;
-      if (h && r == p) break;
+      if (n0 - 1 - p == p && h) break;
+      const int r = (h != (int)rev) ? n0 - 1 - p : p;
       const float tr = s.Tf[r];
       if (tr != tr) continue;   // dead slot
       const float* row = s.D + (size_t)r * s.ld;
@@ -610,14 +612,20 @@ __device__ void grid_pass(const NJDev& s, const GridNJ& g, float nm2f) {
       if (lane < 4 * v0 - c0 && c0 + lane < n0)
         pass_elem(row[c0 + lane], s.Tf[c0 + lane], c0 + lane, tr, nm2f, m1, m2, c1, mag);
       const float4* row4 = reinterpret_cast<const float4*>(row);
-#pragma unroll 4
-      for (int v = v0 + lane; v < nv; v += 32) {
+      auto vec = [&](int v) {
         const float4 d = row4[v];
         const float4 tc = Tf4[v];
         pass_elem(d.x, tc.x, 4 * v, tr, nm2f, m1, m2, c1, mag);
         pass_elem(d.y, tc.y, 4 * v + 1, tr, nm2f, m1, m2, c1, mag);
         pass_elem(d.z, tc.z, 4 * v + 2, tr, nm2f, m1, m2, c1, mag);
         pass_elem(d.w, tc.w, 4 * v + 3, tr, nm2f, m1, m2, c1, mag);
+      };
+      if (!rev) {
+#pragma unroll 4
+        for (int v = v0 + lane; v < nv; v += 32) vec(v);
+      } else {
+#pragma unroll 4
+        for (int v = nv - 1 - lane; v >= v0; v -= 32) vec(v);
       }
       // the row's two smallest over the warp (an equal pair makes m2 = m1)
       for (int o = 16; o > 0; o >>= 1) {
@@ -745,6 +753,14 @@ __device__ int grid_pick_direct(const NJDev& s, const GridNJ& g, double nm2, flo
   __shared__ GCand fc[kFastRows];
   __shared__ int nrows, s_ok;
   const int n0 = s.n0;
+  // the row minima load together with the CTA partials (n0 <= 8 * blockDim)
+  constexpr int kPerThread = 8;
+  int rm[kPerThread];
+#pragma unroll
+  for (int t = 0; t < kPerThread; ++t) {
+    const int p = (int)threadIdx.x + t * (int)blockDim.x;
+    rm[t] = p < n0 ? g.grmin[p] : 0x7F7FFFFF;
+  }
   if (threadIdx.x < 32) {
     const int l = threadIdx.x;
     float q = FLT_MAX, m = 0.f;
@@ -764,10 +780,11 @@ __device__ int grid_pick_direct(const NJDev& s, const GridNJ& g, double nm2, flo
   __syncthreads();
   const float thr = *sthr;
   const int othr = ford(thr);
-  for (int p = threadIdx.x; p < n0; p += blockDim.x) {
-    if (g.grmin[p] <= othr) {
-      const int t = atomicAdd(&nrows, 1);
-      if (t < kFastRows) rows[t] = p;
+#pragma unroll
+  for (int t = 0; t < kPerThread; ++t) {
+    if (rm[t] <= othr) {
+      const int k = atomicAdd(&nrows, 1);
+      if (k < kFastRows) rows[k] = (int)threadIdx.x + t * (int)blockDim.x;
     }
   }
   __syncthreads();
@@ -1076,7 +1093,7 @@ __global__ void __launch_bounds__(1024, 1) nj_grid_kernel(NJDev s, GridNJ g, int
     const int m_n = n - step;
     const float nm2f = (float)(m_n - 2);
     const double nm2 = (double)(m_n - 2);
-    grid_pass(s, g, nm2f);
+    grid_pass(s, g, nm2f, (step & 1) != 0);
     if (!grid_barrier(g, target)) return;
     if (!grid_pick_direct(s, g, nm2, nm2f, watermark, &swin, &spick, &sthr)) {
       grid_cand(s, g, nm2f, nm2, watermark, sthr);
@@ -1621,10 +1638,33 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
     long long ave0 = (((long long)(n - 1) * n) / 2) / kBinT;
     long long ub = ((long long)n * (n - 1)) / 2;
     int watermark = n, m_n = n;
+    // compaction to the live slots, in slot order (every slot comparison of
+    // the record-order rounding is unchanged, so it may run at any step)
+    auto compact = [&](int na) -> int {
+      const int ld2 = (na + 3) & ~3;
+      int e;
+      if ((e = cuda(cudaMemsetAsync(Tfalt, 0xFF, sizeof(float) * ld2, s), "nj launch"))) return e;
+      compact_map_kernel<<<1, 1024, 0, s>>>(d, (int*)S.map.p, Talt, Tfalt, nodealt, nn);
+      compact_copy_kernel<<<d.n0, 256, 0, s>>>(d, (const int*)S.map.p, Dalt, ld2);
+      launches += 2;
+      std::swap(d.D, Dalt);
+      std::swap(d.T, Talt);
+      std::swap(d.Tf, Tfalt);
+      std::swap(d.node, nodealt);
+      d.n0 = na;
+      d.ld = ld2;
+      return NWG_OK;
+    };
+    // Between rebuilds, large matrices are also compacted once a sixteenth of
+    // their slots are dead: the pass streams every column of a live row.
+    constexpr int kCompactMinSlots = 2048, kCompactFrac = 16;
     int step = 0;
     while (step < n - 1) {
-      // the segment ends with the join after which the countdown reaches 0
-      const int seg_end = steps == INT_MAX ? n - 1 : std::min(n - 1, step + steps + 1);
+      // the segment ends with the join after which the countdown reaches 0,
+      // or at the next compaction
+      int seg_end = steps == INT_MAX ? n - 1 : std::min(n - 1, step + steps + 1);
+      const bool comp = d.n0 >= kCompactMinSlots && step + d.n0 / kCompactFrac < seg_end;
+      if (comp) seg_end = step + d.n0 / kCompactFrac;
       if ((rc = cuda(cudaMemsetAsync(S.gbar.p, 0, sizeof(unsigned) * 2, s), "nj launch"))) return rc;
       {
         int a0 = step, a1 = seg_end, an = n, aw = watermark;
@@ -1653,25 +1693,16 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
         }
       }
       if (rebuild) {
-        const int na = m_n;
-        rowsum_kernel<<<(na + 7) / 8, 256, 0, s>>>(d);
-        // compaction to the live slots, in slot order
-        const int ld2 = (na + 3) & ~3;
-        if ((rc = cuda(cudaMemsetAsync(Tfalt, 0xFF, sizeof(float) * ld2, s), "nj launch"))) return rc;
-        compact_map_kernel<<<1, 1024, 0, s>>>(d, (int*)S.map.p, Talt, Tfalt, nodealt, nn);
-        compact_copy_kernel<<<d.n0, 256, 0, s>>>(d, (const int*)S.map.p, Dalt, ld2);
-        launches += 3;
-        std::swap(d.D, Dalt);
-        std::swap(d.T, Talt);
-        std::swap(d.Tf, Tfalt);
-        std::swap(d.node, nodealt);
-        d.n0 = na;
-        d.ld = ld2;
+        rowsum_kernel<<<(m_n + 7) / 8, 256, 0, s>>>(d);
+        ++launches;
+        if ((rc = compact(m_n))) return rc;
         ++stats.rebuilds;
         watermark = n + step;
         steps = (m_n < 200) ? INT_MAX : (int)((float)m_n * 0.5f);
         ave0 = (((long long)(m_n - 1) * m_n) / 2) / kBinT;
         ub = ((long long)m_n * (m_n - 1)) / 2;
+      } else if (comp) {
+        if ((rc = compact(m_n))) return rc;
       }
       if ((rc = cuda(cudaGetLastError(), "nj launch"))) return rc;
     }
