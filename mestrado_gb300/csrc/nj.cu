@@ -764,9 +764,15 @@ __device__ int grid_pick_direct(const NJDev& s, const GridNJ& g, double nm2, flo
   if (threadIdx.x < 32) {
     const int l = threadIdx.x;
     float q = FLT_MAX, m = 0.f;
-    for (int b = l; b < (int)gridDim.x; b += 32) {
-      q = fminf(q, g.part[2 * b]);
-      m = fmaxf(m, g.part[2 * b + 1]);
+    // every partial in flight at once (at most kGridMax CTAs)
+#pragma unroll
+    for (int t = 0; t < kGridMax / 32; ++t) {
+      const int b = l + 32 * t;
+      if (b < (int)gridDim.x) {
+        const float2 pm = reinterpret_cast<const float2*>(g.part)[b];
+        q = fminf(q, pm.x);
+        m = fmaxf(m, pm.y);
+      }
     }
     for (int o = 16; o > 0; o >>= 1) {
       q = fminf(q, __shfl_xor_sync(0xffffffffu, q, o));
@@ -808,7 +814,14 @@ __device__ int grid_pick_direct(const NJDev& s, const GridNJ& g, double nm2, flo
     }
     ok = __all_sync(0xffffffffu, ok);
     PickOut r{};
-    if (ok) r = pick_keys(nr, [&](int k) { return fc[k]; });
+    if (ok && nr == 1) {
+      r.idx = 0;     // one candidate: the winner, a tie with itself only
+      r.ties = 1;
+      r.amb = 0;
+      r.error = false;
+    } else if (ok) {
+      r = pick_keys(nr, [&](int k) { return fc[k]; });
+    }
     if (l == 0) {
       s_ok = ok;
       if (ok) {
@@ -862,63 +875,83 @@ __device__ void grid_cand(const NJDev& s, const GridNJ& g, float nm2f, double nm
   }
 }
 
-// Block-wide min / max of two ints (every thread gets the result).
-__device__ __forceinline__ void block_minmax(int& lo, int& hi, int* slo, int* shi) {
-  for (int o = 16; o > 0; o >>= 1) {
-    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-  }
-  if ((threadIdx.x & 31) == 0) {
-    slo[threadIdx.x >> 5] = lo;
-    shi[threadIdx.x >> 5] = hi;
-  }
-  __syncthreads();
-  lo = INT_MAX;
-  hi = INT_MIN;
-  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-    lo = min(lo, slo[w]);
-    hi = max(hi, shi[w]);
-  }
-  __syncthreads();
-}
-
 // J: this CTA's share of the slots (SpeciesBlock.cpp:787-841: tmp = ((Dik +
 // Djk) - d) / 2 in float, T[k] += (float)(tmp - (Dik + Djk)), the new row and
 // column of slot si, whose diagonal keeps i's old value) and of the active
 // list; the share's exponent range and integer sum go to jexp / jsum.  The
 // shares hold at most one slot and one list position per thread (the launch
 // has at least n0 / blockDim CTAs).
+// An exact sum of floats as u * 2^e (|u| < 2^62), with a = sum of |values| in
+// the same units and t the highest exponent; e = INT_MAX for no values.  A
+// sum whose values span 48 bits or more is not kept (the row's range then
+// rules out the integer sum anyway; e and t stay exact).
+struct USum {
+  long long u, a;
+  int e, t;
+};
+
+__device__ __forceinline__ void usum_add(USum& x, const USum& y) {
+  if (y.e == INT_MAX) return;
+  if (x.e == INT_MAX) {
+    x = y;
+    return;
+  }
+  const int e = min(x.e, y.e), t = max(x.t, y.t);
+  if (t - e >= 48) {
+    x.u = x.a = 0;
+  } else {
+    const long long mx = 1ll << (x.e - e), my = 1ll << (y.e - e);
+    x.u = x.u * mx + y.u * my;
+    x.a = x.a * mx + y.a * my;
+  }
+  x.e = e;
+  x.t = t;
+}
+
+__device__ __forceinline__ void usum_warp(USum& x) {
+  for (int o = 16; o > 0; o >>= 1) {
+    USum y;
+    y.u = __shfl_xor_sync(0xffffffffu, x.u, o);
+    y.a = __shfl_xor_sync(0xffffffffu, x.a, o);
+    y.e = __shfl_xor_sync(0xffffffffu, x.e, o);
+    y.t = __shfl_xor_sync(0xffffffffu, x.t, o);
+    usum_add(x, y);
+  }
+}
+
 __device__ void grid_join_share(const NJDev& s, const GridNJ& g, const GCand& w, int na, const int* act, int* act2) {
-  __shared__ int slo[32], shi[32];
-  __shared__ long long ssum[32], sabs[32];
+  __shared__ USum swarp[32];
   const int i = w.a, j = w.b, si = w.sa, sj = w.sb;
   const float dmin = w.d;
   const int n0 = s.n0;
   const size_t ld = (size_t)s.ld;
   const int per = (n0 + (int)gridDim.x - 1) / (int)gridDim.x;
   const int p = (int)blockIdx.x * per + (int)threadIdx.x;
-  const bool mine = (int)threadIdx.x < per && p < n0;
-  int lowexp = INT_MAX, topexp = INT_MIN;
-  float tmp = 0.f;
-  bool live = false;
-  if (mine) {
+  USum x;
+  x.u = x.a = 0;
+  x.e = INT_MAX;
+  x.t = INT_MIN;
+  if ((int)threadIdx.x < per && p < n0) {
     g.grmin[p] = 0x7F7FFFFF;   // the next join's row minima start at +inf
     const int v = s.node[p];
     const float Dik = s.D[(size_t)si * ld + p];
     const float Djk = s.D[(size_t)sj * ld + p];
     const double Tk = s.T[p];
-    live = v >= 0 && p != si && p != sj;
-    if (live) {
+    if (v >= 0 && p != si && p != sj) {
       const float sumf = __fadd_rn(Dik, Djk);
-      tmp = __fmul_rn(__fsub_rn(sumf, dmin), 0.5f);
+      const float tmp = __fmul_rn(__fsub_rn(sumf, dmin), 0.5f);
       const double t = __dadd_rn(Tk, (double)__fsub_rn(tmp, sumf));
       s.T[p] = t;
       s.Tf[p] = (float)t;
       s.D[(size_t)p * ld + si] = tmp;
       s.D[(size_t)si * ld + p] = tmp;
       g.tv[p] = tmp;
-      lowexp = low_bit_exp(tmp);
-      topexp = top_bit_exp(tmp);
+      if (tmp != 0.f) {
+        x.e = low_bit_exp(tmp);
+        x.t = top_bit_exp(tmp);
+        x.u = float_units(tmp, x.e);
+        x.a = x.u < 0 ? -x.u : x.u;
+      }
     }
   }
   // the active list without i and j (ascending ids), shifted into act2
@@ -928,37 +961,20 @@ __device__ void grid_join_share(const NJDev& s, const GridNJ& g, const GCand& w,
     const int v = act[k];
     if (v != i && v != j) act2[k - (v > i) - (v > j)] = v;
   }
-  block_minmax(lowexp, topexp, slo, shi);
-  // this share's integer sum in units of its own lowest exponent (used only
-  // when the whole row's range is below 48 bits, so only then needed exact)
-  long long isum = 0, iabs = 0;
-  if (live && topexp - lowexp < 48) {
-    isum = float_units(tmp, lowexp);
-    iabs = isum < 0 ? -isum : isum;
+  // the share's slots sit in its first warps (per <= blockDim)
+  const int nwv = (per + 31) >> 5;
+  if ((int)(threadIdx.x >> 5) < nwv) usum_warp(x);
+  if (nwv > 1) {
+    if ((threadIdx.x & 31) == 0 && (int)(threadIdx.x >> 5) < nwv) swarp[threadIdx.x >> 5] = x;
+    __syncthreads();
+    if (threadIdx.x == 0)
+      for (int w2 = 1; w2 < nwv; ++w2) usum_add(x, swarp[w2]);
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    isum += __shfl_xor_sync(0xffffffffu, isum, o);
-    iabs += __shfl_xor_sync(0xffffffffu, iabs, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    ssum[threadIdx.x >> 5] = isum;
-    sabs[threadIdx.x >> 5] = iabs;
-  }
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    const int nwb = (int)(blockDim.x >> 5);
-    isum = (int)threadIdx.x < nwb ? ssum[threadIdx.x] : 0;
-    iabs = (int)threadIdx.x < nwb ? sabs[threadIdx.x] : 0;
-    for (int o = 16; o > 0; o >>= 1) {
-      isum += __shfl_xor_sync(0xffffffffu, isum, o);
-      iabs += __shfl_xor_sync(0xffffffffu, iabs, o);
-    }
-    if (threadIdx.x == 0) {
-      g.jsum[2 * blockIdx.x] = isum;
-      g.jsum[2 * blockIdx.x + 1] = iabs;
-      g.jexp[2 * blockIdx.x] = lowexp;
-      g.jexp[2 * blockIdx.x + 1] = topexp;
-    }
+  if (threadIdx.x == 0) {
+    g.jsum[2 * blockIdx.x] = x.u;
+    g.jsum[2 * blockIdx.x + 1] = x.a;
+    g.jexp[2 * blockIdx.x] = x.e;
+    g.jexp[2 * blockIdx.x + 1] = x.t;
   }
 }
 
