@@ -65,35 +65,22 @@ namespace {
 constexpr int kNJMaxN = 8192;
 constexpr int kCandCap = 1 << 16;      // candidate list capacity per join
 
-struct Pick {
-  double q1, q2;
-  int a, b;      // a < b node ids
-};
-
-struct Cand {
-  double q1, q2;
-  int a, b;
-};
-
 struct NJDev {
-  float* D;            // n0 x n0, slots
+  float* D;            // n0 x ld, slots
   double* T;           // per slot
-  float* Tf;           // per slot, (float)T
+  float* Tf;           // per slot, (float)T; NaN at dead and padding slots (ld entries)
   int* slot;           // per node id (2n0-1), -1 dead
   int* node;           // per slot: node id, -1 dead
   int* act;            // active node ids ascending [n0 + 1]
   int* na;             // active count
-  int* g32;            // [0] min float q (ordered int), [1] max magnitude (ordered int), [2] candidates
-  Cand* cand;          // candidate list
-  Pick* win;
+  int* g32;            // [2] candidates of the fallback scan
   unsigned long long* stats;  // [0] ambiguous steps, [1] tie steps, [2] internal errors,
-                              // [3] open heap-size checks, [4] rebuilds (per-CTA path)
+                              // [3] open heap-size checks, [4] rebuilds (cluster form)
   nwg_join* joins;
-  float* vd;           // per slot, new row values
-  float* rmin;         // per slot: smallest float q of the row's pairs (c > r) in this join
   int n0;              // slots
-  int ld;              // row stride of D (floats)
+  int ld;              // row stride of D (floats), a multiple of 4
   int cand_cap;        // candidate list capacity
+  int pad;
 };
 
 __device__ __forceinline__ int ford(float f) {
@@ -102,28 +89,6 @@ __device__ __forceinline__ int ford(float f) {
   return b >= 0 ? b : b ^ 0x7FFFFFFF;
 }
 
-__device__ __forceinline__ float iord(int b) { return __int_as_float(b >= 0 ? b : b ^ 0x7FFFFFFF); }
-
-__device__ __forceinline__ bool better(double q, int b, int a, double q2, int b2, int a2) {
-  if (q < q2) return true;
-  if (q > q2) return false;
-  return b > b2 || (b == b2 && a > a2);
-}
-
-// q as the reference's candidate list computes it (record order).
-__device__ __forceinline__ double q_record(const NJDev& s, float d, int a, int b, int watermark, double nm2) {
-  const int sa = s.slot[a], sb = s.slot[b];
-  int f = sa, g = sb;
-  if (b >= watermark && sb < sa) {
-    f = sb;
-    g = sa;
-  }
-  return __dsub_rn(__dsub_rn(__dmul_rn((double)d, nm2), s.T[f]), s.T[g]);
-}
-
-__device__ __forceinline__ double q_heap(const NJDev& s, float d, int a, int b, double nm2) {
-  return __dsub_rn(__dmul_rn((double)d, nm2), __dadd_rn(s.T[s.slot[a]], s.T[s.slot[b]]));
-}
 
 // Exponent of the lowest set bit of a nonzero float (INT_MAX for zero).
 __device__ __forceinline__ int low_bit_exp(float f) {
@@ -199,266 +164,20 @@ __global__ void rowsum_kernel(NJDev s) {
   }
 }
 
-// Winner among the candidates and the ambiguity / tie counts, by one warp
-// (the list holds a few entries); every lane returns the same result.  The
-// count and the first 32 entries are loaded together.
+// The pick's outcome: the winner's position among the candidates, the
+// candidates within rounding of it (itself included) as ties or as pairs the
+// reference's heap rounding could have preferred, and a failed pick.
 struct PickOut {
-  int idx;          // the winner's position in the list
+  int idx;
   unsigned ties, amb;
   bool error;       // no candidate, or the list overflowed
 };
-
-template <class C>
-__device__ PickOut pick_warp(const C* cand, const int* count, int cap) {
-  const int l = threadIdx.x & 31;
-  const int ncount = *count;
-  C first{};
-  if (l < cap) first = cand[l];
-  const int nc = min(ncount, cap);
-  // the reduction carries the heap rounding q2 of the best entry with it
-  double bq = DBL_MAX, bq2 = DBL_MAX;
-  int ba = INT_MAX, bb = -1, bi = -1;
-  for (int k = l; k < nc; k += 32) {
-    const C c = k == l ? first : cand[k];
-    if (better(c.q1, c.b, c.a, bq, bb, ba)) {
-      bq = c.q1;
-      bq2 = c.q2;
-      ba = c.a;
-      bb = c.b;
-      bi = k;
-    }
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    const double q = __shfl_xor_sync(0xffffffffu, bq, o);
-    const double q2 = __shfl_xor_sync(0xffffffffu, bq2, o);
-    const int a2 = __shfl_xor_sync(0xffffffffu, ba, o);
-    const int b2 = __shfl_xor_sync(0xffffffffu, bb, o);
-    const int i2 = __shfl_xor_sync(0xffffffffu, bi, o);
-    if (better(q, b2, a2, bq, bb, ba)) {
-      bq = q;
-      bq2 = q2;
-      ba = a2;
-      bb = b2;
-      bi = i2;
-    }
-  }
-  // every lane now holds the winner (the order is total: q, then ids)
-  const double hiw = fmax(bq, bq2);
-  const bool robust_w = bq == bq2;
-  unsigned ties = 0, amb = 0;
-  for (int k = l; k < nc; k += 32) {
-    const C c = k == l ? first : cand[k];
-    const double lo = fmin(c.q1, c.q2);
-    if (lo > hiw) continue;
-    if (c.a == ba && c.b == bb) ++ties;
-    else if (robust_w && c.q1 == c.q2 && c.q1 == bq) ++ties;
-    else ++amb;
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    ties += __shfl_xor_sync(0xffffffffu, ties, o);
-    amb += __shfl_xor_sync(0xffffffffu, amb, o);
-  }
-  PickOut r;
-  r.idx = bi;
-  r.ties = ties;
-  r.amb = amb;
-  r.error = bb < 0 || ncount > cap;
-  return r;
-}
 
 // The pick's statistics: ambiguous step, tie step or internal error.
 __device__ __forceinline__ void record_pick(const NJDev& s, const PickOut& r) {
   if (r.error) atomicAdd(&s.stats[2], 1ull);
   else if (r.amb > 0 || r.ties > 4) atomicAdd(&s.stats[0], 1ull);
   else if (r.ties > 1) atomicAdd(&s.stats[1], 1ull);
-}
-
-// Per-CTA form: warp 0 picks, records and resets the candidate count; the
-// other warps wait at the final barrier.
-__device__ void pick_body(const NJDev& s) {
-  if (threadIdx.x < 32) {
-    const PickOut r = pick_warp(s.cand, &s.g32[2], s.cand_cap);
-    if (threadIdx.x == 0) {
-      Pick w;
-      w.b = -1;
-      if (!r.error) {
-        const Cand c = s.cand[r.idx];
-        w.q1 = c.q1;
-        w.q2 = c.q2;
-        w.a = c.a;
-        w.b = c.b;
-      }
-      *s.win = w;
-      record_pick(s, r);
-      s.g32[2] = 0;
-    }
-  }
-  __syncthreads();
-}
-
-// The join: record, modifyMatrix, active list.  One CTA; tv and ids are
-// shared-memory arrays of n0 entries.
-__device__ void join_body(const NJDev& s, int step, int next, int m_n, float* tv, int* ids) {
-  __shared__ int s_skip[2];
-  __shared__ long long s_isum[32], s_iabs[32];
-  __shared__ int s_low[33], s_top[33];
-  const Pick w = *s.win;
-  if (w.b < 0) return;                 // counted as an internal error by the pick
-  const int i = w.a, j = w.b;          // i < j
-  const int si = s.slot[i], sj = s.slot[j];
-  const int n0 = s.n0;
-  const int na = *s.na;
-  const float dmin = s.D[(size_t)si * s.ld + sj];
-  if (threadIdx.x == 0) {
-    // TreeNode::join with left = min id, right = max id (overlaps the loop below)
-    const double Ti = s.T[si], Tj = s.T[sj];
-    double li, lj;
-    const double half = 0.5;
-    if (m_n == 2) {
-      li = lj = __dmul_rn((double)dmin, half);
-    } else {
-      const double nm2 = (double)(m_n - 2);
-      li = __dmul_rn(half, __dadd_rn((double)dmin, __ddiv_rn(__dsub_rn(Ti, Tj), nm2)));
-      lj = __dmul_rn(half, __dadd_rn((double)dmin, __ddiv_rn(__dsub_rn(Tj, Ti), nm2)));
-    }
-    if (li < 0.0) {
-      lj = __dsub_rn(lj, li);
-      li = 0.0;
-    } else if (lj < 0.0) {
-      li = __dsub_rn(li, lj);
-      lj = 0.0;
-    }
-    nwg_join& J = s.joins[step];
-    J.i = i;
-    J.j = j;
-    J.node = next;
-    J.n = m_n;
-    J.d = dmin;
-    J.pad = 0.f;
-    J.q = w.q1;
-    J.ti = Ti;
-    J.tj = Tj;
-    J.len_i = li;
-    J.len_j = lj;
-  }
-  // One pass over the active nodes k != i, j (SpeciesBlock.cpp:787-841):
-  // tmp = ((Dik + Djk) - d) / 2 in float, T[k] += (float)(tmp - (Dik + Djk)),
-  // the new row and column of slot si (its diagonal keeps i's old value), the
-  // old active list copied for the compaction, and the exponent range of tmp.
-  // Each thread reads and writes only its own k's entries of row si.
-  int lowexp = INT_MAX, topexp = INT_MIN;
-  for (int k = threadIdx.x; k < na; k += blockDim.x) {
-    const int v = s.act[k];
-    ids[k] = v;
-    if (v == i || v == j) {
-      s_skip[v == i ? 0 : 1] = k;
-      tv[k] = 0.f;
-      continue;
-    }
-    const int sk = s.slot[v];
-    const float Dik = s.D[(size_t)si * s.ld + sk];
-    const float Djk = s.D[(size_t)sj * s.ld + sk];
-    const float sumf = __fadd_rn(Dik, Djk);
-    const float tmp = __fmul_rn(__fsub_rn(sumf, dmin), 0.5f);
-    tv[k] = tmp;
-    const double t = __dadd_rn(s.T[sk], (double)__fsub_rn(tmp, sumf));
-    s.T[sk] = t;
-    s.Tf[sk] = (float)t;
-    s.D[(size_t)sk * s.ld + si] = tmp;
-    s.D[(size_t)si * s.ld + sk] = tmp;
-    lowexp = min(lowexp, low_bit_exp(tmp));
-    topexp = max(topexp, top_bit_exp(tmp));
-  }
-  // the new node's sum in ascending id order (SpeciesBlock.cpp:799, :818):
-  // the exact sum in 64-bit integers of 2^e (e = the lowest set bit of any
-  // term) when it proves every partial sum of the sequential loop exact, else
-  // the sequential loop itself
-  for (int o = 16; o > 0; o >>= 1) {
-    lowexp = min(lowexp, __shfl_xor_sync(0xffffffffu, lowexp, o));
-    topexp = max(topexp, __shfl_xor_sync(0xffffffffu, topexp, o));
-  }
-  if ((threadIdx.x & 31) == 0) {
-    s_low[threadIdx.x >> 5] = lowexp;
-    s_top[threadIdx.x >> 5] = topexp;
-  }
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    const int nw = (int)(blockDim.x >> 5);
-    lowexp = threadIdx.x < nw ? s_low[threadIdx.x] : INT_MAX;
-    topexp = threadIdx.x < nw ? s_top[threadIdx.x] : INT_MIN;
-    for (int o = 16; o > 0; o >>= 1) {
-      lowexp = min(lowexp, __shfl_xor_sync(0xffffffffu, lowexp, o));
-      topexp = max(topexp, __shfl_xor_sync(0xffffffffu, topexp, o));
-    }
-    if (threadIdx.x == 0) {
-      s_low[32] = lowexp;
-      s_top[32] = topexp;
-    }
-  }
-  __syncthreads();
-  lowexp = s_low[32];
-  topexp = s_top[32];
-  // every term below 2^49 units of 2^e: sums of up to 8192 terms stay below 2^62
-  const bool fits = lowexp == INT_MAX || topexp - lowexp < 48;
-  long long isum = 0, iabs = 0;
-  if (fits && lowexp != INT_MAX) {
-    for (int k = threadIdx.x; k < na; k += blockDim.x) {
-      const long long v = float_units(tv[k], lowexp);
-      isum += v;
-      iabs += v < 0 ? -v : v;
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      isum += __shfl_xor_sync(0xffffffffu, isum, o);
-      iabs += __shfl_xor_sync(0xffffffffu, iabs, o);
-    }
-    if ((threadIdx.x & 31) == 0) {
-      s_isum[threadIdx.x >> 5] = isum;
-      s_iabs[threadIdx.x >> 5] = iabs;
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    if (fits && lowexp != INT_MAX) {
-      const int nw = (int)(blockDim.x >> 5);
-      isum = threadIdx.x < nw ? s_isum[threadIdx.x] : 0;
-      iabs = threadIdx.x < nw ? s_iabs[threadIdx.x] : 0;
-      for (int o = 16; o > 0; o >>= 1) {
-        isum += __shfl_xor_sync(0xffffffffu, isum, o);
-        iabs += __shfl_xor_sync(0xffffffffu, iabs, o);
-      }
-    }
-    if (threadIdx.x == 0) {
-      double sum;
-      if (lowexp == INT_MAX) {
-        sum = 0.0;                                     // every term is zero
-      } else if (fits && iabs < (1ll << 53)) {
-        sum = ldexp((double)isum, lowexp);             // exact: |isum| < 2^53
-      } else {
-        const int ki = s_skip[0], kj = s_skip[1];
-        sum = 0.0;
-        for (int k = 0; k < na; ++k)
-          if (k != ki && k != kj) sum = __dadd_rn(sum, (double)tv[k]);
-      }
-      s.T[si] = sum;
-      s.Tf[si] = (float)sum;
-    }
-  }
-  // compacted active list: ascending ids without i (at ki) and j (at kj > ki),
-  // plus next at the end -- a shift of the old list
-  {
-    const int ki = s_skip[0], kj = s_skip[1];
-    for (int k = threadIdx.x; k < na - 2; k += blockDim.x) s.act[k] = ids[k < ki ? k : (k < kj - 1 ? k + 1 : k + 2)];
-  }
-  if (threadIdx.x == 0) {
-    s.act[na - 2] = next;
-    *s.na = na - 1;
-    s.slot[j] = -1;
-    s.slot[i] = -1;
-    s.slot[next] = si;
-    s.node[sj] = -1;
-    s.node[si] = next;
-  }
-  __syncthreads();
 }
 
 // ---- large n: one cooperative launch over the whole GPU per segment ---------
@@ -498,6 +217,13 @@ struct GCand {
   int pad;
 };
 
+// An entry of the fallback scan's list: the keys and the node ids (the
+// winner's slots, d and row sums are read again after the pick).
+struct KCand {
+  long long k1, k2;
+  int a, b;
+};
+
 struct GridNJ {
   unsigned* bar;        // [0] barrier arrivals (counts up from 0 per launch)
   int* abort;           // set when a barrier wait gave up; every CTA then leaves
@@ -508,7 +234,7 @@ struct GridNJ {
   float* part;          // [2 * grid]: per CTA smallest q and largest magnitude
   long long* jsum;      // [2 * grid]: per CTA integer sum and sum of magnitudes (units of 2^jexp)
   int* jexp;            // [2 * grid]: per CTA lowest and highest exponent of its values
-  GCand* cand;          // the candidate list of the fallback scan
+  KCand* cand;          // the candidate list of the fallback scan
 };
 
 constexpr long long kBarrierSpinCycles = 4000000000ll;   // about two seconds: no phase takes a millisecond
@@ -556,6 +282,22 @@ __device__ bool grid_barrier(const GridNJ& g, unsigned& target) {
   return s_ok != 0;
 }
 
+// The CTAs that run one job's join loop: the whole cooperative grid (large n)
+// or one thread-block cluster (a job per cluster).
+struct Team {
+  int rank, size;
+};
+
+template <bool CL>
+__device__ __forceinline__ bool team_sync(const GridNJ& g, unsigned& target) {
+  if constexpr (CL) {
+    cooperative_groups::this_cluster().sync();
+    return true;
+  } else {
+    return grid_barrier(g, target);
+  }
+}
+
 // Order-preserving map double -> int64 (finite values; -0 and +0 map alike).
 __device__ __forceinline__ long long dkey(double q) {
   long long b = __double_as_longlong(q);
@@ -590,15 +332,15 @@ __device__ __forceinline__ void pass_elem(float d, float tc, int c, float tr, fl
 
 // Odd joins scan every row backwards: the lines the previous pass read last
 // are still in L2 when the triangle is a little larger than L2.
-__device__ void grid_pass(const NJDev& s, const GridNJ& g, float nm2f, bool rev) {
+__device__ void grid_pass(const NJDev& s, const GridNJ& g, Team tm, float nm2f, bool rev) {
   __shared__ float sq[32], sm[32];
   const int lane = threadIdx.x & 31;
   const int n0 = s.n0, nv = s.ld >> 2;
-  const int nw = (int)gridDim.x * (int)(blockDim.x >> 5);
+  const int nw = tm.size * (int)(blockDim.x >> 5);
   const int npairs = (n0 + 1) >> 1;
   const float4* Tf4 = reinterpret_cast<const float4*>(s.Tf);
   float qmin = FLT_MAX, mmax = 0.f;
-  for (int p = (int)(threadIdx.x >> 5) * (int)gridDim.x + (int)blockIdx.x; p < npairs; p += nw) {
+  for (int p = (int)(threadIdx.x >> 5) * tm.size + tm.rank; p < npairs; p += nw) {
     for (int h = 0; h < 2; ++h) {
       if (n0 - 1 - p == p && h) break;
       const int r = (h != (int)rev) ? n0 - 1 - p : p;
@@ -661,8 +403,8 @@ __device__ void grid_pass(const NJDev& s, const GridNJ& g, float nm2f, bool rev)
       mmax = fmaxf(mmax, __shfl_xor_sync(0xffffffffu, mmax, o));
     }
     if (lane == 0) {
-      g.part[2 * blockIdx.x] = qmin;
-      g.part[2 * blockIdx.x + 1] = mmax;
+      g.part[2 * tm.rank] = qmin;
+      g.part[2 * tm.rank + 1] = mmax;
     }
   }
 }
@@ -693,12 +435,12 @@ __device__ __forceinline__ GCand make_cand(int r, int c, int ur, int uc, double 
 // Winner (smallest q1, then larger b, then larger a) and the ambiguity / tie
 // counts over nc candidates, by one warp; load(k) gives candidate k.
 template <class Load>
-__device__ PickOut pick_keys(int nc, Load&& load) {
+__device__ PickOut pick_keys(int nc, Load&& load) {   // load(k) has k1, k2, a, b
   const int l = threadIdx.x & 31;
   long long bk = LLONG_MAX, bk2 = LLONG_MAX;
   int ba = INT_MAX, bb = -1, bi = -1;
   for (int k = l; k < nc; k += 32) {
-    const GCand c = load(k);
+    const auto c = load(k);
     if (c.k1 < bk || (c.k1 == bk && (c.b > bb || (c.b == bb && c.a > ba)))) {
       bk = c.k1;
       bk2 = c.k2;
@@ -727,7 +469,7 @@ __device__ PickOut pick_keys(int nc, Load&& load) {
   const bool robust_w = bk == bk2;
   unsigned ties = 0, amb = 0;
   for (int k = l; k < nc; k += 32) {
-    const GCand c = load(k);
+    const auto c = load(k);
     if (min(c.k1, c.k2) > hiw) continue;
     if (c.a == ba && c.b == bb) ++ties;
     else if (robust_w && c.k1 == c.k2 && c.k1 == bk) ++ties;
@@ -747,7 +489,7 @@ __device__ PickOut pick_keys(int nc, Load&& load) {
 
 // K.  Returns 1 when the winner is in *win, 0 when the fallback scan is
 // needed (the same in every CTA).
-__device__ int grid_pick_direct(const NJDev& s, const GridNJ& g, double nm2, float nm2f, int watermark, GCand* win,
+__device__ int grid_pick_direct(const NJDev& s, const GridNJ& g, Team tm, double nm2, float nm2f, int watermark, GCand* win,
                                 PickOut* pk, float* sthr) {
   __shared__ int rows[kFastRows];
   __shared__ GCand fc[kFastRows];
@@ -768,7 +510,7 @@ __device__ int grid_pick_direct(const NJDev& s, const GridNJ& g, double nm2, flo
 #pragma unroll
     for (int t = 0; t < kGridMax / 32; ++t) {
       const int b = l + 32 * t;
-      if (b < (int)gridDim.x) {
+      if (b < tm.size) {
         const float2 pm = reinterpret_cast<const float2*>(g.part)[b];
         q = fminf(q, pm.x);
         m = fmaxf(m, pm.y);
@@ -836,7 +578,7 @@ __device__ int grid_pick_direct(const NJDev& s, const GridNJ& g, double nm2, flo
 
 // K, fallback: this CTA's slice of the columns of every row within the
 // threshold into the candidate list.
-__device__ void grid_cand(const NJDev& s, const GridNJ& g, float nm2f, double nm2, int watermark, float thr) {
+__device__ void grid_cand(const NJDev& s, const GridNJ& g, Team tm, float nm2f, double nm2, int watermark, float thr) {
   constexpr int kRows = 512;
   __shared__ int rows[kRows];
   __shared__ int nrows;
@@ -853,7 +595,7 @@ __device__ void grid_cand(const NJDev& s, const GridNJ& g, float nm2f, double nm
   __syncthreads();
   const bool all = nrows > kRows;   // more near-minimal rows than the list holds: every row
   const int nr = all ? n0 : nrows;
-  const int cstride = (int)gridDim.x * (int)blockDim.x;
+  const int cstride = tm.size * (int)blockDim.x;
   for (int t = 0; t < nr; ++t) {
     const int r = all ? t : rows[t];
     const int ur = s.node[r];
@@ -861,7 +603,7 @@ __device__ void grid_cand(const NJDev& s, const GridNJ& g, float nm2f, double nm
     const double Tr = s.T[r];
     if (ur < 0 || g.grmin[r] > othr) continue;
     const float* row = s.D + (size_t)r * s.ld;
-    for (int c = r + 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x); c < n0; c += cstride) {
+    for (int c = r + 1 + (int)(tm.rank * blockDim.x + threadIdx.x); c < n0; c += cstride) {
       const int uc = s.node[c];
       const float d = row[c];
       const float tcf = s.Tf[c];
@@ -870,7 +612,10 @@ __device__ void grid_cand(const NJDev& s, const GridNJ& g, float nm2f, double nm
       const float q = __fsub_rn(__fsub_rn(__fmul_rn(d, nm2f), tr), tcf);
       if (q > thr) continue;
       const int idx = atomicAdd(&s.g32[2], 1);
-      if (idx < s.cand_cap) g.cand[idx] = make_cand(r, c, ur, uc, Tr, Tc, d, nm2, watermark);
+      if (idx < s.cand_cap) {
+        const GCand cd = make_cand(r, c, ur, uc, Tr, Tc, d, nm2, watermark);
+        g.cand[idx] = KCand{cd.k1, cd.k2, cd.a, cd.b};
+      }
     }
   }
 }
@@ -919,14 +664,14 @@ __device__ __forceinline__ void usum_warp(USum& x) {
   }
 }
 
-__device__ void grid_join_share(const NJDev& s, const GridNJ& g, const GCand& w, int na, const int* act, int* act2) {
+__device__ void grid_join_share(const NJDev& s, const GridNJ& g, Team tm, const GCand& w, int na, const int* act, int* act2) {
   __shared__ USum swarp[32];
   const int i = w.a, j = w.b, si = w.sa, sj = w.sb;
   const float dmin = w.d;
   const int n0 = s.n0;
   const size_t ld = (size_t)s.ld;
-  const int per = (n0 + (int)gridDim.x - 1) / (int)gridDim.x;
-  const int p = (int)blockIdx.x * per + (int)threadIdx.x;
+  const int per = (n0 + tm.size - 1) / tm.size;
+  const int p = tm.rank * per + (int)threadIdx.x;
   USum x;
   x.u = x.a = 0;
   x.e = INT_MAX;
@@ -955,8 +700,8 @@ __device__ void grid_join_share(const NJDev& s, const GridNJ& g, const GCand& w,
     }
   }
   // the active list without i and j (ascending ids), shifted into act2
-  const int kper = (na + (int)gridDim.x - 1) / (int)gridDim.x;
-  const int k = (int)blockIdx.x * kper + (int)threadIdx.x;
+  const int kper = (na + tm.size - 1) / tm.size;
+  const int k = tm.rank * kper + (int)threadIdx.x;
   if ((int)threadIdx.x < kper && k < na) {
     const int v = act[k];
     if (v != i && v != j) act2[k - (v > i) - (v > j)] = v;
@@ -971,10 +716,10 @@ __device__ void grid_join_share(const NJDev& s, const GridNJ& g, const GCand& w,
       for (int w2 = 1; w2 < nwv; ++w2) usum_add(x, swarp[w2]);
   }
   if (threadIdx.x == 0) {
-    g.jsum[2 * blockIdx.x] = x.u;
-    g.jsum[2 * blockIdx.x + 1] = x.a;
-    g.jexp[2 * blockIdx.x] = x.e;
-    g.jexp[2 * blockIdx.x + 1] = x.t;
+    g.jsum[2 * tm.rank] = x.u;
+    g.jsum[2 * tm.rank + 1] = x.a;
+    g.jexp[2 * tm.rank] = x.e;
+    g.jexp[2 * tm.rank + 1] = x.t;
   }
 }
 
@@ -985,8 +730,9 @@ __device__ void grid_join_share(const NJDev& s, const GridNJ& g, const GCand& w,
 // record (TreeNode::join's inputs; the lengths follow after the loop) and the
 // id -> slot map.  When the integer sum cannot be used, CTA 0 runs the
 // sequential loop and one more grid barrier follows.
-__device__ bool grid_join_apply(const NJDev& s, const GridNJ& g, const GCand& w, const PickOut& pk, int step, int n,
-                                const int* act_old, int* act_new, unsigned& target) {
+template <bool CL>
+__device__ bool grid_join_apply(const NJDev& s, const GridNJ& g, Team tm, const GCand& w, const PickOut& pk, int step,
+                                int n, const int* act_old, int* act_new, unsigned& target) {
   __shared__ double s_sum;
   __shared__ int s_exact;
   const int i = w.a, j = w.b, si = w.sa, sj = w.sb;
@@ -1003,7 +749,7 @@ __device__ bool grid_join_apply(const NJDev& s, const GridNJ& g, const GCand& w,
       const int b = l + 32 * t;
       je[t] = INT_MAX;
       jsv[t] = jav[t] = 0;
-      if (b < (int)gridDim.x) {
+      if (b < tm.size) {
         je[t] = g.jexp[2 * b];
         jsv[t] = g.jsum[2 * b];
         jav[t] = g.jsum[2 * b + 1];
@@ -1050,7 +796,7 @@ __device__ bool grid_join_apply(const NJDev& s, const GridNJ& g, const GCand& w,
     if (exact) {
       s.T[si] = s_sum;
       s.Tf[si] = __double2float_rn(s_sum);
-    } else if (blockIdx.x == 0) {
+    } else if (tm.rank == 0) {
       double sum = 0.0;   // the reference's loop: active ids ascending, i and j skipped
       for (int k = 0; k < m_n; ++k) {
         const int v = act_old[k];
@@ -1062,7 +808,7 @@ __device__ bool grid_join_apply(const NJDev& s, const GridNJ& g, const GCand& w,
     s.Tf[sj] = __int_as_float(0x7FC00000);   // dead: NaN
     s.node[sj] = -1;
     s.node[si] = next;
-    if (blockIdx.x == 0) {
+    if (tm.rank == 0) {
       nwg_join& J = s.joins[step];
       J.i = i;
       J.j = j;
@@ -1082,18 +828,62 @@ __device__ bool grid_join_apply(const NJDev& s, const GridNJ& g, const GCand& w,
       record_pick(s, pk);
     }
   }
-  if (!exact) return grid_barrier(g, target);   // T[si] from CTA 0
+  if (!exact) return team_sync<CL>(g, target);   // T[si] from CTA 0
   __syncthreads();
   return true;
 }
 
-// Joins step0 .. step1-1 of an n-taxon job (the active count before join t
-// is n - t).
+// One join of the team: pass, pick, share.  False when the team stops (a
+// barrier gave up or the pick failed -- the same in every CTA).
+template <bool CL>
+__device__ bool team_join(const NJDev& s, const GridNJ& g, Team tm, int step, int n, int watermark, int*& act,
+                          int*& act2, PickOut& spick, GCand& swin, float& sthr, unsigned& target) {
+  const int m_n = n - step;
+  const float nm2f = (float)(m_n - 2);
+  const double nm2 = (double)(m_n - 2);
+  grid_pass(s, g, tm, nm2f, (step & 1) != 0);
+  if (!team_sync<CL>(g, target)) return false;
+  if (!grid_pick_direct(s, g, tm, nm2, nm2f, watermark, &swin, &spick, &sthr)) {
+    grid_cand(s, g, tm, nm2f, nm2, watermark, sthr);
+    if (!team_sync<CL>(g, target)) return false;
+    if (threadIdx.x < 32) {
+      const int ncount = s.g32[2];
+      const int nc = min(ncount, s.cand_cap);
+      PickOut r = pick_keys(nc, [&](int k) { return g.cand[k]; });
+      r.error = r.error || ncount > s.cand_cap;
+      if (threadIdx.x == 0) {
+        spick = r;
+        if (!r.error) {
+          // the winner's pair again, as the scan read it (row = the smaller slot)
+          const KCand w = g.cand[r.idx];
+          const int sa = s.slot[w.a], sb = s.slot[w.b];
+          const int r0 = min(sa, sb), c0 = max(sa, sb);
+          swin = make_cand(r0, c0, s.node[r0], s.node[c0], s.T[r0], s.T[c0], s.D[(size_t)r0 * s.ld + c0], nm2,
+                           watermark);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (spick.error) {
+    if (tm.rank == 0 && threadIdx.x == 0) record_pick(s, spick);
+    return false;
+  }
+  grid_join_share(s, g, tm, swin, m_n, act, act2);
+  int* t = act;
+  act = act2;
+  act2 = t;
+  return team_sync<CL>(g, target);
+}
+
+// Joins step0 .. step1-1 of an n-taxon job over the whole GPU (the active
+// count before join t is n - t).
 __global__ void __launch_bounds__(1024, 1) nj_grid_kernel(NJDev s, GridNJ g, int step0, int step1, int n,
                                                          int watermark) {
   __shared__ PickOut spick;
   __shared__ GCand swin;
   __shared__ float sthr;
+  const Team tm{(int)blockIdx.x, (int)gridDim.x};
   unsigned target = 0;
   for (int p = (int)(blockIdx.x * blockDim.x + threadIdx.x); p < s.n0; p += (int)(gridDim.x * blockDim.x))
     g.grmin[p] = 0x7F7FFFFF;   // ordered int of FLT_MAX
@@ -1102,50 +892,17 @@ __global__ void __launch_bounds__(1024, 1) nj_grid_kernel(NJDev s, GridNJ g, int
   int* act = s.act;
   int* act2 = g.act2;
   for (int step = step0; step < step1; ++step) {
-    if (step > step0) {
-      // the previous join's new list is act (swapped below), its old one act2
-      if (!grid_join_apply(s, g, swin, spick, step - 1, n, act2, act, target)) return;
-    }
-    const int m_n = n - step;
-    const float nm2f = (float)(m_n - 2);
-    const double nm2 = (double)(m_n - 2);
-    grid_pass(s, g, nm2f, (step & 1) != 0);
-    if (!grid_barrier(g, target)) return;
-    if (!grid_pick_direct(s, g, nm2, nm2f, watermark, &swin, &spick, &sthr)) {
-      grid_cand(s, g, nm2f, nm2, watermark, sthr);
-      if (!grid_barrier(g, target)) return;
-      if (threadIdx.x < 32) {
-        const int ncount = s.g32[2];
-        const int nc = min(ncount, s.cand_cap);
-        PickOut r = pick_keys(nc, [&](int k) { return g.cand[k]; });
-        r.error = r.error || ncount > s.cand_cap;
-        if (threadIdx.x == 0) {
-          spick = r;
-          if (!r.error) swin = g.cand[r.idx];
-        }
-      }
-      __syncthreads();
-    }
-    if (spick.error) {   // the same in every CTA
-      if (blockIdx.x == 0 && threadIdx.x == 0) record_pick(s, spick);
-      return;
-    }
-    grid_join_share(s, g, swin, m_n, act, act2);
-    int* t = act;
-    act = act2;
-    act2 = t;
-    if (!grid_barrier(g, target)) return;
+    // the previous join's new list is act, its old one act2
+    if (step > step0 && !grid_join_apply<false>(s, g, tm, swin, spick, step - 1, n, act2, act, target)) return;
+    if (!team_join<false>(s, g, tm, step, n, watermark, act, act2, spick, swin, sthr, target)) return;
   }
-  if (step1 > step0) grid_join_apply(s, g, swin, spick, step1 - 1, n, act2, act, target);
+  if (step1 > step0) grid_join_apply<false>(s, g, tm, swin, spick, step1 - 1, n, act2, act, target);
 }
 
-// TreeNode::join (TreeNode.cpp:31-58) for the joins the grid kernel recorded:
-// L_i = (d + (T_i - T_j)/(n-2)) / 2, L_j likewise, n = 2 gives d/2 each, a
-// negative side is clamped to 0 and moved to the other.
-__global__ void nj_lengths_kernel(nwg_join* joins, int count) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= count) return;
-  nwg_join& J = joins[k];
+// TreeNode::join (TreeNode.cpp:31-58) for a recorded join: L_i = (d + (T_i -
+// T_j)/(n-2)) / 2, L_j likewise, n = 2 gives d/2 each, a negative side is
+// clamped to 0 and moved to the other.
+__device__ void join_lengths(nwg_join& J) {
   const double half = 0.5;
   double li, lj;
   if (J.n == 2) {
@@ -1164,6 +921,11 @@ __global__ void nj_lengths_kernel(nwg_join* joins, int count) {
   }
   J.len_i = li;
   J.len_j = lj;
+}
+
+__global__ void nj_lengths_kernel(nwg_join* joins, int count) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < count) join_lengths(joins[k]);
 }
 
 // Compaction, part 1 (one CTA): map[p] = new slot of live slot p (ascending),
@@ -1226,43 +988,32 @@ __global__ void __launch_bounds__(256) compact_copy_kernel(NJDev s, const int* m
   }
 }
 
-// ---- one job per thread-block cluster (serving and small matrices) ----------
+// ---- one job per thread-block cluster (serving and up to 2048 taxa) --------
+// The same phases as the large-n form, with the C CTAs of a cluster as the
+// team and hardware cluster barriers between the phases; the reference's
+// rebuild schedule runs inside the kernel (row sums over the cluster, no
+// compaction: the matrix stays in L2).
 
 struct NJJob {
   NJDev s;
+  GridNJ g;
   int n;
+  int pad;
 };
 
-// Shared-memory copies of the float row sums and the slot -> node map; the
-// row minima of the next pass start at +inf (ordered-int encoding).
-__device__ void cta_refresh(const NJDev& s, float* sTf, int* snode, int* srmin) {
-  for (int k = threadIdx.x; k < s.n0; k += blockDim.x) {
-    sTf[k] = s.Tf[k];
-    snode[k] = s.node[k];
-    srmin[k] = 0x7F7FFFFF;
-  }
-  __syncthreads();
-}
-
-// The join loop, schedule included (as the host loop of the large-n path),
-// with the O(n^2) passes split over the C CTAs
-// of a cluster (rows dealt to the cluster's warps round robin), the global
-// minimum and magnitude combined through distributed shared memory, and
-// hardware cluster barriers between the phases.  The pick and the join are
-// O(n) and run on rank 0; every rank keeps shared-memory copies of the float
-// row sums and the slot -> node map.  Dynamic shared memory: 5 arrays of the
-// largest n of the launch (tv, ids, sTf, snode, srmin).
-
-__device__ void clu_rowsums(const NJDev& s, int w0, int wstride) {
+// Sequential row sums (buildGblRowSums, SpeciesBlock.cpp:426-453) over the
+// active list, one warp per row, warps w0, w0 + wstride, ...; the lanes'
+// any-order sum is used when it is provably exact, else lane 0 sums in order.
+__device__ void team_rowsums(const NJDev& s, const int* act, int w0, int wstride) {
   const int na = *s.na;
   const int lane = threadIdx.x & 31;
   for (int k = w0; k < na; k += wstride) {
-    const int sk = s.slot[s.act[k]];
+    const int sk = s.slot[act[k]];
     const float* row = s.D + (size_t)sk * s.ld;
     double part = 0.0, ab = 0.0;
     int lowexp = INT_MAX;
     for (int j = lane; j < na; j += 32) {
-      const float x = row[s.slot[s.act[j]]];
+      const float x = row[s.slot[act[j]]];
       part = __dadd_rn(part, (double)x);
       ab = __dadd_rn(ab, (double)fabsf(x));
       lowexp = min(lowexp, low_bit_exp(x));
@@ -1276,254 +1027,106 @@ __device__ void clu_rowsums(const NJDev& s, int w0, int wstride) {
       double sum = part;
       if (!sum_is_exact(ab, lowexp)) {
         sum = 0.0;
-        for (int j = 0; j < na; ++j) sum = __dadd_rn(sum, (double)row[s.slot[s.act[j]]]);
+        for (int j = 0; j < na; ++j) sum = __dadd_rn(sum, (double)row[s.slot[act[j]]]);
       }
       s.T[sk] = sum;
-      s.Tf[sk] = (float)sum;
+      s.Tf[sk] = __double2float_rn(sum);
     }
   }
-}
-
-// Rows are dealt to the cluster's warps as folded slot pairs (p, n0-1-p):
-// row r has n0-1-r entries right of the diagonal, so every pair holds about
-// n0 of them.  With fewer pairs than warps, a pair is split over f warps of
-// one CTA (f a power of two, at most 32), each taking every f-th group of 32
-// columns of both rows; the row minima then meet in the CTA's shared memory.
-// Dead slots are skipped.  fn(row, first column offset, column stride).
-struct RowSplit {
-  int f;        // warps per pair
-  int unit;     // this warp's first unit (pair * f + share)
-  int ustride;  // units between this warp's units
-  int npairs;
-};
-
-__device__ __forceinline__ RowSplit row_split(int n0, int C) {
-  const int nw = C * (int)(blockDim.x >> 5);
-  const int npairs = (n0 + 1) >> 1;
-  int f = 1;
-  while (f < 32 && npairs * (f * 2) <= nw) f *= 2;
-  RowSplit rs;
-  rs.f = f;
-  rs.npairs = npairs;
-  // warp g of the cluster (rank-major) owns units g, g + nw, ...; the f units
-  // of a pair are consecutive warps of one CTA
-  rs.unit = (int)cooperative_groups::this_cluster().block_rank() * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5);
-  rs.ustride = nw;
-  return rs;
-}
-
-template <class Fn>
-__device__ __forceinline__ void for_my_rows(int n0, const int* __restrict__ snode, const RowSplit& rs, Fn&& fn) {
-  for (int u = rs.unit; u < rs.npairs * rs.f; u += rs.ustride) {
-    const int p = u / rs.f, share = u - p * rs.f;
-    if (snode[p] >= 0) fn(p, share * 32, rs.f * 32);
-    const int q = n0 - 1 - p;
-    if (q != p && snode[q] >= 0) fn(q, share * 32, rs.f * 32);
-  }
-}
-
-__device__ __forceinline__ int ford_s(float f) {
-  const int b = __float_as_int(f);
-  return b >= 0 ? b : b ^ 0x7FFFFFFF;
-}
-__device__ __forceinline__ float iord_s(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7FFFFFFF); }
-
-// This CTA's rows: the smallest float q and the largest magnitude, reduced
-// over the block into part[0], part[1]; srmin[r] (ordered int, set to the
-// encoding of FLT_MAX beforehand) = the row's smallest q.
-__device__ void clu_pass_min(const NJDev& s, float nm2f, const float* __restrict__ sTf, const int* __restrict__ snode,
-                             int* __restrict__ srmin, const RowSplit& rs, float* part) {
-  __shared__ float sq[32], sm[32];
-  const int lane = threadIdx.x & 31;
-  float qmin = FLT_MAX, mmax = 0.f;
-  for_my_rows(s.n0, snode, rs, [&](int r, int c0, int cstride) {
-    const float tr = sTf[r];
-    const float* row = s.D + (size_t)r * s.ld;
-    float rq = FLT_MAX;
-#pragma unroll 4
-    for (int c = r + 1 + c0 + lane; c < s.n0; c += cstride) {
-      // branch-free: a dead slot's (finite, stale) entries are masked out
-      const float d = row[c];
-      const bool live = snode[c] >= 0;
-      const float tc = sTf[c];
-      const float x = __fmul_rn(d, nm2f);
-      const float q = __fsub_rn(__fsub_rn(x, tr), tc);
-      const float mag = __fadd_rn(__fadd_rn(fabsf(x), fabsf(tr)), fabsf(tc));
-      rq = fminf(rq, live ? q : FLT_MAX);
-      mmax = fmaxf(mmax, live ? mag : 0.f);
-    }
-    for (int o = 16; o > 0; o >>= 1) rq = fminf(rq, __shfl_xor_sync(0xffffffffu, rq, o));
-    if (lane == 0) {
-      if (rs.f == 1) srmin[r] = ford_s(rq);
-      else atomicMin(&srmin[r], ford_s(rq));
-    }
-    qmin = fminf(qmin, rq);
-  });
-  for (int o = 16; o > 0; o >>= 1) mmax = fmaxf(mmax, __shfl_xor_sync(0xffffffffu, mmax, o));
-  if (lane == 0) {
-    sq[threadIdx.x >> 5] = qmin;
-    sm[threadIdx.x >> 5] = mmax;
-  }
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    const int nw = (int)(blockDim.x >> 5);
-    qmin = lane < nw ? sq[lane] : FLT_MAX;
-    mmax = lane < nw ? sm[lane] : 0.f;
-    for (int o = 16; o > 0; o >>= 1) {
-      qmin = fminf(qmin, __shfl_xor_sync(0xffffffffu, qmin, o));
-      mmax = fmaxf(mmax, __shfl_xor_sync(0xffffffffu, mmax, o));
-    }
-    if (lane == 0) {
-      part[0] = qmin;
-      part[1] = mmax;
-    }
-  }
-}
-
-__device__ void clu_pass_cand(const NJDev& s, float nm2f, double nm2, int watermark, float thr,
-                              const float* __restrict__ sTf, const int* __restrict__ snode,
-                              const int* __restrict__ srmin, const RowSplit& rs) {
-  const int lane = threadIdx.x & 31;
-  for_my_rows(s.n0, snode, rs, [&](int r, int c0, int cstride) {
-    if (iord_s(srmin[r]) > thr) return;   // no pair of this row is a candidate
-    const int ur = snode[r];
-    const float tr = sTf[r];
-    const float* row = s.D + (size_t)r * s.ld;
-    for (int c = r + 1 + c0 + lane; c < s.n0; c += cstride) {
-      const float d = row[c];
-      const int uc = snode[c];
-      if (uc < 0) continue;
-      const float q = __fsub_rn(__fsub_rn(__fmul_rn(d, nm2f), tr), sTf[c]);
-      if (q > thr) continue;
-      const int a = min(ur, uc), b = max(ur, uc);
-      Cand cd;
-      cd.q1 = q_record(s, d, a, b, watermark, nm2);
-      cd.q2 = q_heap(s, d, a, b, nm2);
-      cd.a = a;
-      cd.b = b;
-      const int idx = atomicAdd(&s.g32[2], 1);
-      if (idx < s.cand_cap) s.cand[idx] = cd;
-    }
-  });
 }
 
 template <int C>
-__global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_cluster_kernel(const NJJob* jobs, int njobs,
-                                                                                     int nmax) {
-  namespace cg = cooperative_groups;
-  extern __shared__ __align__(16) unsigned char nj_smem[];
-  float* tv = reinterpret_cast<float*>(nj_smem);
-  int* ids = reinterpret_cast<int*>(tv + nmax);
-  float* sTf = reinterpret_cast<float*>(ids + nmax);
-  int* snode = reinterpret_cast<int*>(sTf + nmax);
-  int* srmin = snode + nmax;   // per slot, ordered-int row minimum
-  __shared__ float part[2];   // this CTA's pass-1 partial (read by the other ranks)
-  __shared__ float glob[2];   // the cluster's minimum and magnitude
-  cg::cluster_group cl = cg::this_cluster();
-  const int rank = (int)cl.block_rank();
-  const int job = (int)blockIdx.x / C;           // the same for every CTA of the cluster
+__global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_cluster_kernel(const NJJob* jobs, int njobs) {
+  __shared__ PickOut spick;
+  __shared__ GCand swin;
+  __shared__ float sthr;
+  __shared__ NJJob sjob;   // the job's descriptor (shared memory keeps registers free)
+  const int job = (int)blockIdx.x / C;   // the same for every CTA of the cluster
   if (job >= njobs) return;
-  const NJJob J = jobs[job];
-  const NJDev& s = J.s;
-  const int n = J.n;
-  const int w0 = rank * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5);
+  if (threadIdx.x == 0) sjob = jobs[job];
+  __syncthreads();
+  const NJDev& s = sjob.s;
+  const GridNJ& g = sjob.g;
+  const int n = sjob.n;
+  const Team tm{(int)cooperative_groups::this_cluster().block_rank(), C};
+  const int w0 = tm.rank * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5);
   const int wstride = C * (int)(blockDim.x >> 5);
-  const RowSplit rs = row_split(n, C);
-  if (rank == 0) {
-    for (int k = threadIdx.x; k < 2 * n - 1; k += blockDim.x) s.slot[k] = k < n ? k : -1;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-      s.node[k] = k;
-      s.act[k] = k;
-    }
-    if (threadIdx.x == 0) {
-      *s.na = n;
-      s.g32[2] = 0;
-      s.stats[0] = s.stats[1] = s.stats[2] = s.stats[3] = s.stats[4] = 0;
-    }
+  const int t0 = tm.rank * (int)blockDim.x + (int)threadIdx.x, tstride = C * (int)blockDim.x;
+  unsigned target = 0;   // (grid barriers only)
+  for (int k = t0; k < 2 * n - 1; k += tstride) s.slot[k] = k < n ? k : -1;
+  for (int k = t0; k < n; k += tstride) {
+    s.node[k] = k;
+    s.act[k] = k;
+    g.grmin[k] = 0x7F7FFFFF;
   }
-  cl.sync();
+  for (int k = n + t0; k < s.ld; k += tstride) s.Tf[k] = __int_as_float(0x7FC00000);   // padding: NaN
+  if (tm.rank == 0 && threadIdx.x == 0) {
+    *s.na = n;
+    s.g32[2] = 0;
+    s.stats[0] = s.stats[1] = s.stats[2] = s.stats[3] = s.stats[4] = 0;
+  }
+  cooperative_groups::this_cluster().sync();
   if (n < 2) return;
-  clu_rowsums(s, w0, wstride);
-  cl.sync();
-  cta_refresh(s, sTf, snode, srmin);
+  team_rowsums(s, s.act, w0, wstride);
+  cooperative_groups::this_cluster().sync();
+  // the reference's schedule (SpeciesBlock.cpp:864, :1206-1247)
   const int kBinT = 30 * 31 / 2;
   int steps = max((int)((float)n * 0.5f), 200);
   int pq_ck = 500;
   long long ave0 = (((long long)(n - 1) * n) / 2) / kBinT;
   long long ub = ((long long)n * (n - 1)) / 2;
-  int watermark = n, next = n, m_n = n, na = n;
+  int watermark = n;
+  int* act = s.act;
+  int* act2 = g.act2;
+  bool pending = false;   // a join whose row sum and maps are still to be written
   for (int step = 0; step < n - 1; ++step) {
-    const double nm2 = (double)(m_n - 2);
-    const float nm2f = (float)(m_n - 2);
-    clu_pass_min(s, nm2f, sTf, snode, srmin, rs, part);
-    cl.sync();
-    if (threadIdx.x < 32) {
-      const int l = threadIdx.x;
-      float q = FLT_MAX, m = 0.f;
-      if (l < C) {
-        const float* rp = cl.map_shared_rank(part, l);
-        q = rp[0];
-        m = rp[1];
-      }
-      for (int o = 16; o > 0; o >>= 1) {
-        q = fminf(q, __shfl_xor_sync(0xffffffffu, q, o));
-        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-      }
-      if (l == 0) {
-        glob[0] = q;
-        glob[1] = m;
-      }
-    }
-    __syncthreads();
-    const float thr = glob[0] + 3.f * (8.f * 5.9604645e-8f * glob[1]) + 1e-30f;
-    clu_pass_cand(s, nm2f, nm2, watermark, thr, sTf, snode, srmin, rs);
-    cl.sync();
-    if (rank == 0) {
-      pick_body(s);
-      join_body(s, step, next, m_n, tv, ids);
-    }
+    if (pending) grid_join_apply<true>(s, g, tm, swin, spick, step - 1, n, act2, act, target);
+    if (!team_join<true>(s, g, tm, step, n, watermark, act, act2, spick, swin, sthr, target)) return;
+    pending = true;
     if (--pq_ck == 0) {
       pq_ck = 500;
-      if (steps > 0 && (double)(ub / kBinT) / (double)ave0 > 2.0 && rank == 0 && threadIdx.x == 0) s.stats[3] += 1;
+      if (steps > 0 && (double)(ub / kBinT) / (double)ave0 > 2.0 && tm.rank == 0 && threadIdx.x == 0) s.stats[3] += 1;
     }
-    --m_n;
-    na -= 1;
-    ++next;
-    cl.sync();
+    const int m_after = n - step - 1;
     if (steps == 0) {
-      clu_rowsums(s, w0, wstride);
-      if (rank == 0 && threadIdx.x == 0) s.stats[4] += 1;
-      watermark = next;
-      steps = (m_n < 200) ? INT_MAX : (int)((float)m_n * 0.5f);
-      ave0 = (((long long)(m_n - 1) * m_n) / 2) / kBinT;
-      ub = ((long long)m_n * (m_n - 1)) / 2;
-      cl.sync();
+      grid_join_apply<true>(s, g, tm, swin, spick, step, n, act2, act, target);
+      pending = false;
+      cooperative_groups::this_cluster().sync();
+      team_rowsums(s, act, w0, wstride);
+      if (tm.rank == 0 && threadIdx.x == 0) s.stats[4] += 1;
+      watermark = n + step + 1;
+      steps = (m_after < 200) ? INT_MAX : (int)((float)m_after * 0.5f);
+      ave0 = (((long long)(m_after - 1) * m_after) / 2) / kBinT;
+      ub = ((long long)m_after * (m_after - 1)) / 2;
+      cooperative_groups::this_cluster().sync();
     } else {
       --steps;
-      ub += na - 1;
+      ub += m_after - 1;
     }
-    cta_refresh(s, sTf, snode, srmin);
   }
-  cl.sync();   // no rank leaves while another may still read its shared memory
+  if (pending) grid_join_apply<true>(s, g, tm, swin, spick, n - 2, n, act2, act, target);
+  cooperative_groups::this_cluster().sync();
+  for (int k = t0; k < n - 1; k += tstride) join_lengths(s.joins[k]);
 }
 
 }  // namespace
 
 struct NJState {
-  DevBuf D, T, Tf, slot, node, act, na, g32, cand, win, stats, joins, vd, rmin, desc;
-  // large-n path: compaction buffers, second active list, grid partials and barrier words
-  DevBuf D2, T2, Tf2, node2, map, act2, part, jsum, jexp, gbar, grec;
+  DevBuf D, jobws, desc;
+  // large-n path: row sums, maps, compaction buffers, candidates, grid partials and barrier words
+  DevBuf T, Tf, slot, node, act, na, g32, stats, joins, cand, tv, grmin, grec;
+  DevBuf D2, T2, Tf2, node2, map, act2, part, jsum, jexp, gbar;
   ~NJState() {
-    for (DevBuf* b : {&D, &T, &Tf, &slot, &node, &act, &na, &g32, &cand, &win, &stats, &joins, &vd, &rmin, &desc, &D2,
-                      &T2, &Tf2, &node2, &map, &act2, &part, &jsum, &jexp, &gbar, &grec})
+    for (DevBuf* b : {&D, &jobws, &desc, &T, &Tf, &slot, &node, &act, &na, &g32, &stats, &joins, &cand, &tv, &grmin,
+                      &grec, &D2, &T2, &Tf2, &node2, &map, &act2, &part, &jsum, &jexp, &gbar})
       b->release();
   }
 };
 
 // Up to this many taxa one cluster runs the whole join loop (the matrix stays
-// in L2); larger matrices take the full-GPU first pass per join.  The
-// environment variable NWG_NJ_CLUSTER_MAX_N overrides the threshold (both
-// paths give the same joins; the tests run each path on the same inputs).
+// in L2); larger matrices take the whole GPU per join.  The environment
+// variable NWG_NJ_CLUSTER_MAX_N overrides the threshold (both forms give the
+// same joins; the tests run each form on the same inputs).
 int cluster_nj_max_n() {
   static const int v = [] {
     const char* e = std::getenv("NWG_NJ_CLUSTER_MAX_N");
@@ -1550,65 +1153,67 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
   NJState& S = *reinterpret_cast<NJState*>(nj_state);
   const int nn = 2 * n - 1;
   const bool big = n > cluster_nj_max_n();
+  const int ldd = nj_row_stride(n);   // rows padded to a multiple of 4 floats (16-byte loads)
   int rc;
-  // the large-n path pads rows to a multiple of 4 floats (16-byte loads)
-  const int ldd = big ? (n + 3) & ~3 : n;
-  if ((rc = S.D.ensure(sizeof(float) * (size_t)n * ldd)) || (rc = S.T.ensure(sizeof(double) * n)) ||
-      (rc = S.Tf.ensure(sizeof(float) * ldd)) || (rc = S.slot.ensure(sizeof(int) * nn)) ||
-      (rc = S.node.ensure(sizeof(int) * n)) || (rc = S.act.ensure(sizeof(int) * (n + 1))) ||
-      (rc = S.na.ensure(sizeof(int))) || (rc = S.g32.ensure(sizeof(int) * 4)) ||
-      (rc = S.cand.ensure(std::max(sizeof(Cand), sizeof(GCand)) * kCandCap)) || (rc = S.win.ensure(sizeof(Pick))) ||
-      (rc = S.stats.ensure(sizeof(unsigned long long) * 5)) ||
-      (rc = S.joins.ensure(sizeof(nwg_join) * (n - 1))) || (rc = S.vd.ensure(sizeof(float) * n)) ||
-      (rc = S.rmin.ensure(sizeof(float) * n)) || (rc = S.desc.ensure(sizeof(NJJob))))
-    return fail(rc, "nj allocation");
-  // one CTA of 1024 threads per SM (cooperative launch); every join share
-  // then holds at most one slot per thread
-  const int grid = std::min(sms, kGridMax);
-  if (big && ((rc = S.D2.ensure(sizeof(float) * (size_t)n * ldd)) || (rc = S.T2.ensure(sizeof(double) * n)) ||
-              (rc = S.Tf2.ensure(sizeof(float) * ldd)) || (rc = S.node2.ensure(sizeof(int) * n)) ||
-              (rc = S.map.ensure(sizeof(int) * n)) || (rc = S.act2.ensure(sizeof(int) * (n + 1))) ||
-              (rc = S.part.ensure(sizeof(float) * 2 * grid)) || (rc = S.jsum.ensure(sizeof(long long) * 2 * grid)) ||
-              (rc = S.jexp.ensure(sizeof(int) * 2 * grid)) || (rc = S.gbar.ensure(sizeof(int) * 4)) ||
-              (rc = S.grec.ensure(sizeof(int2) * n))))
-    return fail(rc, "nj allocation");
+  if ((rc = S.D.ensure(sizeof(float) * (size_t)n * ldd))) return fail(rc, "nj allocation");
   cudaStream_t s = stream;
   const cudaMemcpyKind kind = device_D ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   if ((rc = cuda(cudaMemcpy2DAsync(S.D.p, sizeof(float) * ldd, D, sizeof(float) * ld, sizeof(float) * n, n, kind, s),
                  "nj upload")))
     return rc;
-  NJDev d{};
-  d.D = (float*)S.D.p;
-  d.T = (double*)S.T.p;
-  d.Tf = (float*)S.Tf.p;
-  d.slot = (int*)S.slot.p;
-  d.node = (int*)S.node.p;
-  d.act = (int*)S.act.p;
-  d.na = (int*)S.na.p;
-  d.g32 = (int*)S.g32.p;
-  d.cand = (Cand*)S.cand.p;
-  d.win = (Pick*)S.win.p;
-  d.stats = (unsigned long long*)S.stats.p;
-  d.joins = (nwg_join*)S.joins.p;
-  d.vd = (float*)S.vd.p;
-  d.rmin = (float*)S.rmin.p;
-  d.n0 = n;
-  d.ld = ldd;
-  d.cand_cap = kCandCap;
+  const void* jsrc;   // join records and statistics on the device
+  const void* ssrc;
   if (!big) {
+    if ((rc = S.jobws.ensure(nj_job_workspace(n))) || (rc = S.desc.ensure(sizeof(NJJob))))
+      return fail(rc, "nj allocation");
     NJJob J{};
-    J.s = d;
-    J.n = n;
+    nwg_join* jp;
+    unsigned long long* sp;
+    nj_job_setup(&J, (float*)S.D.p, n, ldd, (char*)S.jobws.p, &jp, &sp);
+    jsrc = jp;
+    ssrc = sp;
     // the descriptor travels in the stream (a pageable copy is staged at once)
     if ((rc = cuda(cudaMemcpyAsync(S.desc.p, &J, sizeof(J), cudaMemcpyHostToDevice, s), "nj upload"))) return rc;
     if (st) cudaEventRecord(ev0, s);
-    if ((rc = cuda(launch_nj_cluster(S.desc.p, 1, n, nj_cluster_size(), s), "nj launch"))) return rc;
+    if ((rc = cuda(launch_nj_cluster(S.desc.p, 1, nj_cluster_size(), s), "nj launch"))) return rc;
     ++launches;
   } else {
+    // one CTA of 1024 threads per SM (cooperative launch); every join share
+    // then holds at most one slot per thread
+    const int grid = std::min(sms, kGridMax);
+    if ((rc = S.T.ensure(sizeof(double) * n)) || (rc = S.Tf.ensure(sizeof(float) * ldd)) ||
+        (rc = S.slot.ensure(sizeof(int) * nn)) || (rc = S.node.ensure(sizeof(int) * n)) ||
+        (rc = S.act.ensure(sizeof(int) * (n + 1))) || (rc = S.na.ensure(sizeof(int))) ||
+        (rc = S.g32.ensure(sizeof(int) * 4)) || (rc = S.stats.ensure(sizeof(unsigned long long) * 5)) ||
+        (rc = S.joins.ensure(sizeof(nwg_join) * (n - 1))) || (rc = S.cand.ensure(sizeof(KCand) * kCandCap)) ||
+        (rc = S.tv.ensure(sizeof(float) * n)) || (rc = S.grmin.ensure(sizeof(int) * n)) ||
+        (rc = S.grec.ensure(sizeof(int2) * n)) || (rc = S.D2.ensure(sizeof(float) * (size_t)n * ldd)) ||
+        (rc = S.T2.ensure(sizeof(double) * n)) || (rc = S.Tf2.ensure(sizeof(float) * ldd)) ||
+        (rc = S.node2.ensure(sizeof(int) * n)) || (rc = S.map.ensure(sizeof(int) * n)) ||
+        (rc = S.act2.ensure(sizeof(int) * (n + 1))) || (rc = S.part.ensure(sizeof(float) * 2 * grid)) ||
+        (rc = S.jsum.ensure(sizeof(long long) * 2 * grid)) || (rc = S.jexp.ensure(sizeof(int) * 2 * grid)) ||
+        (rc = S.gbar.ensure(sizeof(int) * 4)))
+      return fail(rc, "nj allocation");
+    NJDev d{};
+    d.D = (float*)S.D.p;
+    d.T = (double*)S.T.p;
+    d.Tf = (float*)S.Tf.p;
+    d.slot = (int*)S.slot.p;
+    d.node = (int*)S.node.p;
+    d.act = (int*)S.act.p;
+    d.na = (int*)S.na.p;
+    d.g32 = (int*)S.g32.p;
+    d.stats = (unsigned long long*)S.stats.p;
+    d.joins = (nwg_join*)S.joins.p;
+    d.n0 = n;
+    d.ld = ldd;
+    d.cand_cap = kCandCap;
+    jsrc = S.joins.p;
+    ssrc = S.stats.p;
     std::vector<int> slot0(nn, -1), act0(n + 1, 0);
     for (int k = 0; k < n; ++k) slot0[k] = k, act0[k] = k;
     const int na0 = n;
-    const int g0[4] = {0x7F7FFFFF, 0, 0, 0};
+    const int g0[4] = {0, 0, 0, 0};
     if ((rc = cuda(cudaMemcpyAsync(S.slot.p, slot0.data(), sizeof(int) * nn, cudaMemcpyHostToDevice, s), "nj upload")) ||
         (rc = cuda(cudaMemcpyAsync(S.node.p, act0.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s), "nj upload")) ||
         (rc = cuda(cudaMemcpyAsync(S.act.p, act0.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s), "nj upload")) ||
@@ -1630,13 +1235,13 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
     g.bar = (unsigned*)S.gbar.p;
     g.abort = (int*)S.gbar.p + 2;
     g.act2 = (int*)S.act2.p;
-    g.grmin = (int*)S.rmin.p;
+    g.grmin = (int*)S.grmin.p;
     g.grec = (int2*)S.grec.p;
-    g.tv = (float*)S.vd.p;
+    g.tv = (float*)S.tv.p;
     g.part = (float*)S.part.p;
     g.jsum = (long long*)S.jsum.p;
     g.jexp = (int*)S.jexp.p;
-    g.cand = (GCand*)S.cand.p;
+    g.cand = (KCand*)S.cand.p;
     // NaN (all bits set) float row sums at the padding slots; rowsum_kernel
     // fills the live ones
     if ((rc = cuda(cudaMemsetAsync(S.gbar.p, 0, sizeof(int) * 4, s), "nj upload")) ||
@@ -1728,8 +1333,8 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
   }
   if (st) cudaEventRecord(ev1, s);
   unsigned long long dst[5] = {0, 0, 0, 0, 0};
-  if ((rc = cuda(cudaMemcpyAsync(joins, S.joins.p, sizeof(nwg_join) * (n - 1), cudaMemcpyDeviceToHost, s), "nj download")) ||
-      (rc = cuda(cudaMemcpyAsync(dst, S.stats.p, sizeof(dst), cudaMemcpyDeviceToHost, s), "nj download")) ||
+  if ((rc = cuda(cudaMemcpyAsync(joins, jsrc, sizeof(nwg_join) * (n - 1), cudaMemcpyDeviceToHost, s), "nj download")) ||
+      (rc = cuda(cudaMemcpyAsync(dst, ssrc, sizeof(dst), cudaMemcpyDeviceToHost, s), "nj download")) ||
       (rc = cuda(cudaStreamSynchronize(s), "nj sync")))
     return rc;
   if (dst[2]) return fail(NWG_ERR_CUDA, "neighbor joining candidate list empty or overflowing");
@@ -1759,38 +1364,71 @@ namespace nwg {
 
 // Workspace of one job of the per-CTA path, laid out from `base` (256-byte
 // aligned pieces); D is the job's matrix (modified in place).
-size_t nj_job_workspace(int n) {
+// Workspace of one job of the cluster form, laid out from `base` (256-byte
+// aligned pieces); fills *J when given.  The job's matrix is separate (n rows
+// of ld floats, ld a multiple of 4, modified in place).
+static size_t job_layout(int n, int ld, char* base, NJJob* J) {
   auto al = [](size_t x) { return (x + 255) / 256 * 256; };
   const size_t cap = std::min<size_t>(kCandCap, (size_t)n * (n - 1) / 2 + 1);
-  return al(sizeof(double) * n) + al(sizeof(float) * n) + al(sizeof(int) * (2 * n)) + al(sizeof(int) * n) +
-         al(sizeof(int) * (n + 1)) + al(sizeof(int) * 4) + al(sizeof(int) * 4) + al(sizeof(unsigned long long) * 5) +
-         al(sizeof(float) * n) + al(sizeof(Cand) * cap) + al(sizeof(Pick)) + al(sizeof(nwg_join) * (n > 1 ? n - 1 : 1));
+  constexpr int kC = 16;   // partials for the largest cluster
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    char* q = base ? base + off : nullptr;
+    off += al(bytes);
+    return q;
+  };
+  char* T = take(sizeof(double) * n);
+  char* Tf = take(sizeof(float) * ld);
+  char* slot = take(sizeof(int) * (2 * n));
+  char* node = take(sizeof(int) * n);
+  char* act = take(sizeof(int) * (n + 1));
+  char* act2 = take(sizeof(int) * (n + 1));
+  char* na = take(sizeof(int) * 4);
+  char* g32 = take(sizeof(int) * 4);
+  char* stats = take(sizeof(unsigned long long) * 5);
+  char* grmin = take(sizeof(int) * n);
+  char* grec = take(sizeof(int2) * n);
+  char* tv = take(sizeof(float) * n);
+  char* part = take(sizeof(float) * 2 * kC);
+  char* jsum = take(sizeof(long long) * 2 * kC);
+  char* jexp = take(sizeof(int) * 2 * kC);
+  char* cand = take(sizeof(KCand) * cap);
+  char* joins = take(sizeof(nwg_join) * (n > 1 ? n - 1 : 1));
+  if (J) {
+    J->s.T = (double*)T;
+    J->s.Tf = (float*)Tf;
+    J->s.slot = (int*)slot;
+    J->s.node = (int*)node;
+    J->s.act = (int*)act;
+    J->s.na = (int*)na;
+    J->s.g32 = (int*)g32;
+    J->s.stats = (unsigned long long*)stats;
+    J->s.joins = (nwg_join*)joins;
+    J->s.n0 = n;
+    J->s.ld = ld;
+    J->s.cand_cap = (int)cap;
+    J->g.act2 = (int*)act2;
+    J->g.grmin = (int*)grmin;
+    J->g.grec = (int2*)grec;
+    J->g.tv = (float*)tv;
+    J->g.part = (float*)part;
+    J->g.jsum = (long long*)jsum;
+    J->g.jexp = (int*)jexp;
+    J->g.cand = (KCand*)cand;
+    J->n = n;
+  }
+  return off;
 }
 
-// Fill the job descriptor for a job of n nodes with matrix D and workspace
-// at base; returns the addresses of its join records and statistics.
-void nj_job_setup(void* job_out, float* D, int n, char* base, nwg_join** joins, unsigned long long** stats) {
-  auto al = [](size_t x) { return (x + 255) / 256 * 256; };
-  const size_t cap = std::min<size_t>(kCandCap, (size_t)n * (n - 1) / 2 + 1);
+size_t nj_job_workspace(int n) { return job_layout(n, nj_row_stride(n), nullptr, nullptr); }
+
+// Fill the job descriptor for a job of n nodes with matrix D (row stride ld)
+// and workspace at base; returns the addresses of its join records and
+// statistics.
+void nj_job_setup(void* job_out, float* D, int n, int ld, char* base, nwg_join** joins, unsigned long long** stats) {
   NJJob J{};
-  char* p = base;
+  job_layout(n, ld, base, &J);
   J.s.D = D;
-  J.s.T = (double*)p; p += al(sizeof(double) * n);
-  J.s.Tf = (float*)p; p += al(sizeof(float) * n);
-  J.s.slot = (int*)p; p += al(sizeof(int) * (2 * n));
-  J.s.node = (int*)p; p += al(sizeof(int) * n);
-  J.s.act = (int*)p; p += al(sizeof(int) * (n + 1));
-  J.s.na = (int*)p; p += al(sizeof(int) * 4);
-  J.s.g32 = (int*)p; p += al(sizeof(int) * 4);
-  J.s.stats = (unsigned long long*)p; p += al(sizeof(unsigned long long) * 5);
-  J.s.vd = (float*)p; p += al(sizeof(float) * n);
-  J.s.cand = (Cand*)p; p += al(sizeof(Cand) * cap);
-  J.s.win = (Pick*)p; p += al(sizeof(Pick));
-  J.s.joins = (nwg_join*)p;
-  J.s.n0 = n;
-  J.s.ld = n;
-  J.s.cand_cap = (int)cap;
-  J.n = n;
   *joins = J.s.joins;
   *stats = J.s.stats;
   std::memcpy(job_out, &J, sizeof(J));
@@ -1798,52 +1436,39 @@ void nj_job_setup(void* job_out, float* D, int n, char* base, nwg_join** joins, 
 
 size_t nj_job_desc_bytes() { return sizeof(NJJob); }
 
-// One job per cluster of C CTAs (C = 1, 8 or 16); nmax: the largest n of the
-// jobs (dynamic shared memory of 5 arrays of nmax 4-byte words).
-cudaError_t launch_nj_cluster(const void* d_jobs, int njobs, int nmax, int C, cudaStream_t s) {
+// One job per cluster of C CTAs (C = 8 or 16).
+cudaError_t launch_nj_cluster(const void* d_jobs, int njobs, int C, cudaStream_t s) {
   if (njobs <= 0) return cudaSuccess;
-  const size_t smem = (size_t)5 * sizeof(float) * (size_t)std::max(nmax, 1);
   const NJJob* jobs = reinterpret_cast<const NJJob*>(d_jobs);
-  auto go = [&](auto kern, int c) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (C == 16) {
+    cudaError_t e = cudaFuncSetAttribute(nj_cluster_kernel<16>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return e;
-    if (c > 8 && (e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1)) != cudaSuccess)
-      return e;
-    kern<<<njobs * c, 1024, smem, s>>>(jobs, njobs, nmax);
-    return cudaGetLastError();
-  };
-  if (C == 16) return go(nj_cluster_kernel<16>, 16);
-  if (C == 8) return go(nj_cluster_kernel<8>, 8);
-  return go(nj_cluster_kernel<1>, 1);
+    nj_cluster_kernel<16><<<njobs * 16, 1024, 0, s>>>(jobs, njobs);
+  } else {
+    nj_cluster_kernel<8><<<njobs * 8, 1024, 0, s>>>(jobs, njobs);
+  }
+  return cudaGetLastError();
 }
 
-// The largest cluster (16, else 8) that the device schedules with the join
-// loop's shared memory for the largest supported n.
+// The largest cluster (16, else 8) that the device schedules for the join loop.
 int nj_cluster_size() {
   static int best = 0;
   if (best) return best;
-  const size_t smem = (size_t)5 * sizeof(float) * kNJMaxN;
   best = 8;
-  for (int c : {16, 8}) {
-    const void* fn = c == 16 ? (const void*)nj_cluster_kernel<16> : (const void*)nj_cluster_kernel<8>;
-    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) continue;
-    if (c > 8 && cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) continue;
+  const void* fn = (const void*)nj_cluster_kernel<16>;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
     cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3(c);
+    cfg.gridDim = dim3(16);
     cfg.blockDim = dim3(1024);
-    cfg.dynamicSmemBytes = smem;
     cudaLaunchAttribute at;
     at.id = cudaLaunchAttributeClusterDimension;
-    at.val.clusterDim.x = c;
+    at.val.clusterDim.x = 16;
     at.val.clusterDim.y = 1;
     at.val.clusterDim.z = 1;
     cfg.attrs = &at;
     cfg.numAttrs = 1;
     int clusters = 0;
-    if (cudaOccupancyMaxActiveClusters(&clusters, fn, &cfg) == cudaSuccess && clusters > 0) {
-      best = c;
-      break;
-    }
+    if (cudaOccupancyMaxActiveClusters(&clusters, fn, &cfg) == cudaSuccess && clusters > 0) best = 16;
   }
   cudaGetLastError();
   return best;

@@ -152,14 +152,17 @@ inline int wave_x_per_front(int V) { return V == 5 ? 2 : 1; }
 cudaError_t launch_plain(const PlainArgs& a, cudaStream_t s);
 cudaError_t launch_rerun(const WaveArgs& a, int2* scratch, int64_t nthreads, cudaStream_t s);
 // neighbor joining of many jobs in one launch, one thread-block cluster per job (nj.cu)
+// Row stride (floats) of a neighbor-joining matrix on the device: rows padded
+// to a multiple of 4 floats for 16-byte loads.
+inline int nj_row_stride(int n) { return (n + 3) & ~3; }
 size_t nj_job_workspace(int n);
-void nj_job_setup(void* job_out, float* D, int n, char* base, nwg_join** joins, unsigned long long** stats);
+void nj_job_setup(void* job_out, float* D, int n, int ld, char* base, nwg_join** joins, unsigned long long** stats);
 size_t nj_job_desc_bytes();
 // residue encoding + reversal on the device (ingest.cu): sequence s of src at
 // src_off[s] (len[s] bytes) -> dst at dst_off[s]; bad[s] = bytes outside the alphabet
 cudaError_t launch_encode(const char* d_src, const int64_t* d_src_off, const int64_t* d_dst_off, const int32_t* d_len,
                           int n, int8_t* d_dst, int* d_bad, cudaStream_t s);
-cudaError_t launch_nj_cluster(const void* d_jobs, int njobs, int nmax, int C, cudaStream_t s);
+cudaError_t launch_nj_cluster(const void* d_jobs, int njobs, int C, cudaStream_t s);
 int nj_cluster_size();
 constexpr int kServeMaxN = 8192;   // largest job of the serving loop (neighbor joining on the device)
 cudaError_t launch_dpx_peak(int P, int form, int cols, int grid, uint32_t* sink, int go, int ge, cudaStream_t s);

@@ -122,7 +122,7 @@ struct Server {
   int device = 0;
 
   size_t footprint(int n) const {
-    return sizeof(float) * (size_t)n * n + nj_job_workspace(n) + (size_t)n * 600 + 4096;
+    return sizeof(float) * (size_t)n * nj_row_stride(n) + nj_job_workspace(n) + (size_t)n * 600 + 4096;
   }
 
   int launch_batch(Slot& S);
@@ -146,8 +146,8 @@ int Server::launch_batch(Slot& S) {
     J->seq_base = (size_t)total_seqs;
     total_codes += (int64_t)J->ascii.size();
     total_seqs += J->n;
-    J->d_off = (size_t)total_D;
-    total_D += (int64_t)J->n * J->n;
+    J->d_off = (size_t)total_D;   // rows padded for the join loop's 16-byte loads
+    total_D += (int64_t)J->n * nj_row_stride(J->n);
     J->nj_off = (size_t)total_ws;
     total_ws += (int64_t)nj_job_workspace(J->n);
   }
@@ -159,6 +159,7 @@ int Server::launch_batch(Slot& S) {
   int64_t base = 0;
   for (ServeJob* J : S.batch) {
     const int n = J->n;
+    const int ldp = nj_row_stride(n);
     std::vector<int> ord(n);
     std::iota(ord.begin(), ord.end(), 0);
     std::stable_sort(ord.begin(), ord.end(),
@@ -180,11 +181,11 @@ int Server::launch_batch(Slot& S) {
       if (!long_set && len[gyi] <= certain) {
         const int y2 = y + 1 < n ? gyi + 1 : -1;
         const int last = y2 >= 0 ? y + 1 : y;
-        groups.push_back({gyi, y2, last + 1, (int)base, tc.R, tc.V, tc.W, 2, (int64_t)J->d_off, n});
+        groups.push_back({gyi, y2, last + 1, (int)base, tc.R, tc.V, tc.W, 2, (int64_t)J->d_off, ldp});
         y = last + 1;
       } else {
         const TuneChoice t32 = int32_choice(tc);
-        groups.push_back({gyi, -1, y + 1, (int)base, t32.R, t32.V, 32, 1, (int64_t)J->d_off, n});
+        groups.push_back({gyi, -1, y + 1, (int)base, t32.R, t32.V, 32, 1, (int64_t)J->d_off, ldp});
         ++y;
       }
     }
@@ -247,7 +248,8 @@ int Server::launch_batch(Slot& S) {
   for (int k = 0; k < nj; ++k) {
     ServeJob* J = S.batch[k];
     J->desc_idx = (size_t)k;
-    nj_job_setup(&descs[desc * k], (float*)S.D.p + J->d_off, J->n, (char*)S.njws.p + J->nj_off, &jptr[k], &sptr[k]);
+    nj_job_setup(&descs[desc * k], (float*)S.D.p + J->d_off, J->n, nj_row_stride(J->n), (char*)S.njws.p + J->nj_off,
+                 &jptr[k], &sptr[k]);
   }
   std::vector<int32_t> a_gy(ng), a_gy2(ng), a_gx(ng), a_gxb(ng), a_gld(ng);
   std::vector<int64_t> a_gdofs(ng);
@@ -333,7 +335,7 @@ int Server::launch_batch(Slot& S) {
   int nmax = 1;
   for (ServeJob* J : S.batch) nmax = std::max(nmax, J->n);
   const int csize = nmax >= kNJWideN ? nj_cluster_size() : kNJClusterServe;
-  if ((rc = c.cuda(launch_nj_cluster(S.njdesc.p, nj, nmax, csize, st), "serve nj launch"))) return rc;
+  if ((rc = c.cuda(launch_nj_cluster(S.njdesc.p, nj, csize, st), "serve nj launch"))) return rc;
   char* hj = (char*)S.h_joins.p;
   size_t jo = 0;
   for (int k = 0; k < nj; ++k) {
@@ -431,7 +433,10 @@ void Server::completer_loop(int si) {
     for (ServeJob* J : S.batch) {
       int nbad = 0;
       for (int k = 0; k < J->n; ++k) nbad += badseq[J->seq_base + k];
-      J->D.assign((const float*)S.h_D.p + J->d_off, (const float*)S.h_D.p + J->d_off + (size_t)J->n * J->n);
+      const int n = J->n, ldp = nj_row_stride(n);
+      J->D.resize((size_t)n * n);
+      const float* src = (const float*)S.h_D.p + J->d_off;
+      for (int r = 0; r < n; ++r) std::memcpy(J->D.data() + (size_t)r * n, src + (size_t)r * ldp, sizeof(float) * n);
       J->status = e != cudaSuccess ? NWG_ERR_CUDA
                   : nbad           ? NWG_ERR_BAD_RESIDUE
                   : J->njst[2]     ? NWG_ERR_CUDA
