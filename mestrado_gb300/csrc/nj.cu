@@ -32,21 +32,23 @@
 // Search per join:
 //  1. one streaming pass over the live triangle of D (4 B per live pair):
 //     q in float, fl(fl(fl(d*(n-2)) - Tf_r) - Tf_c) with Tf the float copy of
-//     T; per row its minimum, overall the minimum and the largest magnitude
-//     M = |d|(n-2) + |T_r| + |T_c|.  Every float q is within E = 8 * 2^-24 * M
-//     of the exact q.
-//  2. the rows whose minimum is at most min + 3E (usually one or two) are
-//     scanned again; every pair of them within that threshold gets its exact
-//     double q in both roundings; those candidates go to a list.
-// Warp 0 then takes the winner with the tie-break and runs the ambiguity
-// check on the list: any pair left out has q > winner + E, beyond reach of
-// either rounding.  All floating-point operations use the _rn intrinsics in
-// the reference's evaluation order (no contraction).
+//     T; per row its two smallest q (and the column of the smallest), overall
+//     the minimum and the largest magnitude M = |d|(n-2) + |T_r| + |T_c|.
+//     Every float q is within E = 8 * 2^-24 * M of the exact q.
+//  2. the candidates are the pairs whose float q is at most min + 3E: when
+//     each row within that threshold has one such pair (its second smallest q
+//     is beyond), they are those rows' minima; otherwise the rows are scanned
+//     again into a list.  Each candidate gets its exact double q in both
+//     roundings.
+// The winner follows the tie-break; the ambiguity check runs over the
+// candidates: any pair left out has q > winner + E, beyond reach of either
+// rounding.  All floating-point operations use the _rn intrinsics in the
+// reference's evaluation order (no contraction).
 //
-// Two launch forms: up to 2048 taxa (and for the serving loop, every job) one
-// thread-block cluster runs the whole loop; larger matrices take a full-GPU
-// kernel for pass 1 and one CTA for the rest of each join, and are compacted
-// to their live slots (in slot order) at every rebuild step.
+// A team of CTAs runs a job's join loop: the whole GPU (one cooperative
+// launch per rebuild segment, more than 2048 taxa; compacted to the live
+// slots, in slot order, between segments) or one thread-block cluster (up to
+// 2048 taxa, and every serving job, one cluster per job).
 #include <algorithm>
 #include <cfloat>
 #include <climits>
