@@ -300,6 +300,47 @@ def _peaks():
         return {"hbm_gbs": 6800.0}, "fallback"
 
 
+def config1_leg():
+    """Configuration 1: 2,000 sequences in 10 families of 200 (lengths about
+    300-600), all pairs, in the plain form (one thread per pair, int32, one
+    launch per pair-length group) and in the batched form, device-resident,
+    each timed once after a warm-up with CUDA events on the library's stream;
+    the two matrices must be equal."""
+    import torch
+
+    from mestrado_gb300 import MODE_BATCHED, MODE_PLAIN, Context, encode, synth
+    S = synth.config(1)
+    n = len(S)
+    cells = S.cells()
+    codes, off = encode(S)
+    ctx = Context(10, 2)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    ctx.autotune()
+    d_codes = torch.from_numpy(codes).to("cuda")
+    out = {}
+    mats = {}
+    for name, mode in (("plain", MODE_PLAIN), ("batched", MODE_BATCHED)):
+        d_D = torch.empty((n, n), dtype=torch.float32, device="cuda")
+        with torch.cuda.stream(stream):
+            ctx.score_all_dev(d_codes.data_ptr(), off, d_D.data_ptr(), n, mode)   # warm-up (plan, graph)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            ctx.score_all_dev(d_codes.data_ptr(), off, d_D.data_ptr(), n, mode)
+            b.record(stream)
+            torch.cuda.synchronize()
+        ms = a.elapsed_time(b)
+        out[name] = {"gcups": cells / (ms / 1e3) / 1e9, "ms": ms}
+        mats[name] = d_D.cpu().numpy()
+    ctx.close()
+    return {"workload": "configuration 1: 2000 seqs, 10 families x 200, root 450, p_s 0.08 (lengths about "
+                        "300-600), all pairs incl. diagonal; device-resident",
+            "pairs": n * (n + 1) // 2, "cells": cells, **out,
+            "batched_over_plain": out["batched"]["gcups"] / out["plain"]["gcups"],
+            "matrices_equal": bool(np.array_equal(mats["plain"], mats["batched"]))}
+
+
 def pipeline_leg(cpu_nj_n: int = 2000):
     """Configuration 3 end to end through the public API (host buffers): 8,000
     sequences -> distance matrix -> neighbor joining -> cherry traceback,
@@ -589,6 +630,7 @@ def main():
 
     if rank != 0:
         return
+    config1 = None if args.no_plain else config1_leg()
     serving = serving_leg(args.serve_seconds) if args.serve_seconds > 0 else None
     pipeline = None if args.no_pipeline else pipeline_leg()
     roof = None
@@ -629,6 +671,7 @@ def main():
         "pairs_int16": st["pairs_int16"], "pairs_int32": st["pairs_int32"],
         "wall_s": wall,
         "clocks": clk,
+        "config1": config1,
         "serving": serving,
         "pipeline": pipeline,
     }

@@ -231,7 +231,8 @@ struct GridNJ {
   int* abort;           // set when a barrier wait gave up; every CTA then leaves
   int* act2;            // the other active list (the join writes the shifted list there)
   int* grmin;           // per slot: smallest float q of the row's pairs (ordered int)
-  int2* grec;           // per slot: second smallest q (ordered int), column of the smallest
+  int4* grec;           // per slot: second smallest q (ordered int), column and distance of the smallest
+  double* tsnap;        // per slot: T as the pass saw it (the pick reads these, never T itself)
   float* tv;            // per slot: the new row's value
   float* part;          // [2 * grid]: per CTA smallest q and largest magnitude
   long long* jsum;      // [2 * grid]: per CTA integer sum and sum of magnitudes (units of 2^jexp)
@@ -347,7 +348,11 @@ __device__ void grid_pass(const NJDev& s, const GridNJ& g, Team tm, float nm2f, 
       if (n0 - 1 - p == p && h) break;
       const int r = (h != (int)rev) ? n0 - 1 - p : p;
       const float tr = s.Tf[r];
-      if (tr != tr) continue;   // dead slot
+      if (tr != tr) {   // dead slot
+        if (lane == 0) g.grmin[r] = 0x7F7FFFFF;
+        continue;
+      }
+      const double Tr = s.T[r];
       const float* row = s.D + (size_t)r * s.ld;
       float m1 = FLT_MAX, m2 = FLT_MAX, mag = 0.f;
       int c1 = -1;
@@ -384,8 +389,11 @@ __device__ void grid_pass(const NJDev& s, const GridNJ& g, Team tm, float nm2f, 
         mag = fmaxf(mag, __shfl_xor_sync(0xffffffffu, mag, o));
       }
       if (lane == 0) {
+        // the pick reads only what the pass wrote: a fast CTA's join share may
+        // already be changing T and D while a slow one still picks
         g.grmin[r] = ford(m1);
-        g.grec[r] = make_int2(ford(m2), c1);
+        g.grec[r] = make_int4(ford(m2), c1, __float_as_int(c1 >= 0 ? row[c1] : 0.f), 0);
+        g.tsnap[r] = Tr;
       }
       qmin = fminf(qmin, m1);
       mmax = fmaxf(mmax, __fadd_rn(mag, fabsf(tr)));
@@ -544,14 +552,14 @@ __device__ int grid_pick_direct(const NJDev& s, const GridNJ& g, Team tm, double
     int ok = nr >= 1 && nr <= kFastRows;
     if (ok && l < nr) {
       const int r = rows[l];
-      const int2 rec = g.grec[r];
+      const int4 rec = g.grec[r];
       const int c = rec.y;
       if (rec.x <= othr || c < 0) {
         ok = 0;   // a second pair of the row within the threshold
       } else {
         const int ur = s.node[r], uc = s.node[c];
-        const double Tr = s.T[r], Tc = s.T[c];
-        const float d = s.D[(size_t)r * s.ld + c];
+        const double Tr = g.tsnap[r], Tc = g.tsnap[c];
+        const float d = __int_as_float(rec.z);
         fc[l] = make_cand(r, c, ur, uc, Tr, Tc, d, nm2, watermark);
         if (ur < 0 || uc < 0) ok = 0;
       }
@@ -679,7 +687,6 @@ __device__ void grid_join_share(const NJDev& s, const GridNJ& g, Team tm, const 
   x.e = INT_MAX;
   x.t = INT_MIN;
   if ((int)threadIdx.x < per && p < n0) {
-    g.grmin[p] = 0x7F7FFFFF;   // the next join's row minima start at +inf
     const int v = s.node[p];
     const float Dik = s.D[(size_t)si * ld + p];
     const float Djk = s.D[(size_t)sj * ld + p];
@@ -1111,16 +1118,539 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_cluster_
   for (int k = t0; k < n - 1; k += tstride) join_lengths(s.joins[k]);
 }
 
+// ---- small jobs: the whole join loop in the cluster's shared memory --------
+// Up to kSmemNJMax taxa the matrix fits the distributed shared memory of one
+// cluster.  CTA q holds the rows of the folded slot pairs p = q, q + C, ...
+// (rows p and n-1-p; local row 2*(p/C) + (row != p)); every CTA keeps its own
+// copy of the float row sums, the slot -> node and id -> slot maps and the
+// active list, updated identically, and reads the other CTAs' row minima,
+// partials, row sums and rows through distributed shared memory.  The phases
+// and the arithmetic are those of the global forms (pass with the two
+// smallest q per row, direct pick or fallback scan, join share, apply, the
+// reference's rebuild schedule); only the join records and a fallback
+// candidate list use global memory.
+
+constexpr int kSmemNJMax = 768;
+
+struct SmemLayout {
+  int ldl;   // local row stride (floats, a multiple of 4)
+  int lr;    // local rows per CTA (two per local pair)
+  size_t rows, tf, tloc, tsn, node, slot, act_a, act_b, grm, grc, tvl, bytes;
+};
+
+__host__ __device__ inline SmemLayout smem_layout(int n, int C) {
+  auto al = [](size_t x) { return (x + 15) / 16 * 16; };
+  SmemLayout L;
+  L.ldl = (n + 3) & ~3;
+  const int npairs = (n + 1) / 2;
+  L.lr = 2 * ((npairs + C - 1) / C);
+  size_t o = 0;
+  L.rows = o; o += al(sizeof(float) * (size_t)L.lr * L.ldl);
+  L.tf = o; o += al(sizeof(float) * L.ldl);
+  L.tloc = o; o += al(sizeof(double) * L.lr);
+  L.tsn = o; o += al(sizeof(double) * L.lr);
+  L.node = o; o += al(sizeof(int) * n);
+  L.slot = o; o += al(sizeof(int) * 2 * n);
+  L.act_a = o; o += al(sizeof(int) * (n + 1));
+  L.act_b = o; o += al(sizeof(int) * (n + 1));
+  L.grm = o; o += al(sizeof(int) * L.lr);
+  L.grc = o; o += al(sizeof(int4) * L.lr);
+  L.tvl = o; o += al(sizeof(float) * L.lr);
+  L.bytes = o;
+  return L;
+}
+
+template <int C>
+struct SmemNJ {
+  int n, npairs, ldl, lr, rank;
+  float* rows;     // local rows, ldl floats each
+  float* Tf;       // float row sums of every slot (NaN dead / padding)
+  double* Tloc;    // T of the local rows
+  double* Tsn;     // T of the local rows as the pass saw it (the pick reads these)
+  int* node;       // slot -> node id
+  int* slot;       // node id -> slot
+  int* grm;        // local rows: smallest float q (ordered int)
+  int4* grc;       // local rows: second smallest q (ordered int), column and distance of the smallest
+  float* tvl;      // local rows: the new row's value in this join
+  // slot -> owner CTA and local row
+  __device__ __forceinline__ int owner(int r) const {
+    const int p = min(r, n - 1 - r);
+    return p % C;
+  }
+  __device__ __forceinline__ int local_row(int r) const {
+    const int p = min(r, n - 1 - r);
+    return 2 * (p / C) + (r != p ? 1 : 0);
+  }
+  // local row lr of CTA q -> slot, or -1
+  __device__ __forceinline__ int slot_of(int q, int l) const {
+    const int p = (l >> 1) * C + q;
+    if (p >= npairs) return -1;
+    if (l & 1) return n - 1 - p == p ? -1 : n - 1 - p;
+    return p;
+  }
+  template <class T>
+  __device__ __forceinline__ T* at(T* local, int q) const {
+    return cooperative_groups::this_cluster().map_shared_rank(local, q);
+  }
+};
+
+// Row sums of this CTA's live rows over the active list (the reference's
+// ascending-id order; any-order lanes when provably exact), with the float
+// copies written into every CTA's row-sum array.
+template <int C>
+__device__ void smem_rowsums(const SmemNJ<C>& m, const int* act, int na) {
+  const int lane = threadIdx.x & 31;
+  for (int l = (int)(threadIdx.x >> 5); l < m.lr; l += (int)(blockDim.x >> 5)) {
+    const int r = m.slot_of(m.rank, l);
+    if (r < 0 || m.node[r] < 0) continue;
+    const float* row = m.rows + (size_t)l * m.ldl;
+    double part = 0.0, ab = 0.0;
+    int lowexp = INT_MAX;
+    for (int j = lane; j < na; j += 32) {
+      const float x = row[m.slot[act[j]]];
+      part = __dadd_rn(part, (double)x);
+      ab = __dadd_rn(ab, (double)fabsf(x));
+      lowexp = min(lowexp, low_bit_exp(x));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      part = __dadd_rn(part, __shfl_down_sync(0xffffffffu, part, o));
+      ab = __dadd_rn(ab, __shfl_down_sync(0xffffffffu, ab, o));
+      lowexp = min(lowexp, __shfl_down_sync(0xffffffffu, lowexp, o));
+    }
+    double sum = __shfl_sync(0xffffffffu, part, 0);
+    if (lane == 0 && !sum_is_exact(ab, lowexp)) {
+      sum = 0.0;
+      for (int j = 0; j < na; ++j) sum = __dadd_rn(sum, (double)row[m.slot[act[j]]]);
+    }
+    sum = __shfl_sync(0xffffffffu, sum, 0);
+    if (lane == 0) m.Tloc[l] = sum;
+    const float tf = __double2float_rn(sum);
+    if (lane < C) m.at(m.Tf, lane)[r] = tf;
+  }
+}
+
+template <int C>
+__global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_kernel(const NJJob* jobs, int njobs) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ NJJob sjob;
+  __shared__ float spart[2];   // this CTA's pass partial (read by the other CTAs)
+  __shared__ USum susum;       // this CTA's share sum (read by the other CTAs)
+  __shared__ int rows_sel[kFastRows];
+  __shared__ GCand fc[kFastRows];
+  __shared__ int nsel, s_ok;
+  __shared__ PickOut spick;
+  __shared__ GCand swin;
+  __shared__ float sthr;
+  __shared__ double s_sum;
+  __shared__ int s_exact;
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  const int job = (int)blockIdx.x / C;   // the same for every CTA of the cluster
+  if (job >= njobs) return;
+  if (threadIdx.x == 0) sjob = jobs[job];
+  __syncthreads();
+  const NJDev& s = sjob.s;
+  const GridNJ& g = sjob.g;
+  const int n = sjob.n;
+  __shared__ SmemNJ<C> sm;   // the layout's pointers (shared memory keeps registers free)
+  const SmemLayout L = smem_layout(n, C);
+  if (threadIdx.x == 0) {
+    sm.n = n;
+    sm.npairs = (n + 1) / 2;
+    sm.ldl = L.ldl;
+    sm.lr = L.lr;
+    sm.rank = (int)cl.block_rank();
+    sm.rows = reinterpret_cast<float*>(smem + L.rows);
+    sm.Tf = reinterpret_cast<float*>(smem + L.tf);
+    sm.Tloc = reinterpret_cast<double*>(smem + L.tloc);
+    sm.node = reinterpret_cast<int*>(smem + L.node);
+    sm.slot = reinterpret_cast<int*>(smem + L.slot);
+    sm.grm = reinterpret_cast<int*>(smem + L.grm);
+    sm.grc = reinterpret_cast<int4*>(smem + L.grc);
+    sm.Tsn = reinterpret_cast<double*>(smem + L.tsn);
+    sm.tvl = reinterpret_cast<float*>(smem + L.tvl);
+  }
+  __syncthreads();
+  const SmemNJ<C>& m = sm;
+  int* act = reinterpret_cast<int*>(smem + L.act_a);
+  int* act2 = reinterpret_cast<int*>(smem + L.act_b);
+  const int rank = m.rank;
+  const int tid = (int)threadIdx.x, nth = (int)blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  // this CTA's rows from the matrix (padding columns 0); maps and lists
+  for (int l = 0; l < m.lr; ++l) {
+    const int r = m.slot_of(rank, l);
+    float* row = m.rows + (size_t)l * m.ldl;
+    for (int c = tid; c < m.ldl; c += nth) row[c] = (r >= 0 && c < n) ? s.D[(size_t)r * s.ld + c] : 0.f;
+  }
+  for (int k = tid; k < m.ldl; k += nth) m.Tf[k] = __int_as_float(0x7FC00000);
+  for (int k = tid; k < 2 * n; k += nth) m.slot[k] = k < n ? k : -1;
+  for (int k = tid; k < n; k += nth) {
+    m.node[k] = k;
+    act[k] = k;
+  }
+  for (int l = tid; l < m.lr; l += nth) m.grm[l] = 0x7F7FFFFF;
+  if (rank == 0 && tid == 0) {
+    s.g32[2] = 0;
+    s.stats[0] = s.stats[1] = s.stats[2] = s.stats[3] = s.stats[4] = 0;
+  }
+  cl.sync();   // every CTA's row-sum array is NaN before any broadcast lands
+  if (n >= 2) {
+    __syncthreads();
+    smem_rowsums(m, act, n);
+  }
+  cl.sync();
+  const int kBinT = 30 * 31 / 2;
+  int steps = max((int)((float)n * 0.5f), 200);
+  int pq_ck = 500;
+  long long ave0 = (((long long)(n - 1) * n) / 2) / kBinT;
+  long long ub = ((long long)n * (n - 1)) / 2;
+  int watermark = n;
+  bool failed = false;
+  for (int step = 0; step < n - 1 && !failed; ++step) {
+    const int m_n = n - step, next = n + step;
+    const float nm2f = (float)(m_n - 2);
+    const double nm2 = (double)(m_n - 2);
+    // ---- pass: each warp one local pair, 16-byte loads from shared memory
+    {
+      float qmin = FLT_MAX, mmax = 0.f;
+      const float4* Tf4 = reinterpret_cast<const float4*>(m.Tf);
+      const int nv = m.ldl >> 2;
+      for (int lp = warp; 2 * lp < m.lr; lp += nth >> 5) {
+        for (int h = 0; h < 2; ++h) {
+          const int l = 2 * lp + h;
+          const int r = m.slot_of(rank, l);
+          if (r < 0) continue;
+          const float tr = m.Tf[r];
+          if (tr != tr) {   // dead
+            if (lane == 0) m.grm[l] = 0x7F7FFFFF;
+            continue;
+          }
+          const float* row = m.rows + (size_t)l * m.ldl;
+          float m1 = FLT_MAX, m2 = FLT_MAX, mag = 0.f;
+          int c1 = -1;
+          const int c0 = r + 1, v0 = (c0 + 3) >> 2;
+          if (lane < 4 * v0 - c0 && c0 + lane < n) pass_elem(row[c0 + lane], m.Tf[c0 + lane], c0 + lane, tr, nm2f, m1, m2, c1, mag);
+          const float4* row4 = reinterpret_cast<const float4*>(row);
+          for (int v = v0 + lane; v < nv; v += 32) {
+            const float4 d = row4[v];
+            const float4 tc = Tf4[v];
+            pass_elem(d.x, tc.x, 4 * v, tr, nm2f, m1, m2, c1, mag);
+            pass_elem(d.y, tc.y, 4 * v + 1, tr, nm2f, m1, m2, c1, mag);
+            pass_elem(d.z, tc.z, 4 * v + 2, tr, nm2f, m1, m2, c1, mag);
+            pass_elem(d.w, tc.w, 4 * v + 3, tr, nm2f, m1, m2, c1, mag);
+          }
+          for (int o = 16; o > 0; o >>= 1) {
+            const float om1 = __shfl_xor_sync(0xffffffffu, m1, o);
+            const float om2 = __shfl_xor_sync(0xffffffffu, m2, o);
+            const int oc1 = __shfl_xor_sync(0xffffffffu, c1, o);
+            const bool take = om1 < m1 || (om1 == m1 && oc1 < c1);
+            const float lo = take ? om1 : m1, hi = take ? m1 : om1;
+            m2 = fminf(hi, fminf(m2, om2));
+            m1 = lo;
+            c1 = take ? oc1 : c1;
+            mag = fmaxf(mag, __shfl_xor_sync(0xffffffffu, mag, o));
+          }
+          if (lane == 0) {
+            // the pick reads only what the pass wrote (a fast CTA's join share
+            // may already be changing rows and row sums)
+            m.grm[l] = ford(m1);
+            m.grc[l] = make_int4(ford(m2), c1, __float_as_int(c1 >= 0 ? row[c1] : 0.f), 0);
+            m.Tsn[l] = m.Tloc[l];
+          }
+          qmin = fminf(qmin, m1);
+          mmax = fmaxf(mmax, __fadd_rn(mag, fabsf(tr)));
+        }
+      }
+      __shared__ float wq[32], wm[32];
+      if (lane == 0) {
+        wq[warp] = qmin;
+        wm[warp] = mmax;
+      }
+      __syncthreads();
+      if (warp == 0) {
+        qmin = lane < (nth >> 5) ? wq[lane] : FLT_MAX;
+        mmax = lane < (nth >> 5) ? wm[lane] : 0.f;
+        for (int o = 16; o > 0; o >>= 1) {
+          qmin = fminf(qmin, __shfl_xor_sync(0xffffffffu, qmin, o));
+          mmax = fmaxf(mmax, __shfl_xor_sync(0xffffffffu, mmax, o));
+        }
+        if (lane == 0) {
+          spart[0] = qmin;
+          spart[1] = mmax;
+        }
+      }
+    }
+    cl.sync();
+    // ---- pick: threshold from the CTA partials, rows within it, candidates
+    if (warp == 0) {
+      float q = FLT_MAX, mm = 0.f;
+      if (lane < C) {
+        const float* pp = m.at(spart, lane);
+        q = pp[0];
+        mm = pp[1];
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        q = fminf(q, __shfl_xor_sync(0xffffffffu, q, o));
+        mm = fmaxf(mm, __shfl_xor_sync(0xffffffffu, mm, o));
+      }
+      if (lane == 0) {
+        sthr = q + 3.f * (8.f * 5.9604645e-8f * mm) + 1e-30f;
+        nsel = 0;
+      }
+    }
+    __syncthreads();
+    const float thr = sthr;
+    const int othr = ford(thr);
+    for (int t = tid; t < C * m.lr; t += nth) {
+      const int q = t / m.lr, l = t - q * m.lr;
+      const int r = m.slot_of(q, l);
+      if (r >= 0 && m.at(m.grm, q)[l] <= othr) {
+        const int k = atomicAdd(&nsel, 1);
+        if (k < kFastRows) rows_sel[k] = r;
+      }
+    }
+    __syncthreads();
+    const int nr = nsel;
+    if (warp == 0) {
+      int ok = nr >= 1 && nr <= kFastRows;
+      if (ok && lane < nr) {
+        const int r = rows_sel[lane];
+        const int q = m.owner(r), l = m.local_row(r);
+        const int4 rec = m.at(m.grc, q)[l];
+        const int c = rec.y;
+        if (rec.x <= othr || c < 0) {
+          ok = 0;   // a second pair of the row within the threshold
+        } else {
+          const int qc = m.owner(c), lc = m.local_row(c);
+          const double Tr = m.at(m.Tsn, q)[l], Tc = m.at(m.Tsn, qc)[lc];
+          const float d = __int_as_float(rec.z);
+          const int ur = m.node[r], uc = m.node[c];
+          fc[lane] = make_cand(r, c, ur, uc, Tr, Tc, d, nm2, watermark);
+          if (ur < 0 || uc < 0) ok = 0;
+        }
+      }
+      ok = __all_sync(0xffffffffu, ok);
+      PickOut pr{};
+      if (ok && nr == 1) {
+        pr.idx = 0;
+        pr.ties = 1;
+        pr.amb = 0;
+        pr.error = false;
+      } else if (ok) {
+        pr = pick_keys(nr, [&](int k) { return fc[k]; });
+      }
+      if (lane == 0) {
+        s_ok = ok;
+        if (ok) {
+          spick = pr;
+          swin = fc[pr.idx];
+        }
+      }
+    }
+    __syncthreads();
+    if (!s_ok) {
+      // fallback: each CTA scans its own rows within the threshold into the list
+      for (int l = 0; l < m.lr; ++l) {
+        const int r = m.slot_of(rank, l);
+        if (r < 0 || m.grm[l] > othr) continue;
+        const int ur = m.node[r];
+        const float tr = m.Tf[r];
+        const double Tr = m.Tloc[l];
+        const float* row = m.rows + (size_t)l * m.ldl;
+        for (int c = r + 1 + tid; c < n; c += nth) {
+          const int uc = m.node[c];
+          if (uc < 0) continue;
+          const float d = row[c];
+          const float q = __fsub_rn(__fsub_rn(__fmul_rn(d, nm2f), tr), m.Tf[c]);
+          if (q > thr) continue;
+          const double Tc = m.at(m.Tloc, m.owner(c))[m.local_row(c)];
+          const int idx = atomicAdd(&s.g32[2], 1);
+          if (idx < s.cand_cap) {
+            const GCand cd = make_cand(r, c, ur, uc, Tr, Tc, d, nm2, watermark);
+            g.cand[idx] = KCand{cd.k1, cd.k2, cd.a, cd.b};
+          }
+        }
+      }
+      cl.sync();
+      if (warp == 0) {
+        const int ncount = *(volatile int*)&s.g32[2];
+        const int nc = min(ncount, s.cand_cap);
+        PickOut pr = pick_keys(nc, [&](int k) { return g.cand[k]; });
+        pr.error = pr.error || ncount > s.cand_cap;
+        if (lane == 0) {
+          spick = pr;
+          if (!pr.error) {
+            const KCand w = g.cand[pr.idx];
+            const int sa = m.slot[w.a], sb = m.slot[w.b];
+            const int r0 = min(sa, sb), c0 = max(sa, sb);
+            const int q = m.owner(r0), l = m.local_row(r0);
+            const double Tr = m.at(m.Tloc, q)[l], Tc = m.at(m.Tloc, m.owner(c0))[m.local_row(c0)];
+            const float d = m.at(m.rows, q)[(size_t)l * m.ldl + c0];
+            swin = make_cand(r0, c0, m.node[r0], m.node[c0], Tr, Tc, d, nm2, watermark);
+          }
+        }
+      }
+      __syncthreads();
+      if (spick.error) {   // the same in every CTA
+        if (rank == 0 && tid == 0) record_pick(s, spick);
+        failed = true;
+        break;
+      }
+    }
+    // ---- join share: this CTA's rows
+    const GCand w = swin;
+    const int i = w.a, j = w.b, si = w.sa, sj = w.sb;
+    {
+      USum x;
+      x.u = x.a = 0;
+      x.e = INT_MAX;
+      x.t = INT_MIN;
+      if (tid < m.lr) {
+        const int l = tid;
+        const int r = m.slot_of(rank, l);
+        if (r >= 0 && m.node[r] >= 0 && r != si && r != sj) {
+          float* row = m.rows + (size_t)l * m.ldl;
+          const float Dik = row[si], Djk = row[sj];
+          const float sumf = __fadd_rn(Dik, Djk);
+          const float tmp = __fmul_rn(__fsub_rn(sumf, w.d), 0.5f);
+          const double t = __dadd_rn(m.Tloc[l], (double)__fsub_rn(tmp, sumf));
+          m.Tloc[l] = t;
+          const float tf = __double2float_rn(t);
+          row[si] = tmp;
+          m.at(m.rows, m.owner(si))[(size_t)m.local_row(si) * m.ldl + r] = tmp;   // the new row
+#pragma unroll
+          for (int q = 0; q < C; ++q) m.at(m.Tf, q)[r] = tf;
+          m.tvl[l] = tmp;
+          if (tmp != 0.f) {
+            x.e = low_bit_exp(tmp);
+            x.t = top_bit_exp(tmp);
+            x.u = float_units(tmp, x.e);
+            x.a = x.u < 0 ? -x.u : x.u;
+          }
+        }
+      }
+      const int nwv = (m.lr + 31) >> 5;
+      if (warp < nwv) usum_warp(x);
+      __shared__ USum swp[32];
+      if (lane == 0 && warp < nwv) swp[warp] = x;
+      __syncthreads();   // also: every read of this join's maps is done
+      if (tid == 0) {
+        for (int w2 = 1; w2 < nwv; ++w2) usum_add(x, swp[w2]);
+        susum = x;
+      }
+      // the maps and the active list, identically in every CTA
+      for (int k = tid; k < m_n; k += nth) {
+        const int v = act[k];
+        if (v != i && v != j) act2[k - (v > i) - (v > j)] = v;
+      }
+      if (tid == 0) {
+        act2[m_n - 2] = next;
+        m.node[sj] = -1;
+        m.node[si] = next;
+        m.slot[j] = -1;
+        m.slot[i] = -1;
+        m.slot[next] = si;
+        m.Tf[sj] = __int_as_float(0x7FC00000);
+      }
+    }
+    cl.sync();
+    // ---- apply: the new node's row sum from the CTA sums
+    if (warp == 0) {
+      USum x;
+      x.u = x.a = 0;
+      x.e = INT_MAX;
+      x.t = INT_MIN;
+      if (lane < C) x = *m.at(&susum, lane);
+      usum_warp(x);
+      if (lane == 0) {
+        if (x.e == INT_MAX) {
+          s_sum = 0.0;
+          s_exact = 1;
+        } else if (x.t - x.e < 48 && x.a < (1ll << 53)) {
+          s_sum = units_to_double(x.u, x.e);
+          s_exact = 1;
+        } else {
+          s_exact = 0;
+        }
+      }
+    }
+    __syncthreads();
+    if (s_exact) {
+      if (tid == 0) {
+        m.Tf[si] = __double2float_rn(s_sum);
+        if (m.owner(si) == rank) m.Tloc[m.local_row(si)] = s_sum;
+      }
+    } else {
+      if (rank == 0 && tid == 0) {
+        double sum = 0.0;   // the reference's loop: active ids ascending, i and j skipped
+        for (int k = 0; k < m_n; ++k) {
+          const int v = act[k];
+          if (v == i || v == j) continue;
+          const int sv = v == next ? si : m.slot[v];
+          sum = __dadd_rn(sum, (double)m.at(m.tvl, m.owner(sv))[m.local_row(sv)]);
+        }
+        const float tf = __double2float_rn(sum);
+        for (int q = 0; q < C; ++q) m.at(m.Tf, q)[si] = tf;
+        m.at(m.Tloc, m.owner(si))[m.local_row(si)] = sum;
+      }
+      cl.sync();
+    }
+    if (rank == 0 && tid == 0) {
+      nwg_join& J = s.joins[step];
+      J.i = i;
+      J.j = j;
+      J.node = next;
+      J.n = m_n;
+      J.d = w.d;
+      J.pad = 0.f;
+      J.q = w.q1;
+      J.ti = w.ta;
+      J.tj = w.tb;
+      s.g32[2] = 0;
+      record_pick(s, spick);
+    }
+    {
+      int* t = act;
+      act = act2;
+      act2 = t;
+    }
+    // ---- the reference's rebuild schedule (SpeciesBlock.cpp:864, :1206-1247)
+    if (--pq_ck == 0) {
+      pq_ck = 500;
+      if (steps > 0 && (double)(ub / kBinT) / (double)ave0 > 2.0 && rank == 0 && tid == 0) s.stats[3] += 1;
+    }
+    const int m_after = m_n - 1;
+    if (steps == 0) {
+      cl.sync();   // every CTA's own write of the new row sum lands before the broadcasts
+      smem_rowsums(m, act, m_after);
+      if (rank == 0 && tid == 0) s.stats[4] += 1;
+      watermark = next + 1;
+      steps = (m_after < 200) ? INT_MAX : (int)((float)m_after * 0.5f);
+      ave0 = (((long long)(m_after - 1) * m_after) / 2) / kBinT;
+      ub = ((long long)m_after * (m_after - 1)) / 2;
+      cl.sync();
+    } else {
+      --steps;
+      ub += m_after - 1;
+      __syncthreads();
+    }
+  }
+  cl.sync();   // every join record is written; no CTA reads another's shared memory after this
+  if (!failed)
+    for (int k = rank * nth + tid; k < n - 1; k += C * nth) join_lengths(s.joins[k]);
+}
+
 }  // namespace
 
 struct NJState {
   DevBuf D, jobws, desc;
   // large-n path: row sums, maps, compaction buffers, candidates, grid partials and barrier words
-  DevBuf T, Tf, slot, node, act, na, g32, stats, joins, cand, tv, grmin, grec;
+  DevBuf T, Tf, slot, node, act, na, g32, stats, joins, cand, tv, grmin, grec, tsnap;
   DevBuf D2, T2, Tf2, node2, map, act2, part, jsum, jexp, gbar;
   ~NJState() {
     for (DevBuf* b : {&D, &jobws, &desc, &T, &Tf, &slot, &node, &act, &na, &g32, &stats, &joins, &cand, &tv, &grmin,
-                      &grec, &D2, &T2, &Tf2, &node2, &map, &act2, &part, &jsum, &jexp, &gbar})
+                      &grec, &tsnap, &D2, &T2, &Tf2, &node2, &map, &act2, &part, &jsum, &jexp, &gbar})
       b->release();
   }
 };
@@ -1177,7 +1707,10 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
     // the descriptor travels in the stream (a pageable copy is staged at once)
     if ((rc = cuda(cudaMemcpyAsync(S.desc.p, &J, sizeof(J), cudaMemcpyHostToDevice, s), "nj upload"))) return rc;
     if (st) cudaEventRecord(ev0, s);
-    if ((rc = cuda(launch_nj_cluster(S.desc.p, 1, nj_cluster_size(), s), "nj launch"))) return rc;
+    const int csm = smem_nj_cluster(n);
+    if ((rc = cuda(csm ? launch_nj_smem(S.desc.p, 1, n, csm, s) : launch_nj_cluster(S.desc.p, 1, nj_cluster_size(), s),
+                   "nj launch")))
+      return rc;
     ++launches;
   } else {
     // one CTA of 1024 threads per SM (cooperative launch); every join share
@@ -1189,7 +1722,7 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
         (rc = S.g32.ensure(sizeof(int) * 4)) || (rc = S.stats.ensure(sizeof(unsigned long long) * 5)) ||
         (rc = S.joins.ensure(sizeof(nwg_join) * (n - 1))) || (rc = S.cand.ensure(sizeof(KCand) * kCandCap)) ||
         (rc = S.tv.ensure(sizeof(float) * n)) || (rc = S.grmin.ensure(sizeof(int) * n)) ||
-        (rc = S.grec.ensure(sizeof(int2) * n)) || (rc = S.D2.ensure(sizeof(float) * (size_t)n * ldd)) ||
+        (rc = S.grec.ensure(sizeof(int4) * n)) || (rc = S.tsnap.ensure(sizeof(double) * n)) || (rc = S.D2.ensure(sizeof(float) * (size_t)n * ldd)) ||
         (rc = S.T2.ensure(sizeof(double) * n)) || (rc = S.Tf2.ensure(sizeof(float) * ldd)) ||
         (rc = S.node2.ensure(sizeof(int) * n)) || (rc = S.map.ensure(sizeof(int) * n)) ||
         (rc = S.act2.ensure(sizeof(int) * (n + 1))) || (rc = S.part.ensure(sizeof(float) * 2 * grid)) ||
@@ -1238,7 +1771,8 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
     g.abort = (int*)S.gbar.p + 2;
     g.act2 = (int*)S.act2.p;
     g.grmin = (int*)S.grmin.p;
-    g.grec = (int2*)S.grec.p;
+    g.grec = (int4*)S.grec.p;
+    g.tsnap = (double*)S.tsnap.p;
     g.tv = (float*)S.tv.p;
     g.part = (float*)S.part.p;
     g.jsum = (long long*)S.jsum.p;
@@ -1389,7 +1923,8 @@ static size_t job_layout(int n, int ld, char* base, NJJob* J) {
   char* g32 = take(sizeof(int) * 4);
   char* stats = take(sizeof(unsigned long long) * 5);
   char* grmin = take(sizeof(int) * n);
-  char* grec = take(sizeof(int2) * n);
+  char* grec = take(sizeof(int4) * n);
+  char* tsnap = take(sizeof(double) * n);
   char* tv = take(sizeof(float) * n);
   char* part = take(sizeof(float) * 2 * kC);
   char* jsum = take(sizeof(long long) * 2 * kC);
@@ -1411,7 +1946,8 @@ static size_t job_layout(int n, int ld, char* base, NJJob* J) {
     J->s.cand_cap = (int)cap;
     J->g.act2 = (int*)act2;
     J->g.grmin = (int*)grmin;
-    J->g.grec = (int2*)grec;
+    J->g.grec = (int4*)grec;
+    J->g.tsnap = (double*)tsnap;
     J->g.tv = (float*)tv;
     J->g.part = (float*)part;
     J->g.jsum = (long long*)jsum;
@@ -1448,6 +1984,45 @@ cudaError_t launch_nj_cluster(const void* d_jobs, int njobs, int C, cudaStream_t
     nj_cluster_kernel<16><<<njobs * 16, 1024, 0, s>>>(jobs, njobs);
   } else {
     nj_cluster_kernel<8><<<njobs * 8, 1024, 0, s>>>(jobs, njobs);
+  }
+  return cudaGetLastError();
+}
+
+// Jobs of at most this many taxa run the join loop in the cluster's shared
+// memory (nj_smem_kernel); NWG_NJ_SMEM_MAX_N overrides it (0: never).
+int smem_nj_max_n() {
+  static const int v = [] {
+    const char* e = std::getenv("NWG_NJ_SMEM_MAX_N");
+    return e ? std::min(std::atoi(e), kSmemNJMax) : kSmemNJMax;
+  }();
+  return v;
+}
+
+// The shared-memory form's cluster size for a launch whose largest job has
+// nmax taxa (0 when it does not fit either size).
+int smem_nj_cluster(int nmax) {
+  const size_t cap = 200 * 1024;   // dynamic shared memory per CTA
+  if (nmax > smem_nj_max_n()) return 0;
+  const bool fit8 = smem_layout(nmax, 8).bytes <= cap;
+  const bool fit16 = nj_cluster_size() == 16 && smem_layout(nmax, 16).bytes <= cap;
+  if (nmax < 256 && fit8) return 8;
+  if (fit16) return 16;
+  return fit8 ? 8 : 0;
+}
+
+cudaError_t launch_nj_smem(const void* d_jobs, int njobs, int nmax, int C, cudaStream_t s) {
+  if (njobs <= 0) return cudaSuccess;
+  const NJJob* jobs = reinterpret_cast<const NJJob*>(d_jobs);
+  const int bytes = (int)smem_layout(std::max(nmax, 2), C).bytes;
+  cudaError_t e;
+  if (C == 16) {
+    if ((e = cudaFuncSetAttribute(nj_smem_kernel<16>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1)) ||
+        (e = cudaFuncSetAttribute(nj_smem_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+      return e;
+    nj_smem_kernel<16><<<njobs * 16, 1024, bytes, s>>>(jobs, njobs);
+  } else {
+    if ((e = cudaFuncSetAttribute(nj_smem_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes))) return e;
+    nj_smem_kernel<8><<<njobs * 8, 1024, bytes, s>>>(jobs, njobs);
   }
   return cudaGetLastError();
 }

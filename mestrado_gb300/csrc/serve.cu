@@ -6,19 +6,20 @@
 // give for that job alone.  Jobs are submitted at any time.  A worker thread
 // forms batches from the pending queue: a job is admitted when its HBM
 // footprint (n^2 matrix, NJ workspace, codes) fits the budget left by the jobs
-// in flight.  A batch is queued on one of two pipeline slots (own stream,
+// in flight.  A batch is queued on one of four pipeline slots (own stream,
 // device arenas, pinned staging):
 //   residues in (ASCII; encoded and reversed on the device) -> one
-//   multi-job plan: every job's Y groups in shared
-//   length buckets, so one persistent launch per bucket interleaves pairs of
-//   different jobs -> matrices out -> one launch of the per-CTA join loop
-//   (one CTA per job) -> join lists out.
+//   multi-job plan: every job's Y groups in shared length buckets, so one
+//   persistent launch per bucket interleaves pairs of different jobs ->
+//   matrices out -> the join loops, one thread-block cluster per job (jobs
+//   that fit, with the matrix in the cluster's shared memory) -> join lists
+//   out.
 // While one slot's batch is on the device the next batch is formed and queued
-// on another free slot (four slots), so arrivals overlap the work in flight.
-// Each slot has its own completion thread that waits for that slot's event,
-// hands results to their jobs and frees their footprint, so a short batch
-// is returned without waiting for a longer one launched before it.  Nothing waits on the device except those host-side event
-// waits.
+// on another free slot, so arrivals overlap the work in flight.  Each slot has
+// its own completion thread that waits for that slot's event, hands results
+// to their jobs and frees their footprint, so a short batch is returned
+// without waiting for a longer one launched before it.  Nothing waits on the
+// device except those host-side event waits.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -40,6 +41,7 @@ namespace {
 // over 8 SMs (jobs of one batch run side by side).
 constexpr int kNJClusterServe = 8;
 constexpr int kNJWideN = 256;   // from this job size on, the widest cluster
+constexpr int kNJSmemServeMax = 768;   // jobs up to this size: join loop in shared memory
 
 double clock_ms() {
   using clk = std::chrono::steady_clock;
@@ -242,14 +244,25 @@ int Server::launch_batch(Slot& S) {
       (rc = S.njws.ensure((size_t)total_ws)) || (rc = S.njdesc.ensure(desc * nj)))
     return rc;
   // pinned staging: codes, then the plan arrays, then NJ descriptors
+  // NJ descriptors: jobs whose join loop runs in a cluster's shared memory
+  // first (one launch), the others after them (one launch)
+  int nmax_small = 0;
+  for (ServeJob* J : S.batch)
+    if (J->n <= kNJSmemServeMax) nmax_small = std::max(nmax_small, J->n);
+  const int csm = nmax_small > 0 ? smem_nj_cluster(nmax_small) : 0;
   std::vector<char> descs(desc * nj);
   std::vector<nwg_join*> jptr(nj);
   std::vector<unsigned long long*> sptr(nj);
-  for (int k = 0; k < nj; ++k) {
+  int n_small = 0, nmax_big = 1;
+  for (ServeJob* J : S.batch)
+    if (csm && J->n <= nmax_small) ++n_small;
+  for (int k = 0, a = 0, b = n_small; k < nj; ++k) {
     ServeJob* J = S.batch[k];
-    J->desc_idx = (size_t)k;
-    nj_job_setup(&descs[desc * k], (float*)S.D.p + J->d_off, J->n, nj_row_stride(J->n), (char*)S.njws.p + J->nj_off,
-                 &jptr[k], &sptr[k]);
+    const bool small = csm && J->n <= nmax_small;
+    J->desc_idx = (size_t)(small ? a++ : b++);
+    if (!small) nmax_big = std::max(nmax_big, J->n);
+    nj_job_setup(&descs[desc * J->desc_idx], (float*)S.D.p + J->d_off, J->n, nj_row_stride(J->n),
+                 (char*)S.njws.p + J->nj_off, &jptr[k], &sptr[k]);
   }
   std::vector<int32_t> a_gy(ng), a_gy2(ng), a_gx(ng), a_gxb(ng), a_gld(ng);
   std::vector<int64_t> a_gdofs(ng);
@@ -330,12 +343,16 @@ int Server::launch_batch(Slot& S) {
   }
   if ((rc = c.cuda(cudaMemcpyAsync(S.h_D.p, S.D.p, sizeof(float) * total_D, cudaMemcpyDeviceToHost, st), "serve")))
     return rc;
-  // join loops: one cluster per job, all jobs in one launch; batches with a
-  // large job take the device's largest cluster (the passes split wider)
-  int nmax = 1;
-  for (ServeJob* J : S.batch) nmax = std::max(nmax, J->n);
-  const int csize = nmax >= kNJWideN ? nj_cluster_size() : kNJClusterServe;
-  if ((rc = c.cuda(launch_nj_cluster(S.njdesc.p, nj, csize, st), "serve nj launch"))) return rc;
+  // join loops: one cluster per job; the small jobs in one launch with the
+  // matrix in the cluster's shared memory, the others in one launch over L2
+  // (jobs with 256 sequences or more take the device's largest cluster)
+  if (n_small && (rc = c.cuda(launch_nj_smem(S.njdesc.p, n_small, nmax_small, csm, st), "serve nj launch"))) return rc;
+  if (nj > n_small) {
+    const int csize = nmax_big >= kNJWideN ? nj_cluster_size() : kNJClusterServe;
+    if ((rc = c.cuda(launch_nj_cluster((const char*)S.njdesc.p + desc * n_small, nj - n_small, csize, st),
+                     "serve nj launch")))
+      return rc;
+  }
   char* hj = (char*)S.h_joins.p;
   size_t jo = 0;
   for (int k = 0; k < nj; ++k) {

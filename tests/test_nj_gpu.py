@@ -103,25 +103,33 @@ print('ok')
 """
 
 
-@pytest.mark.parametrize("path", ["cluster", "full_gpu"])
-def test_both_nj_paths_match_oracle(path):
-    # the large-matrix path (one cooperative full-GPU launch per segment,
-    # compaction at the rebuild steps) and the one-cluster path give the
-    # oracle's joins on families, tiny n, duplicates and tie-heavy integer
-    # matrices; run in a child process so that the path threshold applies
-    # from the library's first use
+# the three launch forms, selected by the size thresholds
+_FORMS = {
+    "smem": {},                                                        # matrix in the cluster's shared memory
+    "cluster": {"NWG_NJ_SMEM_MAX_N": "0", "NWG_NJ_CLUSTER_MAX_N": "100000"},   # one cluster over L2
+    "full_gpu": {"NWG_NJ_CLUSTER_MAX_N": "0"},                          # cooperative launch over every SM
+}
+
+
+@pytest.mark.parametrize("path", list(_FORMS))
+def test_every_nj_form_matches_oracle(path):
+    # every launch form gives the oracle's joins on families, tiny n,
+    # duplicates and tie-heavy integer matrices; run in a child process so
+    # that the thresholds apply from the library's first use
     import subprocess
     import sys
-    env = dict(os.environ, NWG_NJ_CLUSTER_MAX_N="0" if path == "full_gpu" else "100000")
+    env = dict(os.environ, **_FORMS[path])
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     r = subprocess.run([sys.executable, "-c", _BOTH_PATHS], cwd=root, env=env, capture_output=True, text=True,
                        timeout=900)
     assert r.returncode == 0 and r.stdout.strip().endswith("ok"), r.stdout + r.stderr
 
 
+@pytest.mark.parametrize("path", ["cluster", "full_gpu"])
 @pytest.mark.parametrize("case", ["cfg0", "nj300", "nj1200"])
-def test_full_gpu_path_matches_reference_tree(case):
-    # the golden reference trees through the large-matrix path
+def test_every_nj_form_matches_reference_tree(case, path):
+    # the golden reference trees through the forms the default sizes do not
+    # pick (the default run covers the shared-memory form up to 768 taxa)
     import subprocess
     import sys
     code = (
@@ -140,7 +148,7 @@ def test_full_gpu_path_matches_reference_tree(case):
         "(b['node'], b['i'], b['j'], b['len_i'], b['len_j'])\n"
         "assert newick(j, names) == open(os.path.join(d, 'tree.nwk')).read()\n"
         "print('ok')\n")
-    env = dict(os.environ, NWG_NJ_CLUSTER_MAX_N="0")
+    env = dict(os.environ, **_FORMS[path])
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     r = subprocess.run([sys.executable, "-c", code], cwd=root, env=env, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0 and r.stdout.strip().endswith("ok"), r.stdout + r.stderr
