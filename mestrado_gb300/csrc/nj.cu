@@ -1135,7 +1135,7 @@ constexpr int kSmemNJMax = 768;
 struct SmemLayout {
   int ldl;   // local row stride (floats, a multiple of 4)
   int lr;    // local rows per CTA (two per local pair)
-  size_t rows, tf, tloc, tsn, node, slot, act_a, act_b, grm, grc, tvl, bytes;
+  size_t rows, tf, tloc, tsn, node, slot, act_a, act_b, grm, grc, tvl, bytes;   // grm: every slot
 };
 
 __host__ __device__ inline SmemLayout smem_layout(int n, int C) {
@@ -1153,7 +1153,7 @@ __host__ __device__ inline SmemLayout smem_layout(int n, int C) {
   L.slot = o; o += al(sizeof(int) * 2 * n);
   L.act_a = o; o += al(sizeof(int) * (n + 1));
   L.act_b = o; o += al(sizeof(int) * (n + 1));
-  L.grm = o; o += al(sizeof(int) * L.lr);
+  L.grm = o; o += al(sizeof(int) * n);
   L.grc = o; o += al(sizeof(int4) * L.lr);
   L.tvl = o; o += al(sizeof(float) * L.lr);
   L.bytes = o;
@@ -1169,7 +1169,7 @@ struct SmemNJ {
   double* Tsn;     // T of the local rows as the pass saw it (the pick reads these)
   int* node;       // slot -> node id
   int* slot;       // node id -> slot
-  int* grm;        // local rows: smallest float q (ordered int)
+  int* grm;        // every slot: smallest float q of its row (ordered int), pushed by the row's owner
   int4* grc;       // local rows: second smallest q (ordered int), column and distance of the smallest
   float* tvl;      // local rows: the new row's value in this join
   // slot -> owner CTA and local row
@@ -1233,8 +1233,8 @@ template <int C>
 __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_kernel(const NJJob* jobs, int njobs) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ NJJob sjob;
-  __shared__ float spart[2];   // this CTA's pass partial (read by the other CTAs)
-  __shared__ USum susum;       // this CTA's share sum (read by the other CTAs)
+  __shared__ float sparts[2 * 16];   // every CTA's pass partial (pushed by each CTA)
+  __shared__ USum susums[16];        // every CTA's share sum (pushed by each CTA)
   __shared__ int rows_sel[kFastRows];
   __shared__ GCand fc[kFastRows];
   __shared__ int nsel, s_ok;
@@ -1289,7 +1289,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
     m.node[k] = k;
     act[k] = k;
   }
-  for (int l = tid; l < m.lr; l += nth) m.grm[l] = 0x7F7FFFFF;
+  for (int k = tid; k < n; k += nth) m.grm[k] = 0x7F7FFFFF;
   if (rank == 0 && tid == 0) {
     s.g32[2] = 0;
     s.stats[0] = s.stats[1] = s.stats[2] = s.stats[3] = s.stats[4] = 0;
@@ -1323,7 +1323,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
           if (r < 0) continue;
           const float tr = m.Tf[r];
           if (tr != tr) {   // dead
-            if (lane == 0) m.grm[l] = 0x7F7FFFFF;
+            if (lane < C) m.at(m.grm, lane)[r] = 0x7F7FFFFF;
             continue;
           }
           const float* row = m.rows + (size_t)l * m.ldl;
@@ -1351,10 +1351,11 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
             c1 = take ? oc1 : c1;
             mag = fmaxf(mag, __shfl_xor_sync(0xffffffffu, mag, o));
           }
+          // the pick reads only what the pass wrote (a fast CTA's join share
+          // may already be changing rows and row sums); the row minimum goes to
+          // every CTA
+          if (lane < C) m.at(m.grm, lane)[r] = ford(m1);
           if (lane == 0) {
-            // the pick reads only what the pass wrote (a fast CTA's join share
-            // may already be changing rows and row sums)
-            m.grm[l] = ford(m1);
             m.grc[l] = make_int4(ford(m2), c1, __float_as_int(c1 >= 0 ? row[c1] : 0.f), 0);
             m.Tsn[l] = m.Tloc[l];
           }
@@ -1375,21 +1376,17 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
           qmin = fminf(qmin, __shfl_xor_sync(0xffffffffu, qmin, o));
           mmax = fmaxf(mmax, __shfl_xor_sync(0xffffffffu, mmax, o));
         }
-        if (lane == 0) {
-          spart[0] = qmin;
-          spart[1] = mmax;
+        if (lane < C) {
+          float* dst = m.at(sparts, lane);
+          dst[2 * rank] = qmin;
+          dst[2 * rank + 1] = mmax;
         }
       }
     }
     cl.sync();
     // ---- pick: threshold from the CTA partials, rows within it, candidates
     if (warp == 0) {
-      float q = FLT_MAX, mm = 0.f;
-      if (lane < C) {
-        const float* pp = m.at(spart, lane);
-        q = pp[0];
-        mm = pp[1];
-      }
+      float q = lane < C ? sparts[2 * lane] : FLT_MAX, mm = lane < C ? sparts[2 * lane + 1] : 0.f;
       for (int o = 16; o > 0; o >>= 1) {
         q = fminf(q, __shfl_xor_sync(0xffffffffu, q, o));
         mm = fmaxf(mm, __shfl_xor_sync(0xffffffffu, mm, o));
@@ -1402,10 +1399,8 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
     __syncthreads();
     const float thr = sthr;
     const int othr = ford(thr);
-    for (int t = tid; t < C * m.lr; t += nth) {
-      const int q = t / m.lr, l = t - q * m.lr;
-      const int r = m.slot_of(q, l);
-      if (r >= 0 && m.at(m.grm, q)[l] <= othr) {
+    for (int r = tid; r < n; r += nth) {
+      if (m.grm[r] <= othr) {
         const int k = atomicAdd(&nsel, 1);
         if (k < kFastRows) rows_sel[k] = r;
       }
@@ -1453,7 +1448,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
       // fallback: each CTA scans its own rows within the threshold into the list
       for (int l = 0; l < m.lr; ++l) {
         const int r = m.slot_of(rank, l);
-        if (r < 0 || m.grm[l] > othr) continue;
+        if (r < 0 || m.grm[r] > othr) continue;
         const int ur = m.node[r];
         const float tr = m.Tf[r];
         const double Tr = m.Tloc[l];
@@ -1537,7 +1532,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
       __syncthreads();   // also: every read of this join's maps is done
       if (tid == 0) {
         for (int w2 = 1; w2 < nwv; ++w2) usum_add(x, swp[w2]);
-        susum = x;
+        for (int q = 0; q < C; ++q) m.at(susums, q)[rank] = x;   // to every CTA
       }
       // the maps and the active list, identically in every CTA
       for (int k = tid; k < m_n; k += nth) {
@@ -1561,7 +1556,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
       x.u = x.a = 0;
       x.e = INT_MAX;
       x.t = INT_MIN;
-      if (lane < C) x = *m.at(&susum, lane);
+      if (lane < C) x = susums[lane];
       usum_warp(x);
       if (lane == 0) {
         if (x.e == INT_MAX) {
