@@ -15,7 +15,8 @@
 //   A lane's 8 rows of one column make one 32-bit word; the 32 lanes of a
 //   step store 32 consecutive words (one 128-byte line): word (b*(Lx+31) + t)
 //   *32 + k holds rows b*256 + 8k .. +7 at column t-k, row r in bits 4r..4r+3.
-// back_kernel: one thread per pair walks from (Lx-1, Ly-1) with the
+// The walk runs in lane 0 of the same warp right after the pair's last band,
+//   while its flags are still in L2: one thread per pair walks from (Lx-1, Ly-1) with the
 //   reference's rule set (continue flags of the previous move first, then up,
 //   then left, else diagonal), row -1 reads as left+continue, column -1 as
 //   up+continue, and an up move out of row 0 ends the walk (the reference's
@@ -33,7 +34,7 @@ namespace {
 
 constexpr int kTR = 8;             // rows per lane
 constexpr int kTBand = 32 * kTR;   // rows per band
-constexpr int kTWarps = 1;         // warps (pairs) per CTA (24 KB profile per warp)
+constexpr int kTWarps = 4;         // warps (pairs) per CTA (6 KB profile per warp)
 
 struct TraceArgs {
   const int8_t* codes;
@@ -60,9 +61,69 @@ __device__ __forceinline__ unsigned tclamp(int c) {
   return u < (unsigned)kLetters ? u : (unsigned)(kLetters - 1);
 }
 
+__constant__ char c_dec[kLetters + 1] = "ARNDCQEGHILKMFPSTWYVBZX*";   // code -> letter
+
+static_assert(kTR == 8, "a lane's scores of one column are one 8-byte load");
+
+__device__ __forceinline__ unsigned nibble_at(const uint32_t* nib, int Lx, int x, int y) {
+  if (y < 0) return x < 0 ? 0u : 9u;     // row -1: left + continue-left; corner: stop
+  if (x < 0) return 6u;                  // column -1: up + continue-up
+  const int b = y / kTBand, yy = y - b * kTBand, k = yy / kTR;
+  const uint32_t w = nib[((size_t)b * (Lx + 31) + (x + k)) * 32 + k];
+  return (w >> (4 * (yy - k * kTR))) & 15u;
+}
+
+// The backtrace of pair p from its flags (one thread).
+__device__ void walk_pair(const TraceArgs& a, int p) {
+  const int ix = a.px[p], iy = a.py[p];
+  const int8_t* X = a.codes + a.start[ix];
+  const int8_t* Y = a.codes + a.start[iy];
+  const int Lx = a.len[ix], Ly = a.len[iy];
+  const uint32_t* nib = a.nib + a.nib_off[p];
+  char* ox = a.outx + (size_t)p * a.stride;
+  char* oy = a.outy + (size_t)p * a.stride;
+  int x = Lx - 1, y = Ly - 1, k = 0;
+  unsigned prev = 12u;
+  unsigned cell = nibble_at(nib, Lx, x, y);
+  const int cap = Lx + Ly;
+  while ((cell & 12u) && k < cap) {
+    unsigned todo;
+    if (((prev & 12u) == 4u) && (prev & 2u)) todo = 4u;
+    else if (((prev & 12u) == 8u) && (prev & 1u)) todo = 8u;
+    else if ((cell & 12u) == 4u) todo = 4u;
+    else if ((cell & 12u) == 8u) todo = 8u;
+    else todo = 12u;
+    // a well-formed matrix never asks for a move off the -1 row/column other
+    // than the ones handled below; stop rather than read outside the inputs
+    if ((todo != 4u && x < 0) || (todo != 8u && y < 0)) break;
+    bool stop = false;
+    if (todo == 8u) {
+      ox[k] = c_dec[tclamp(X[x])];
+      oy[k] = '-';
+      --x;
+    } else if (todo == 4u) {
+      ox[k] = '-';
+      oy[k] = c_dec[tclamp(Y[y])];
+      --y;
+      stop = y < 0;     // no word reload for row -1 after an up move
+    } else {
+      ox[k] = c_dec[tclamp(X[x])];
+      oy[k] = c_dec[tclamp(Y[y])];
+      --x;
+      --y;
+    }
+    prev = todo | (cell & 3u);
+    ++k;
+    cell = stop ? 0u : nibble_at(nib, Lx, x, y);
+  }
+  ox[k] = 0;
+  oy[k] = 0;
+  a.outlen[p] = k;
+}
+
 __global__ void __launch_bounds__(32 * kTWarps) match_kernel(const TraceArgs a) {
   __shared__ int8_t s_sub[kLetters * kLetters];
-  __shared__ int32_t s_prof[kTWarps][kLetters * kTBand];   // per-warp profile [letter][row]
+  __shared__ __align__(8) int8_t s_prof[kTWarps][kLetters * kTBand];   // per-warp profile [letter][row]
   for (int e = threadIdx.x; e < kLetters * kLetters; e += blockDim.x) s_sub[e] = a.sub[e];
   __syncthreads();
   const int lane = threadIdx.x & 31;
@@ -75,7 +136,7 @@ __global__ void __launch_bounds__(32 * kTWarps) match_kernel(const TraceArgs a) 
   const int Lx = a.len[ix], Ly = a.len[iy];
   const int go = a.go, ge = a.ge;
   const int nb = (Ly + kTBand - 1) / kTBand;
-  int32_t* prof = s_prof[warp];
+  int8_t* prof = s_prof[warp];
   int32_t* scr = a.scratch + (size_t)p * 4 * a.scratch_cols;
   uint32_t* nib = a.nib + a.nib_off[p];
   const int kSent = kShortMin + ge;
@@ -84,7 +145,7 @@ __global__ void __launch_bounds__(32 * kTWarps) match_kernel(const TraceArgs a) 
     __syncwarp();
     for (int e = lane; e < kLetters * kTBand; e += 32) {
       const int x = e / kTBand, row = e - x * kTBand, grow = b * kTBand + row;
-      prof[e] = grow < Ly ? (int)s_sub[tclamp(Y[grow]) * kLetters + x] : 0;
+      prof[e] = grow < Ly ? s_sub[tclamp(Y[grow]) * kLetters + x] : (int8_t)0;
     }
     __syncwarp();
     const int rowbase = b * kTBand + lane * kTR;
@@ -112,7 +173,8 @@ __global__ void __launch_bounds__(32 * kTWarps) match_kernel(const TraceArgs a) 
             fin = rd[2 * c + 1];
           }
         }
-        const int* pr = prof + tclamp(X[c]) * kTBand + lane * kTR;
+        // the lane's 8 scores of column c: one 8-byte load
+        const uint2 pw = *reinterpret_cast<const uint2*>(prof + tclamp(X[c]) * kTBand + lane * kTR);
         int diag = hprev;
         hprev = hin;
         int f = fin, hup = hin;
@@ -123,7 +185,8 @@ __global__ void __launch_bounds__(32 * kTWarps) match_kernel(const TraceArgs a) 
           f = max(fo, hup - go);
           const int eo = E[r] - ge;
           const int e = max(eo, H[r] - go);
-          const int sim = diag + pr[r];
+          const int sv = (int)(int8_t)((r < 4 ? pw.x : pw.y) >> (8 * (r & 3)));
+          const int sim = diag + sv;
           int h = max(e, f);
           h = max(h, sim);
           const uint32_t L = ((h == e) && (h != f)) || (h == sim);
@@ -154,64 +217,10 @@ __global__ void __launch_bounds__(32 * kTWarps) match_kernel(const TraceArgs a) 
       a.score[p] = v;
     }
   }
-}
-
-__device__ __forceinline__ unsigned nibble_at(const uint32_t* nib, int Lx, int x, int y) {
-  if (y < 0) return x < 0 ? 0u : 9u;     // row -1: left + continue-left; corner: stop
-  if (x < 0) return 6u;                  // column -1: up + continue-up
-  const int b = y / kTBand, yy = y - b * kTBand, k = yy / kTR;
-  const uint32_t w = nib[((size_t)b * (Lx + 31) + (x + k)) * 32 + k];
-  return (w >> (4 * (yy - k * kTR))) & 15u;
-}
-
-__global__ void back_kernel(const TraceArgs a) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= a.npairs) return;
-  const int ix = a.px[p], iy = a.py[p];
-  const int8_t* X = a.codes + a.start[ix];
-  const int8_t* Y = a.codes + a.start[iy];
-  const int Lx = a.len[ix], Ly = a.len[iy];
-  const uint32_t* nib = a.nib + a.nib_off[p];
-  char* ox = a.outx + (size_t)p * a.stride;
-  char* oy = a.outy + (size_t)p * a.stride;
-  const char kDec[kLetters + 1] = "ARNDCQEGHILKMFPSTWYVBZX*";
-  int x = Lx - 1, y = Ly - 1, k = 0;
-  unsigned prev = 12u;
-  unsigned cell = nibble_at(nib, Lx, x, y);
-  const int cap = Lx + Ly;
-  while ((cell & 12u) && k < cap) {
-    unsigned todo;
-    if (((prev & 12u) == 4u) && (prev & 2u)) todo = 4u;
-    else if (((prev & 12u) == 8u) && (prev & 1u)) todo = 8u;
-    else if ((cell & 12u) == 4u) todo = 4u;
-    else if ((cell & 12u) == 8u) todo = 8u;
-    else todo = 12u;
-    // a well-formed matrix never asks for a move off the -1 row/column other
-    // than the ones handled below; stop rather than read outside the inputs
-    if ((todo != 4u && x < 0) || (todo != 8u && y < 0)) break;
-    bool stop = false;
-    if (todo == 8u) {
-      ox[k] = kDec[tclamp(X[x])];
-      oy[k] = '-';
-      --x;
-    } else if (todo == 4u) {
-      ox[k] = '-';
-      oy[k] = kDec[tclamp(Y[y])];
-      --y;
-      stop = y < 0;     // no word reload for row -1 after an up move
-    } else {
-      ox[k] = kDec[tclamp(X[x])];
-      oy[k] = kDec[tclamp(Y[y])];
-      --x;
-      --y;
-    }
-    prev = todo | (cell & 3u);
-    ++k;
-    cell = stop ? 0u : nibble_at(nib, Lx, x, y);
-  }
-  ox[k] = 0;
-  oy[k] = 0;
-  a.outlen[p] = k;
+  // the walk, while the pair's flags are still in L2 (the warp's stores are
+  // visible to lane 0 after the warp barrier)
+  __syncwarp();
+  if (lane == 0) walk_pair(a, p);
 }
 
 }  // namespace
@@ -314,8 +323,7 @@ int Ctx::align_pairs(const int8_t* codes, const int64_t* offsets, int n, const i
     a.ge = ge;
     a.sub = (const int8_t*)b_sub.p;
     match_kernel<<<(m + kTWarps - 1) / kTWarps, 32 * kTWarps, 0, s>>>(a);
-    back_kernel<<<(m + 127) / 128, 128, 0, s>>>(a);
-    launches += 2;
+    ++launches;
     if ((rc = cuda(cudaGetLastError(), "traceback launch"))) return rc;
     if ((rc = cuda(cudaMemcpyAsync(outx + (size_t)k0 * stride, T.outx.p, (size_t)m * stride, cudaMemcpyDeviceToHost, s),
                    "download")) ||
