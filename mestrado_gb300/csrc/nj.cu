@@ -1316,51 +1316,59 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
       float qmin = FLT_MAX, mmax = 0.f;
       const float4* Tf4 = reinterpret_cast<const float4*>(m.Tf);
       const int nv = m.ldl >> 2;
-      for (int lp = warp; 2 * lp < m.lr; lp += nth >> 5) {
-        for (int h = 0; h < 2; ++h) {
-          const int l = 2 * lp + h;
-          const int r = m.slot_of(rank, l);
-          if (r < 0) continue;
-          const float tr = m.Tf[r];
-          if (tr != tr) {   // dead
-            if (lane < C) m.at(m.grm, lane)[r] = 0x7F7FFFFF;
-            continue;
-          }
-          const float* row = m.rows + (size_t)l * m.ldl;
-          float m1 = FLT_MAX, m2 = FLT_MAX, mag = 0.f;
-          int c1 = -1;
-          const int c0 = r + 1, v0 = (c0 + 3) >> 2;
-          if (lane < 4 * v0 - c0 && c0 + lane < n) pass_elem(row[c0 + lane], m.Tf[c0 + lane], c0 + lane, tr, nm2f, m1, m2, c1, mag);
-          const float4* row4 = reinterpret_cast<const float4*>(row);
-          for (int v = v0 + lane; v < nv; v += 32) {
-            const float4 d = row4[v];
-            const float4 tc = Tf4[v];
-            pass_elem(d.x, tc.x, 4 * v, tr, nm2f, m1, m2, c1, mag);
-            pass_elem(d.y, tc.y, 4 * v + 1, tr, nm2f, m1, m2, c1, mag);
-            pass_elem(d.z, tc.z, 4 * v + 2, tr, nm2f, m1, m2, c1, mag);
-            pass_elem(d.w, tc.w, 4 * v + 3, tr, nm2f, m1, m2, c1, mag);
-          }
-          for (int o = 16; o > 0; o >>= 1) {
-            const float om1 = __shfl_xor_sync(0xffffffffu, m1, o);
-            const float om2 = __shfl_xor_sync(0xffffffffu, m2, o);
-            const int oc1 = __shfl_xor_sync(0xffffffffu, c1, o);
-            const bool take = om1 < m1 || (om1 == m1 && oc1 < c1);
-            const float lo = take ? om1 : m1, hi = take ? m1 : om1;
-            m2 = fminf(hi, fminf(m2, om2));
-            m1 = lo;
-            c1 = take ? oc1 : c1;
-            mag = fmaxf(mag, __shfl_xor_sync(0xffffffffu, mag, o));
-          }
-          // the pick reads only what the pass wrote (a fast CTA's join share
-          // may already be changing rows and row sums); the row minimum goes to
-          // every CTA
-          if (lane < C) m.at(m.grm, lane)[r] = ford(m1);
-          if (lane == 0) {
-            m.grc[l] = make_int4(ford(m2), c1, __float_as_int(c1 >= 0 ? row[c1] : 0.f), 0);
-            m.Tsn[l] = m.Tloc[l];
-          }
-          qmin = fminf(qmin, m1);
-          mmax = fmaxf(mmax, __fadd_rn(mag, fabsf(tr)));
+      auto row_pass = [&](int l) {
+        const int r = m.slot_of(rank, l);
+        if (r < 0) return;
+        const float tr = m.Tf[r];
+        if (tr != tr) {   // dead
+          if (lane < C) m.at(m.grm, lane)[r] = 0x7F7FFFFF;
+          return;
+        }
+        const float* row = m.rows + (size_t)l * m.ldl;
+        float m1 = FLT_MAX, m2 = FLT_MAX, mag = 0.f;
+        int c1 = -1;
+        const int c0 = r + 1, v0 = (c0 + 3) >> 2;
+        if (lane < 4 * v0 - c0 && c0 + lane < n) pass_elem(row[c0 + lane], m.Tf[c0 + lane], c0 + lane, tr, nm2f, m1, m2, c1, mag);
+        const float4* row4 = reinterpret_cast<const float4*>(row);
+        for (int v = v0 + lane; v < nv; v += 32) {
+          const float4 d = row4[v];
+          const float4 tc = Tf4[v];
+          pass_elem(d.x, tc.x, 4 * v, tr, nm2f, m1, m2, c1, mag);
+          pass_elem(d.y, tc.y, 4 * v + 1, tr, nm2f, m1, m2, c1, mag);
+          pass_elem(d.z, tc.z, 4 * v + 2, tr, nm2f, m1, m2, c1, mag);
+          pass_elem(d.w, tc.w, 4 * v + 3, tr, nm2f, m1, m2, c1, mag);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+          const float om1 = __shfl_xor_sync(0xffffffffu, m1, o);
+          const float om2 = __shfl_xor_sync(0xffffffffu, m2, o);
+          const int oc1 = __shfl_xor_sync(0xffffffffu, c1, o);
+          const bool take = om1 < m1 || (om1 == m1 && oc1 < c1);
+          const float lo = take ? om1 : m1, hi = take ? m1 : om1;
+          m2 = fminf(hi, fminf(m2, om2));
+          m1 = lo;
+          c1 = take ? oc1 : c1;
+          mag = fmaxf(mag, __shfl_xor_sync(0xffffffffu, mag, o));
+        }
+        // the pick reads only what the pass wrote (a fast CTA's join share
+        // may already be changing rows and row sums); the row minimum goes to
+        // every CTA
+        if (lane < C) m.at(m.grm, lane)[r] = ford(m1);
+        if (lane == 0) {
+          m.grc[l] = make_int4(ford(m2), c1, __float_as_int(c1 >= 0 ? row[c1] : 0.f), 0);
+          m.Tsn[l] = m.Tloc[l];
+        }
+        qmin = fminf(qmin, m1);
+        mmax = fmaxf(mmax, __fadd_rn(mag, fabsf(tr)));
+      };
+      // one row per warp when the CTA's rows fit its warps (the two rows'
+      // reductions then run side by side), else one row pair per warp
+      const int nw = nth >> 5;
+      if (m.lr <= nw) {
+        if (warp < m.lr) row_pass(warp);
+      } else {
+        for (int lp = warp; 2 * lp < m.lr; lp += nw) {
+          row_pass(2 * lp);
+          row_pass(2 * lp + 1);
         }
       }
       __shared__ float wq[32], wm[32];
