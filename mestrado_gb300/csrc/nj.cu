@@ -1897,15 +1897,10 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
   return NWG_OK;
 }
 
-}  // namespace nwg
-
-namespace nwg {
-
-// Workspace of one job of the per-CTA path, laid out from `base` (256-byte
-// aligned pieces); D is the job's matrix (modified in place).
-// Workspace of one job of the cluster form, laid out from `base` (256-byte
+// Workspace of one job of the cluster forms, laid out from `base` (256-byte
 // aligned pieces); fills *J when given.  The job's matrix is separate (n rows
-// of ld floats, ld a multiple of 4, modified in place).
+// of ld floats, ld a multiple of 4; the form over L2 modifies it in place,
+// the shared-memory form only reads it).
 static size_t job_layout(int n, int ld, char* base, NJJob* J) {
   auto al = [](size_t x) { return (x + 255) / 256 * 256; };
   const size_t cap = std::min<size_t>(kCandCap, (size_t)n * (n - 1) / 2 + 1);
