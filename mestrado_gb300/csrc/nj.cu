@@ -1244,7 +1244,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
   __shared__ double s_sum;
   __shared__ int s_exact;
   namespace cg = cooperative_groups;
-  cg::cluster_group cl = cg::this_cluster();
+  const int crank = (int)cg::this_cluster().block_rank();
   const int job = (int)blockIdx.x / C;   // the same for every CTA of the cluster
   if (job >= njobs) return;
   if (threadIdx.x == 0) sjob = jobs[job];
@@ -1259,7 +1259,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
     sm.npairs = (n + 1) / 2;
     sm.ldl = L.ldl;
     sm.lr = L.lr;
-    sm.rank = (int)cl.block_rank();
+    sm.rank = crank;
     sm.rows = reinterpret_cast<float*>(smem + L.rows);
     sm.Tf = reinterpret_cast<float*>(smem + L.tf);
     sm.Tloc = reinterpret_cast<double*>(smem + L.tloc);
@@ -1294,12 +1294,12 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
     s.g32[2] = 0;
     s.stats[0] = s.stats[1] = s.stats[2] = s.stats[3] = s.stats[4] = 0;
   }
-  cl.sync();   // every CTA's row-sum array is NaN before any broadcast lands
+  cg::this_cluster().sync();   // every CTA's row-sum array is NaN before any broadcast lands
   if (n >= 2) {
     __syncthreads();
     smem_rowsums(m, act, n);
   }
-  cl.sync();
+  cg::this_cluster().sync();
   const int kBinT = 30 * 31 / 2;
   int steps = max((int)((float)n * 0.5f), 200);
   int pq_ck = 500;
@@ -1314,21 +1314,30 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
     // ---- pass: each warp one local pair, 16-byte loads from shared memory
     {
       float qmin = FLT_MAX, mmax = 0.f;
-      const float4* Tf4 = reinterpret_cast<const float4*>(m.Tf);
-      const int nv = m.ldl >> 2;
+      // the layout's fields in registers (shared-memory stores below would
+      // otherwise make the compiler reload them)
+      const float* const Tfp = m.Tf;
+      const float* const rowsp = m.rows;
+      const int ldl = m.ldl;
+      int* const grmp = m.grm;
+      int4* const grcp = m.grc;
+      double* const tsnp = m.Tsn;
+      const double* const tlocp = m.Tloc;
+      const float4* Tf4 = reinterpret_cast<const float4*>(Tfp);
+      const int nv = ldl >> 2;
       auto row_pass = [&](int l) {
         const int r = m.slot_of(rank, l);
         if (r < 0) return;
-        const float tr = m.Tf[r];
+        const float tr = Tfp[r];
         if (tr != tr) {   // dead
-          if (lane < C) m.at(m.grm, lane)[r] = 0x7F7FFFFF;
+          if (lane < C) m.at(grmp, lane)[r] = 0x7F7FFFFF;
           return;
         }
-        const float* row = m.rows + (size_t)l * m.ldl;
+        const float* row = rowsp + (size_t)l * ldl;
         float m1 = FLT_MAX, m2 = FLT_MAX, mag = 0.f;
         int c1 = -1;
         const int c0 = r + 1, v0 = (c0 + 3) >> 2;
-        if (lane < 4 * v0 - c0 && c0 + lane < n) pass_elem(row[c0 + lane], m.Tf[c0 + lane], c0 + lane, tr, nm2f, m1, m2, c1, mag);
+        if (lane < 4 * v0 - c0 && c0 + lane < n) pass_elem(row[c0 + lane], Tfp[c0 + lane], c0 + lane, tr, nm2f, m1, m2, c1, mag);
         const float4* row4 = reinterpret_cast<const float4*>(row);
         for (int v = v0 + lane; v < nv; v += 32) {
           const float4 d = row4[v];
@@ -1352,24 +1361,82 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
         // the pick reads only what the pass wrote (a fast CTA's join share
         // may already be changing rows and row sums); the row minimum goes to
         // every CTA
-        if (lane < C) m.at(m.grm, lane)[r] = ford(m1);
+        if (lane < C) m.at(grmp, lane)[r] = ford(m1);
         if (lane == 0) {
-          m.grc[l] = make_int4(ford(m2), c1, __float_as_int(c1 >= 0 ? row[c1] : 0.f), 0);
-          m.Tsn[l] = m.Tloc[l];
+          grcp[l] = make_int4(ford(m2), c1, __float_as_int(c1 >= 0 ? row[c1] : 0.f), 0);
+          tsnp[l] = tlocp[l];
         }
         qmin = fminf(qmin, m1);
         mmax = fmaxf(mmax, __fadd_rn(mag, fabsf(tr)));
       };
-      // one row per warp when the CTA's rows fit its warps (the two rows'
-      // reductions then run side by side), else one row pair per warp
+      // a row pair per warp, the two rows' warp reductions in the same
+      // shuffle rounds
+      auto pair_pass = [&](int lp) {
+        float m1[2], m2[2], mag[2], trs[2];
+        int c1[2], rs[2];
+        bool live[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int l = 2 * lp + h;
+          rs[h] = m.slot_of(rank, l);
+          trs[h] = rs[h] >= 0 ? Tfp[rs[h]] : 0.f;
+          live[h] = rs[h] >= 0 && trs[h] == trs[h];
+          if (rs[h] >= 0 && !live[h] && lane < C) m.at(grmp, lane)[rs[h]] = 0x7F7FFFFF;   // dead
+          m1[h] = m2[h] = FLT_MAX;
+          mag[h] = 0.f;
+          c1[h] = -1;
+          if (!live[h]) continue;
+          const int r = rs[h];
+          const float tr = trs[h];
+          const float* row = rowsp + (size_t)l * ldl;
+          const int c0 = r + 1, v0 = (c0 + 3) >> 2;
+          if (lane < 4 * v0 - c0 && c0 + lane < n)
+            pass_elem(row[c0 + lane], Tfp[c0 + lane], c0 + lane, tr, nm2f, m1[h], m2[h], c1[h], mag[h]);
+          const float4* row4 = reinterpret_cast<const float4*>(row);
+          for (int v = v0 + lane; v < nv; v += 32) {
+            const float4 d = row4[v];
+            const float4 tc = Tf4[v];
+            pass_elem(d.x, tc.x, 4 * v, tr, nm2f, m1[h], m2[h], c1[h], mag[h]);
+            pass_elem(d.y, tc.y, 4 * v + 1, tr, nm2f, m1[h], m2[h], c1[h], mag[h]);
+            pass_elem(d.z, tc.z, 4 * v + 2, tr, nm2f, m1[h], m2[h], c1[h], mag[h]);
+            pass_elem(d.w, tc.w, 4 * v + 3, tr, nm2f, m1[h], m2[h], c1[h], mag[h]);
+          }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const float om1 = __shfl_xor_sync(0xffffffffu, m1[h], o);
+            const float om2 = __shfl_xor_sync(0xffffffffu, m2[h], o);
+            const int oc1 = __shfl_xor_sync(0xffffffffu, c1[h], o);
+            const bool take = om1 < m1[h] || (om1 == m1[h] && oc1 < c1[h]);
+            const float lo = take ? om1 : m1[h], hi = take ? m1[h] : om1;
+            m2[h] = fminf(hi, fminf(m2[h], om2));
+            m1[h] = lo;
+            c1[h] = take ? oc1 : c1[h];
+            mag[h] = fmaxf(mag[h], __shfl_xor_sync(0xffffffffu, mag[h], o));
+          }
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          if (!live[h]) continue;
+          const int l = 2 * lp + h, r = rs[h];
+          if (lane < C) m.at(grmp, lane)[r] = ford(m1[h]);
+          if (lane == 0) {
+            const float* row = rowsp + (size_t)l * ldl;
+            grcp[l] = make_int4(ford(m2[h]), c1[h], __float_as_int(c1[h] >= 0 ? row[c1[h]] : 0.f), 0);
+            tsnp[l] = tlocp[l];
+          }
+          qmin = fminf(qmin, m1[h]);
+          mmax = fmaxf(mmax, __fadd_rn(mag[h], fabsf(trs[h])));
+        }
+      };
+      // one row per warp when the CTA's rows fit its warps, else one row pair
+      // per warp
       const int nw = nth >> 5;
       if (m.lr <= nw) {
         if (warp < m.lr) row_pass(warp);
       } else {
-        for (int lp = warp; 2 * lp < m.lr; lp += nw) {
-          row_pass(2 * lp);
-          row_pass(2 * lp + 1);
-        }
+        for (int lp = warp; 2 * lp < m.lr; lp += nw) pair_pass(lp);
       }
       __shared__ float wq[32], wm[32];
       if (lane == 0) {
@@ -1391,7 +1458,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
         }
       }
     }
-    cl.sync();
+    cg::this_cluster().sync();
     // ---- pick: threshold from the CTA partials, rows within it, candidates
     if (warp == 0) {
       float q = lane < C ? sparts[2 * lane] : FLT_MAX, mm = lane < C ? sparts[2 * lane + 1] : 0.f;
@@ -1475,7 +1542,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
           }
         }
       }
-      cl.sync();
+      cg::this_cluster().sync();
       if (warp == 0) {
         const int ncount = *(volatile int*)&s.g32[2];
         const int nc = min(ncount, s.cand_cap);
@@ -1557,7 +1624,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
         m.Tf[sj] = __int_as_float(0x7FC00000);
       }
     }
-    cl.sync();
+    cg::this_cluster().sync();
     // ---- apply: the new node's row sum from the CTA sums
     if (warp == 0) {
       USum x;
@@ -1597,7 +1664,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
         for (int q = 0; q < C; ++q) m.at(m.Tf, q)[si] = tf;
         m.at(m.Tloc, m.owner(si))[m.local_row(si)] = sum;
       }
-      cl.sync();
+      cg::this_cluster().sync();
     }
     if (rank == 0 && tid == 0) {
       nwg_join& J = s.joins[step];
@@ -1625,21 +1692,21 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
     }
     const int m_after = m_n - 1;
     if (steps == 0) {
-      cl.sync();   // every CTA's own write of the new row sum lands before the broadcasts
+      cg::this_cluster().sync();   // every CTA's own write of the new row sum lands before the broadcasts
       smem_rowsums(m, act, m_after);
       if (rank == 0 && tid == 0) s.stats[4] += 1;
       watermark = next + 1;
       steps = (m_after < 200) ? INT_MAX : (int)((float)m_after * 0.5f);
       ave0 = (((long long)(m_after - 1) * m_after) / 2) / kBinT;
       ub = ((long long)m_after * (m_after - 1)) / 2;
-      cl.sync();
+      cg::this_cluster().sync();
     } else {
       --steps;
       ub += m_after - 1;
       __syncthreads();
     }
   }
-  cl.sync();   // every join record is written; no CTA reads another's shared memory after this
+  cg::this_cluster().sync();   // every join record is written; no CTA reads another's shared memory after this
   if (!failed)
     for (int k = rank * nth + tid; k < n - 1; k += C * nth) join_lengths(s.joins[k]);
 }

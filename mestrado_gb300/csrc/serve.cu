@@ -244,23 +244,25 @@ int Server::launch_batch(Slot& S) {
       (rc = S.njws.ensure((size_t)total_ws)) || (rc = S.njdesc.ensure(desc * nj)))
     return rc;
   // pinned staging: codes, then the plan arrays, then NJ descriptors
-  // NJ descriptors: jobs whose join loop runs in a cluster's shared memory
-  // first (one launch), the others after them (one launch)
-  int nmax_small = 0;
-  for (ServeJob* J : S.batch)
-    if (J->n <= kNJSmemServeMax) nmax_small = std::max(nmax_small, J->n);
-  const int csm = nmax_small > 0 ? smem_nj_cluster(nmax_small) : 0;
+  // NJ descriptors grouped by launch form: jobs whose join loop runs in a
+  // cluster's shared memory first, then the rest (join loop over L2); one
+  // launch per group
+  int nmax_g[2] = {0, 0}, cnt_g[2] = {0, 0};
+  std::vector<int> form(nj);
+  for (int k = 0; k < nj; ++k) {
+    const int n = S.batch[k]->n;
+    form[k] = n <= kNJSmemServeMax && smem_nj_cluster(n) ? 0 : 1;
+    nmax_g[form[k]] = std::max(nmax_g[form[k]], n);
+    ++cnt_g[form[k]];
+  }
+  const int c_smem = cnt_g[0] ? smem_nj_cluster(nmax_g[0]) : 0;
   std::vector<char> descs(desc * nj);
   std::vector<nwg_join*> jptr(nj);
   std::vector<unsigned long long*> sptr(nj);
-  int n_small = 0, nmax_big = 1;
-  for (ServeJob* J : S.batch)
-    if (csm && J->n <= nmax_small) ++n_small;
-  for (int k = 0, a = 0, b = n_small; k < nj; ++k) {
+  int next_idx[2] = {0, cnt_g[0]};
+  for (int k = 0; k < nj; ++k) {
     ServeJob* J = S.batch[k];
-    const bool small = csm && J->n <= nmax_small;
-    J->desc_idx = (size_t)(small ? a++ : b++);
-    if (!small) nmax_big = std::max(nmax_big, J->n);
+    J->desc_idx = (size_t)next_idx[form[k]]++;
     nj_job_setup(&descs[desc * J->desc_idx], (float*)S.D.p + J->d_off, J->n, nj_row_stride(J->n),
                  (char*)S.njws.p + J->nj_off, &jptr[k], &sptr[k]);
   }
@@ -343,13 +345,13 @@ int Server::launch_batch(Slot& S) {
   }
   if ((rc = c.cuda(cudaMemcpyAsync(S.h_D.p, S.D.p, sizeof(float) * total_D, cudaMemcpyDeviceToHost, st), "serve")))
     return rc;
-  // join loops: one cluster per job; the small jobs in one launch with the
-  // matrix in the cluster's shared memory, the others in one launch over L2
-  // (jobs with 256 sequences or more take the device's largest cluster)
-  if (n_small && (rc = c.cuda(launch_nj_smem(S.njdesc.p, n_small, nmax_small, csm, st), "serve nj launch"))) return rc;
-  if (nj > n_small) {
-    const int csize = nmax_big >= kNJWideN ? nj_cluster_size() : kNJClusterServe;
-    if ((rc = c.cuda(launch_nj_cluster((const char*)S.njdesc.p + desc * n_small, nj - n_small, csize, st),
+  // join loops, one cluster per job, one launch per form (jobs with 256
+  // sequences or more take the device's largest cluster)
+  if (cnt_g[0] && (rc = c.cuda(launch_nj_smem(S.njdesc.p, cnt_g[0], nmax_g[0], c_smem, st), "serve nj launch")))
+    return rc;
+  if (cnt_g[1]) {
+    const int csize = nmax_g[1] >= kNJWideN ? nj_cluster_size() : kNJClusterServe;
+    if ((rc = c.cuda(launch_nj_cluster((const char*)S.njdesc.p + desc * cnt_g[0], cnt_g[1], csize, st),
                      "serve nj launch")))
       return rc;
   }
