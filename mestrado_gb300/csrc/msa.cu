@@ -15,12 +15,15 @@
 //  1. msa_dp_kernel, one CTA per merge: 256 rows per strip, one thread per
 //     row, an anti-diagonal step per __syncthreads; thread r keeps
 //     W[x] = sum_y cY[r][y] S[x][y] in registers, so a cell costs 24
-//     multiply-adds; (H, F) of the row above comes through shared memory, the
-//     bottom row of a strip through global scratch; the 4 flag bits of every
-//     cell are stored one byte per cell, anti-diagonal major (coalesced);
-//  2. msa_walk_kernel, one thread per merge: the traceback rules, ops in
-//     forward order (columns the walk leaves are appended opposite gaps);
-//  3. msa_build_kernel, one CTA per merge: the merged profile and, for both
+//     multiply-adds (in int32 when kX * kY * max|S| < 2^31, which bounds the
+//     sum; else in int64), with the next column's counts loaded a step
+//     ahead; (H, F) of the row above comes through shared memory, the bottom
+//     row of a strip through global scratch; the 4 flag bits of every cell
+//     are stored one byte per cell, anti-diagonal major (coalesced); then
+//     thread 0 walks the flags with the traceback rules while they are still
+//     in L2, ops in forward order (columns the walk leaves are appended
+//     opposite gaps);
+//  2. msa_build_kernel, one CTA per merge: the merged profile and, for both
 //     children, the map of their columns to the new ones.
 // At the end the final position of every column is resolved parents first
 // (msa_pos_kernel) and every leaf's residues are scattered into its row.
@@ -44,97 +47,10 @@ struct MergeDesc {
   int64_t scratch;            // first (H, F) pair of the strip-boundary scratch (lx entries)
   int32_t lx, ly, kx, ky;
   int32_t nops;               // written by the walk
-  int32_t pad;
+  int32_t mac32;              // kx * ky * max|S| < 2^31: a cell's score sum fits int32
 };
 
 __device__ __forceinline__ int64_t mx64(int64_t a, int64_t b) { return a > b ? a : b; }
-
-__global__ void __launch_bounds__(kMR) msa_dp_kernel(const MergeDesc* __restrict__ md, const int16_t* __restrict__ cnt,
-                                                     uint8_t* __restrict__ nib, longlong2* __restrict__ scratch,
-                                                     const int8_t* __restrict__ sub, int go, int ge) {
-  __shared__ int8_t s_sub[kLetters * kLetters];
-  __shared__ int64_t sh_h[2][kMR], sh_f[2][kMR];
-  const MergeDesc m = md[blockIdx.x];
-  for (int e = threadIdx.x; e < kLetters * kLetters; e += blockDim.x) s_sub[e] = sub[e];
-  __syncthreads();
-  const int lx = m.lx, ly = m.ly;
-  const int64_t kk = (int64_t)m.kx * m.ky;
-  const int64_t GO = (int64_t)go * kk, GE = (int64_t)ge * kk;
-  const int64_t kSent = -(((int64_t)1) << 60);
-  const int16_t* X = cnt + m.xoff * kLetters;
-  const int16_t* Y = cnt + m.yoff * kLetters;
-  longlong2* bnd = scratch + m.scratch;
-  const int tid = threadIdx.x;
-  const int nstrips = (ly + kMR - 1) / kMR;
-  for (int sidx = 0; sidx < nstrips; ++sidx) {
-    const int r = sidx * kMR + tid;       // this thread's row
-    const bool live = r < ly;
-    int32_t W[kLetters];
-#pragma unroll
-    for (int x = 0; x < kLetters; ++x) W[x] = 0;
-    if (live) {
-      const int16_t* cy = Y + (size_t)r * kLetters;
-      for (int b = 0; b < kLetters; ++b) {
-        const int c = cy[b];
-        if (c == 0) continue;
-#pragma unroll
-        for (int x = 0; x < kLetters; ++x) W[x] += c * (int)s_sub[b * kLetters + x];
-      }
-    }
-    int64_t hleft = -GE * (r + 1), eleft = kSent;
-    int64_t diag = -GE * r;               // H[r-1][-1] (0 for row 0)
-    uint8_t* nb = nib + m.nib + (size_t)sidx * (size_t)(lx + kMR - 1) * kMR;
-    const int steps = lx + kMR - 1;
-    for (int t = 0; t < steps; ++t) {
-      const int c = t - tid;
-      const int par = t & 1;
-      if (live && c >= 0 && c < lx) {
-        int64_t hup, fup;
-        if (tid == 0) {
-          if (sidx == 0) {
-            hup = -GE * (c + 1);
-            fup = kSent;
-          } else {
-            const longlong2 v = bnd[c];
-            hup = v.x;
-            fup = v.y;
-          }
-        } else {
-          hup = sh_h[par ^ 1][tid - 1];
-          fup = sh_f[par ^ 1][tid - 1];
-        }
-        const uint4* cx4 = reinterpret_cast<const uint4*>(X + (size_t)c * kLetters);
-        int64_t s = 0;
-#pragma unroll
-        for (int q = 0; q < 3; ++q) {
-          const uint4 v = cx4[q];
-          const uint32_t w[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-          for (int h = 0; h < 4; ++h) {
-            s += (int64_t)(int16_t)(w[h] & 0xFFFFu) * W[q * 8 + 2 * h];
-            s += (int64_t)(int16_t)(w[h] >> 16) * W[q * 8 + 2 * h + 1];
-          }
-        }
-        const int64_t f = mx64(fup - GE, hup - GO);
-        const uint32_t cu = f == fup - GE;
-        const int64_t e = mx64(eleft - GE, hleft - GO);
-        const uint32_t cl = e == eleft - GE;
-        const int64_t sim = diag + s;
-        const int64_t h = mx64(mx64(e, f), sim);
-        const uint32_t L = ((h == e) && (h != f)) || (h == sim);
-        const uint32_t U = (h == f) || (h == sim);
-        nb[(size_t)t * kMR + tid] = (uint8_t)((L << 3) | (U << 2) | (cu << 1) | cl);
-        diag = hup;
-        hleft = h;
-        eleft = e;
-        sh_h[par][tid] = h;
-        sh_f[par][tid] = f;
-        if (tid == kMR - 1 && sidx + 1 < nstrips) bnd[c] = make_longlong2(h, f);
-      }
-      __syncthreads();
-    }
-  }
-}
 
 __device__ __forceinline__ unsigned msa_nib(const uint8_t* nib, int lx, int x, int y) {
   if (y < 0) return x < 0 ? 0u : 9u;     // row -1: left + continue-left; corner: stop
@@ -143,10 +59,9 @@ __device__ __forceinline__ unsigned msa_nib(const uint8_t* nib, int lx, int x, i
   return nib[(size_t)s * (size_t)(lx + kMR - 1) * kMR + (size_t)(x + yl) * kMR + yl];
 }
 
-__global__ void msa_walk_kernel(MergeDesc* md, int nm, const uint8_t* __restrict__ nib, uint8_t* __restrict__ ops) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= nm) return;
-  MergeDesc& m = md[p];
+// The traceback rules of the cherry alignment over the merge's flags, ops in
+// forward order (one thread).
+__device__ void msa_walk(MergeDesc& m, const uint8_t* nib, uint8_t* ops) {
   const int lx = m.lx, ly = m.ly;
   const uint8_t* nb = nib + m.nib;
   uint8_t* op = ops + m.ops;
@@ -184,6 +99,122 @@ __global__ void msa_walk_kernel(MergeDesc* md, int nm, const uint8_t* __restrict
     --y;
   }
   m.nops = k;
+}
+
+__global__ void __launch_bounds__(kMR) msa_dp_kernel(MergeDesc* md, const int16_t* __restrict__ cnt, uint8_t* nib,
+                                                     longlong2* __restrict__ scratch, const int8_t* __restrict__ sub,
+                                                     int go, int ge, uint8_t* __restrict__ ops) {
+  __shared__ int8_t s_sub[kLetters * kLetters];
+  __shared__ int64_t sh_h[2][kMR], sh_f[2][kMR];
+  const MergeDesc m = md[blockIdx.x];
+  for (int e = threadIdx.x; e < kLetters * kLetters; e += blockDim.x) s_sub[e] = sub[e];
+  __syncthreads();
+  const int lx = m.lx, ly = m.ly;
+  const int64_t kk = (int64_t)m.kx * m.ky;
+  const int64_t GO = (int64_t)go * kk, GE = (int64_t)ge * kk;
+  const int64_t kSent = -(((int64_t)1) << 60);
+  const int16_t* X = cnt + m.xoff * kLetters;
+  const int16_t* Y = cnt + m.yoff * kLetters;
+  longlong2* bnd = scratch + m.scratch;
+  const int tid = threadIdx.x;
+  const int nstrips = (ly + kMR - 1) / kMR;
+  for (int sidx = 0; sidx < nstrips; ++sidx) {
+    const int r = sidx * kMR + tid;       // this thread's row
+    const bool live = r < ly;
+    int32_t W[kLetters];
+#pragma unroll
+    for (int x = 0; x < kLetters; ++x) W[x] = 0;
+    if (live) {
+      const int16_t* cy = Y + (size_t)r * kLetters;
+      for (int b = 0; b < kLetters; ++b) {
+        const int c = cy[b];
+        if (c == 0) continue;
+#pragma unroll
+        for (int x = 0; x < kLetters; ++x) W[x] += c * (int)s_sub[b * kLetters + x];
+      }
+    }
+    int64_t hleft = -GE * (r + 1), eleft = kSent;
+    int64_t diag = -GE * r;               // H[r-1][-1] (0 for row 0)
+    uint8_t* nb = nib + m.nib + (size_t)sidx * (size_t)(lx + kMR - 1) * kMR;
+    const int steps = lx + kMR - 1;
+    // the counts of this thread's column, loaded one step ahead
+    auto load_col = [&](int c, uint4 (&v)[3]) {
+      if (c >= 0 && c < lx) {
+        const uint4* p = reinterpret_cast<const uint4*>(X + (size_t)c * kLetters);
+        v[0] = p[0];
+        v[1] = p[1];
+        v[2] = p[2];
+      }
+    };
+    uint4 cur[3] = {}, nxt[3] = {};
+    load_col(-tid, cur);
+    for (int t = 0; t < steps; ++t) {
+      const int c = t - tid;
+      const int par = t & 1;
+      load_col(c + 1, nxt);
+      if (live && c >= 0 && c < lx) {
+        int64_t hup, fup;
+        if (tid == 0) {
+          if (sidx == 0) {
+            hup = -GE * (c + 1);
+            fup = kSent;
+          } else {
+            const longlong2 v = bnd[c];
+            hup = v.x;
+            fup = v.y;
+          }
+        } else {
+          hup = sh_h[par ^ 1][tid - 1];
+          fup = sh_f[par ^ 1][tid - 1];
+        }
+        int64_t s = 0;
+        if (m.mac32) {   // |s| <= kx * ky * max|S| < 2^31
+          int32_t s32 = 0;
+#pragma unroll
+          for (int q = 0; q < 3; ++q) {
+            const uint32_t w[4] = {cur[q].x, cur[q].y, cur[q].z, cur[q].w};
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+              s32 += (int32_t)(int16_t)(w[h] & 0xFFFFu) * W[q * 8 + 2 * h];
+              s32 += (int32_t)(int16_t)(w[h] >> 16) * W[q * 8 + 2 * h + 1];
+            }
+          }
+          s = s32;
+        } else {
+#pragma unroll
+          for (int q = 0; q < 3; ++q) {
+            const uint32_t w[4] = {cur[q].x, cur[q].y, cur[q].z, cur[q].w};
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+              s += (int64_t)(int16_t)(w[h] & 0xFFFFu) * W[q * 8 + 2 * h];
+              s += (int64_t)(int16_t)(w[h] >> 16) * W[q * 8 + 2 * h + 1];
+            }
+          }
+        }
+        const int64_t f = mx64(fup - GE, hup - GO);
+        const uint32_t cu = f == fup - GE;
+        const int64_t e = mx64(eleft - GE, hleft - GO);
+        const uint32_t cl = e == eleft - GE;
+        const int64_t sim = diag + s;
+        const int64_t h = mx64(mx64(e, f), sim);
+        const uint32_t L = ((h == e) && (h != f)) || (h == sim);
+        const uint32_t U = (h == f) || (h == sim);
+        nb[(size_t)t * kMR + tid] = (uint8_t)((L << 3) | (U << 2) | (cu << 1) | cl);
+        diag = hup;
+        hleft = h;
+        eleft = e;
+        sh_h[par][tid] = h;
+        sh_f[par][tid] = f;
+        if (tid == kMR - 1 && sidx + 1 < nstrips) bnd[c] = make_longlong2(h, f);
+      }
+#pragma unroll
+      for (int q = 0; q < 3; ++q) cur[q] = nxt[q];
+      __syncthreads();
+    }
+  }
+  // the walk, while the merge's flags are still in L2 (the CTA barrier above
+  // makes every thread's flags visible to thread 0)
+  if (tid == 0) msa_walk(md[blockIdx.x], nib, ops);
 }
 
 // Merged profile and child maps; one CTA per merge, ops scanned in chunks.
@@ -366,6 +397,8 @@ int Ctx::msa(const int8_t* codes, const int64_t* offsets, int n, const int32_t* 
   std::vector<std::vector<int>> bylevel(levels + 1);
   for (int k = 0; k < n - 1; ++k) bylevel[height[n + k]].push_back(n + k);
   int64_t cells = 0;
+  int64_t smax = 1;   // largest |S| of the context's matrix
+  for (int k = 0; k < kLetters * kLetters; ++k) smax = std::max<int64_t>(smax, sub[k] < 0 ? -sub[k] : sub[k]);
   std::vector<MergeDesc> md;
   for (int l = 1; l <= levels; ++l) {
     const std::vector<int>& nodes = bylevel[l];
@@ -381,6 +414,7 @@ int Ctx::msa(const int8_t* codes, const int64_t* offsets, int n, const int32_t* 
       d.ly = (int)len[b];
       d.kx = kseq[a];
       d.ky = kseq[b];
+      d.mac32 = (int64_t)d.kx * d.ky * smax < ((int64_t)1 << 31) ? 1 : 0;
       d.xmap = col[a];
       d.ymap = col[b];
       d.ooff = pool;
@@ -402,13 +436,11 @@ int Ctx::msa(const int8_t* codes, const int64_t* offsets, int n, const int32_t* 
       return fail(rc, "msa allocation");
     if ((rc = cuda(cudaMemcpyAsync(M.md.p, md.data(), sizeof(MergeDesc) * nm, cudaMemcpyHostToDevice, s), "msa upload")))
       return rc;
-    msa_dp_kernel<<<nm, kMR, 0, s>>>((const MergeDesc*)M.md.p, (const int16_t*)M.cnt.p, (uint8_t*)M.nib.p,
-                                     (longlong2*)M.scratch.p, (const int8_t*)b_sub.p, go, ge);
-    msa_walk_kernel<<<(nm + 127) / 128, 128, 0, s>>>((MergeDesc*)M.md.p, nm, (const uint8_t*)M.nib.p,
-                                                    (uint8_t*)M.ops.p);
+    msa_dp_kernel<<<nm, kMR, 0, s>>>((MergeDesc*)M.md.p, (const int16_t*)M.cnt.p, (uint8_t*)M.nib.p,
+                                     (longlong2*)M.scratch.p, (const int8_t*)b_sub.p, go, ge, (uint8_t*)M.ops.p);
     msa_build_kernel<<<nm, 1024, 0, s>>>((const MergeDesc*)M.md.p, (int16_t*)M.cnt.p, (int32_t*)M.maps.p,
                                         (const uint8_t*)M.ops.p);
-    launches += 3;
+    launches += 2;
     if ((rc = cuda(cudaGetLastError(), "msa launch"))) return rc;
     // the new profiles' lengths (the next level sizes its work with them)
     if ((rc = cuda(cudaMemcpyAsync(md.data(), M.md.p, sizeof(MergeDesc) * nm, cudaMemcpyDeviceToHost, s), "msa")) ||
