@@ -62,6 +62,24 @@ def test_serving_mix_equals_alone_and_context(ctx):
         assert im["nj_ambiguous_steps"] == 0
 
 
+def test_serving_batch_with_both_join_forms(ctx):
+    # one batch holding jobs of up to 768 sequences (join loop in a cluster's
+    # shared memory) and a job above that (join loop over L2): two launches in
+    # one batch, every job as the context path gives it
+    # (the first job usually goes alone; the big one, submitted last, joins
+    # the small ones that arrive while the first batch runs)
+    jobs = [S for _, S in synth.serving_jobs(6, seed=31, n_hi=400, median=60)]
+    jobs.append(synth.family(900, 40, ps=0.1, pi=0.01, seed=7))
+    with Server(hbm_budget=8 << 30, max_batch_jobs=8) as srv:
+        res = _run(srv, jobs)
+    assert max(info["batch_jobs"] for _, _, info in res) > 1
+    for S, (D, J, info) in zip(jobs, res):
+        assert info["status"] == 0
+        Dc = ctx.score_all(S)
+        assert np.array_equal(D, Dc)
+        _same_joins(J, ctx.nj(Dc))
+
+
 def test_serving_matches_oracle():
     jobs = [S for _, S in synth.serving_jobs(6, seed=21, n_hi=40, median=120)]
     with Server(max_batch_jobs=6) as srv:
