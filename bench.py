@@ -496,8 +496,9 @@ def main():
     ap.add_argument("--subset", type=int, default=0,
                     help="score only the first N sequences (whole families first); for profiling runs")
     ap.add_argument("--no-pipeline", action="store_true", help="skip the configuration-3 pipeline leg")
-    ap.add_argument("--serve-seconds", type=float, default=10.0,
-                    help="length of the serving run (Poisson arrivals at 200 jobs/s); 0 skips it")
+    ap.add_argument("--serve-seconds", type=float, default=60.0,
+                    help="length of the serving run (Poisson arrivals at 200 jobs/s, configuration 4: "
+                         "60 s); 0 skips it")
     ap.add_argument("--quick", action="store_true",
                     help="device-resident timing only (no e2e, plain, CPU or parity legs); for profiling runs")
     args = ap.parse_args()
