@@ -894,6 +894,7 @@ __global__ void __launch_bounds__(1024, 1) nj_grid_kernel(NJDev s, GridNJ g, int
   __shared__ float sthr;
   const Team tm{(int)blockIdx.x, (int)gridDim.x};
   unsigned target = 0;
+  if (*(volatile int*)g.abort) return;   // an earlier segment gave up: every CTA leaves
   for (int p = (int)(blockIdx.x * blockDim.x + threadIdx.x); p < s.n0; p += (int)(gridDim.x * blockDim.x))
     g.grmin[p] = 0x7F7FFFFF;   // ordered int of FLT_MAX
   if (blockIdx.x == 0 && threadIdx.x == 0) s.g32[2] = 0;
@@ -1893,6 +1894,13 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
       const bool comp = d.n0 >= kCompactMinSlots && step + d.n0 / kCompactFrac < seg_end;
       if (comp) seg_end = step + d.n0 / kCompactFrac;
       if ((rc = cuda(cudaMemsetAsync(S.gbar.p, 0, sizeof(unsigned) * 2, s), "nj launch"))) return rc;
+      // failure injection for the tests (NWG_NJ_INJECT_BARRIER_STALL=1): the
+      // arrival count of the first segment starts one short, so its first
+      // barrier never completes and every CTA gives up after the spin limit
+      if (step == 0 && std::getenv("NWG_NJ_INJECT_BARRIER_STALL") &&
+          std::atoi(std::getenv("NWG_NJ_INJECT_BARRIER_STALL")) == 1 &&
+          (rc = cuda(cudaMemsetAsync(S.gbar.p, 0xFF, sizeof(unsigned), s), "nj launch")))
+        return rc;
       {
         int a0 = step, a1 = seg_end, an = n, aw = watermark;
         void* args[] = {&d, &g, &a0, &a1, &an, &aw};

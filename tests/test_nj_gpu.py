@@ -152,3 +152,25 @@ def test_every_nj_form_matches_reference_tree(case, path):
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     r = subprocess.run([sys.executable, "-c", code], cwd=root, env=env, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0 and r.stdout.strip().endswith("ok"), r.stdout + r.stderr
+
+
+def test_grid_barrier_timeout_is_reported_and_context_recovers(ctx):
+    # failure detection without a GPU fault: the first grid barrier of the
+    # full-GPU form is made unreachable (its arrival count starts one short),
+    # every CTA gives up after the spin limit (about two seconds), the call
+    # returns a CUDA status, and the same context then joins correctly
+    from mestrado_gb300 import NWGError
+    from mestrado_gb300._native import NWG_ERR_CUDA
+    S = synth.family(2100, 36, ps=0.1, pi=0.01, seed=17)   # above the cluster threshold: the full-GPU form
+    D = ctx.score_all(S)
+    os.environ["NWG_NJ_INJECT_BARRIER_STALL"] = "1"
+    try:
+        with pytest.raises(NWGError) as e:
+            ctx.nj(D)
+        assert e.value.status == NWG_ERR_CUDA
+    finally:
+        del os.environ["NWG_NJ_INJECT_BARRIER_STALL"]
+    joins = ctx.nj(D)
+    oj, _ = O.nj(D)
+    for a, b in zip(joins, oj):
+        assert (a["i"], a["j"], a["len_i"], a["len_j"]) == (b["i"], b["j"], b["len_i"], b["len_j"])
