@@ -1119,6 +1119,343 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_cluster_
   for (int k = t0; k < n - 1; k += tstride) join_lengths(s.joins[k]);
 }
 
+// ---- small jobs: the whole join loop in one CTA ----------------------------
+// Up to kCtaNJMax taxa one CTA holds the job in its shared memory: the rows,
+// T, the float row sums, the maps and the active lists.  A thread scans its
+// own folded row pair sequentially (no per-row warp reduction), and every
+// phase boundary is a CTA barrier; the new node's row sum is complete when the
+// join share's block reduction is.  The arithmetic is that of the other forms.
+
+constexpr int kCtaNJMax = 160;   // above it a cluster's shared memory is faster (measured crossover near 170)
+constexpr int kCtaThreads = 256;
+
+struct CtaLayout {
+  int ldl;
+  size_t rows, tf, t, node, slot, act_a, act_b, grm, grc, tv, bytes;
+};
+
+__host__ __device__ inline CtaLayout cta_layout(int n) {
+  auto al = [](size_t x) { return (x + 15) / 16 * 16; };
+  CtaLayout L;
+  L.ldl = (n + 3) & ~3;
+  size_t o = 0;
+  L.rows = o; o += al(sizeof(float) * (size_t)n * L.ldl);
+  L.tf = o; o += al(sizeof(float) * L.ldl);
+  L.t = o; o += al(sizeof(double) * n);
+  L.node = o; o += al(sizeof(int) * n);
+  L.slot = o; o += al(sizeof(int) * 2 * n);
+  L.act_a = o; o += al(sizeof(int) * (n + 1));
+  L.act_b = o; o += al(sizeof(int) * (n + 1));
+  L.grm = o; o += al(sizeof(int) * n);
+  L.grc = o; o += al(sizeof(int4) * n);
+  L.tv = o; o += al(sizeof(float) * n);
+  L.bytes = o;
+  return L;
+}
+
+// Block-wide reduction of a USum over kCtaThreads threads (result in thread 0).
+__device__ __forceinline__ USum cta_usum(USum x, USum* swarp) {
+  usum_warp(x);
+  if ((threadIdx.x & 31) == 0) swarp[threadIdx.x >> 5] = x;
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int w = 1; w < kCtaThreads / 32; ++w) usum_add(x, swarp[w]);
+  return x;
+}
+
+__global__ void __launch_bounds__(kCtaThreads, 1) nj_cta_kernel(const NJJob* jobs, int njobs) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ NJJob sjob;
+  __shared__ float wq[kCtaThreads / 32], wm[kCtaThreads / 32];
+  __shared__ USum swarp[kCtaThreads / 32];
+  __shared__ int rows_sel[kFastRows];
+  __shared__ GCand fc[kFastRows];
+  __shared__ int nsel, s_ok;
+  __shared__ PickOut spick;
+  __shared__ GCand swin;
+  __shared__ float sthr;
+  __shared__ double s_sum;
+  __shared__ int s_exact;
+  if ((int)blockIdx.x >= njobs) return;
+  if (threadIdx.x == 0) sjob = jobs[blockIdx.x];
+  __syncthreads();
+  const NJDev& s = sjob.s;
+  const GridNJ& g = sjob.g;
+  const int n = sjob.n;
+  const CtaLayout L = cta_layout(n);
+  const int ldl = L.ldl;
+  float* rows = reinterpret_cast<float*>(smem + L.rows);
+  float* Tf = reinterpret_cast<float*>(smem + L.tf);
+  double* T = reinterpret_cast<double*>(smem + L.t);
+  int* node = reinterpret_cast<int*>(smem + L.node);
+  int* slot = reinterpret_cast<int*>(smem + L.slot);
+  int* act = reinterpret_cast<int*>(smem + L.act_a);
+  int* act2 = reinterpret_cast<int*>(smem + L.act_b);
+  int* grm = reinterpret_cast<int*>(smem + L.grm);
+  int4* grc = reinterpret_cast<int4*>(smem + L.grc);
+  float* tv = reinterpret_cast<float*>(smem + L.tv);
+  const int tid = (int)threadIdx.x, nth = kCtaThreads;
+  const int lane = tid & 31, warp = tid >> 5;
+  for (int e = tid; e < n * ldl; e += nth) {
+    const int r = e / ldl, c = e - r * ldl;
+    rows[e] = c < n ? s.D[(size_t)r * s.ld + c] : 0.f;
+  }
+  for (int k = tid; k < ldl; k += nth) Tf[k] = __int_as_float(0x7FC00000);
+  for (int k = tid; k < 2 * n; k += nth) slot[k] = k < n ? k : -1;
+  for (int k = tid; k < n; k += nth) {
+    node[k] = k;
+    act[k] = k;
+  }
+  if (tid == 0) {
+    s.g32[2] = 0;
+    s.stats[0] = s.stats[1] = s.stats[2] = s.stats[3] = s.stats[4] = 0;
+  }
+  __syncthreads();
+  // row sums (buildGblRowSums): a thread per row, the reference's sequential
+  // double sum over the active list in ascending id order
+  auto rowsums = [&](int na) {
+    for (int k = tid; k < na; k += nth) {
+      const int r = slot[act[k]];
+      const float* row = rows + (size_t)r * ldl;
+      double sum = 0.0;
+      for (int j = 0; j < na; ++j) sum = __dadd_rn(sum, (double)row[slot[act[j]]]);
+      T[r] = sum;
+      Tf[r] = __double2float_rn(sum);
+    }
+    __syncthreads();
+  };
+  if (n >= 2) rowsums(n);
+  const int kBinT = 30 * 31 / 2;
+  int steps = max((int)((float)n * 0.5f), 200);
+  int pq_ck = 500;
+  long long ave0 = (((long long)(n - 1) * n) / 2) / kBinT;
+  long long ub = ((long long)n * (n - 1)) / 2;
+  int watermark = n;
+  const int npairs = (n + 1) / 2;
+  for (int step = 0; step < n - 1; ++step) {
+    const int m_n = n - step, next = n + step;
+    const float nm2f = (float)(m_n - 2);
+    const double nm2 = (double)(m_n - 2);
+    // ---- pass: a thread per folded row pair, its rows scanned sequentially
+    float qmin = FLT_MAX, mmax = 0.f;
+    if (tid < npairs) {
+#pragma unroll 1
+      for (int h = 0; h < 2; ++h) {
+        const int r = h ? n - 1 - tid : tid;
+        if (h && r == tid) break;
+        const float tr = Tf[r];
+        if (tr != tr) {   // dead
+          grm[r] = 0x7F7FFFFF;
+          continue;
+        }
+        const float* row = rows + (size_t)r * ldl;
+        float m1 = FLT_MAX, m2 = FLT_MAX, mag = 0.f;
+        int c1 = -1;
+        for (int c = r + 1; c < n; ++c) pass_elem(row[c], Tf[c], c, tr, nm2f, m1, m2, c1, mag);
+        grm[r] = ford(m1);
+        grc[r] = make_int4(ford(m2), c1, __float_as_int(c1 >= 0 ? row[c1] : 0.f), 0);
+        qmin = fminf(qmin, m1);
+        mmax = fmaxf(mmax, __fadd_rn(mag, fabsf(tr)));
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      qmin = fminf(qmin, __shfl_xor_sync(0xffffffffu, qmin, o));
+      mmax = fmaxf(mmax, __shfl_xor_sync(0xffffffffu, mmax, o));
+    }
+    if (lane == 0) {
+      wq[warp] = qmin;
+      wm[warp] = mmax;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      float q = FLT_MAX, mm = 0.f;
+      for (int w = 0; w < nth / 32; ++w) {
+        q = fminf(q, wq[w]);
+        mm = fmaxf(mm, wm[w]);
+      }
+      sthr = q + 3.f * (8.f * 5.9604645e-8f * mm) + 1e-30f;
+      nsel = 0;
+    }
+    __syncthreads();
+    // ---- pick
+    const float thr = sthr;
+    const int othr = ford(thr);
+    for (int r = tid; r < n; r += nth) {
+      if (grm[r] <= othr) {
+        const int k = atomicAdd(&nsel, 1);
+        if (k < kFastRows) rows_sel[k] = r;
+      }
+    }
+    __syncthreads();
+    const int nr = nsel;
+    if (warp == 0) {
+      int ok = nr >= 1 && nr <= kFastRows;
+      if (ok && lane < nr) {
+        const int r = rows_sel[lane];
+        const int4 rec = grc[r];
+        const int c = rec.y;
+        if (rec.x <= othr || c < 0) {
+          ok = 0;   // a second pair of the row within the threshold
+        } else {
+          fc[lane] = make_cand(r, c, node[r], node[c], T[r], T[c], __int_as_float(rec.z), nm2, watermark);
+        }
+      }
+      ok = __all_sync(0xffffffffu, ok);
+      PickOut pr{};
+      if (ok && nr == 1) {
+        pr.idx = 0;
+        pr.ties = 1;
+        pr.amb = 0;
+        pr.error = false;
+      } else if (ok) {
+        pr = pick_keys(nr, [&](int k) { return fc[k]; });
+      }
+      if (lane == 0) {
+        s_ok = ok;
+        if (ok) {
+          spick = pr;
+          swin = fc[pr.idx];
+        }
+      }
+    }
+    __syncthreads();
+    if (!s_ok) {
+      // fallback: the selected rows' pairs within the threshold into the list
+      for (int r = 0; r < n; ++r) {
+        if (grm[r] > othr) continue;
+        const int ur = node[r];
+        const float tr = Tf[r];
+        const float* row = rows + (size_t)r * ldl;
+        for (int c = r + 1 + tid; c < n; c += nth) {
+          const int uc = node[c];
+          if (uc < 0) continue;
+          const float d = row[c];
+          const float q = __fsub_rn(__fsub_rn(__fmul_rn(d, nm2f), tr), Tf[c]);
+          if (q > thr) continue;
+          const int idx = atomicAdd(&s.g32[2], 1);
+          if (idx < s.cand_cap) {
+            const GCand cd = make_cand(r, c, ur, uc, T[r], T[c], d, nm2, watermark);
+            g.cand[idx] = KCand{cd.k1, cd.k2, cd.a, cd.b};
+          }
+        }
+      }
+      __syncthreads();
+      if (warp == 0) {
+        const int ncount = *(volatile int*)&s.g32[2];
+        const int nc = min(ncount, s.cand_cap);
+        PickOut pr = pick_keys(nc, [&](int k) { return g.cand[k]; });
+        pr.error = pr.error || ncount > s.cand_cap;
+        if (lane == 0) {
+          spick = pr;
+          if (!pr.error) {
+            const KCand w = g.cand[pr.idx];
+            const int sa = slot[w.a], sb = slot[w.b];
+            const int r0 = min(sa, sb), c0 = max(sa, sb);
+            swin = make_cand(r0, c0, node[r0], node[c0], T[r0], T[c0], rows[(size_t)r0 * ldl + c0], nm2, watermark);
+          }
+          s.g32[2] = 0;
+        }
+      }
+      __syncthreads();
+      if (spick.error) {
+        if (tid == 0) record_pick(s, spick);
+        break;
+      }
+    }
+    // ---- join share: a thread per slot
+    const GCand w = swin;
+    const int i = w.a, j = w.b, si = w.sa, sj = w.sb;
+    USum x;
+    x.u = x.a = 0;
+    x.e = INT_MAX;
+    x.t = INT_MIN;
+    for (int p = tid; p < n; p += nth) {
+      if (node[p] < 0 || p == si || p == sj) continue;
+      float* row = rows + (size_t)p * ldl;
+      const float sumf = __fadd_rn(row[si], row[sj]);
+      const float tmp = __fmul_rn(__fsub_rn(sumf, w.d), 0.5f);
+      const double t = __dadd_rn(T[p], (double)__fsub_rn(tmp, sumf));
+      T[p] = t;
+      Tf[p] = __double2float_rn(t);
+      row[si] = tmp;
+      rows[(size_t)si * ldl + p] = tmp;
+      tv[p] = tmp;
+      if (tmp != 0.f) {
+        USum y;
+        y.e = low_bit_exp(tmp);
+        y.t = top_bit_exp(tmp);
+        y.u = float_units(tmp, y.e);
+        y.a = y.u < 0 ? -y.u : y.u;
+        usum_add(x, y);
+      }
+    }
+    for (int k = tid; k < m_n; k += nth) {
+      const int v = act[k];
+      if (v != i && v != j) act2[k - (v > i) - (v > j)] = v;
+    }
+    x = cta_usum(x, swarp);   // ends with every thread past the share
+    if (tid == 0) {
+      double sum;
+      if (x.e == INT_MAX) {
+        sum = 0.0;
+      } else if (x.t - x.e < 48 && x.a < (1ll << 53)) {
+        sum = units_to_double(x.u, x.e);   // exact: the sequential sum's value
+      } else {
+        sum = 0.0;   // the reference's loop: active ids ascending, i and j skipped
+        for (int k = 0; k < m_n; ++k) {
+          const int v = act[k];
+          if (v != i && v != j) sum = __dadd_rn(sum, (double)tv[slot[v]]);
+        }
+      }
+      T[si] = sum;
+      Tf[si] = __double2float_rn(sum);
+      Tf[sj] = __int_as_float(0x7FC00000);
+      node[sj] = -1;
+      node[si] = next;
+      slot[j] = -1;
+      slot[i] = -1;
+      slot[next] = si;
+      act2[m_n - 2] = next;
+      nwg_join& J = s.joins[step];
+      J.i = i;
+      J.j = j;
+      J.node = next;
+      J.n = m_n;
+      J.d = w.d;
+      J.pad = 0.f;
+      J.q = w.q1;
+      J.ti = w.ta;
+      J.tj = w.tb;
+      record_pick(s, spick);
+    }
+    {
+      int* t = act;
+      act = act2;
+      act2 = t;
+    }
+    // ---- the reference's rebuild schedule (SpeciesBlock.cpp:864, :1206-1247)
+    if (--pq_ck == 0) {
+      pq_ck = 500;
+      if (steps > 0 && (double)(ub / kBinT) / (double)ave0 > 2.0 && tid == 0) s.stats[3] += 1;
+    }
+    const int m_after = m_n - 1;
+    __syncthreads();
+    if (steps == 0) {
+      rowsums(m_after);
+      if (tid == 0) s.stats[4] += 1;
+      watermark = next + 1;
+      steps = (m_after < 200) ? INT_MAX : (int)((float)m_after * 0.5f);
+      ave0 = (((long long)(m_after - 1) * m_after) / 2) / kBinT;
+      ub = ((long long)m_after * (m_after - 1)) / 2;
+    } else {
+      --steps;
+      ub += m_after - 1;
+    }
+  }
+  __syncthreads();
+  for (int k = tid; k < n - 1; k += nth) join_lengths(s.joins[k]);
+}
+
 // ---- small jobs: the whole join loop in the cluster's shared memory --------
 // Up to kSmemNJMax taxa the matrix fits the distributed shared memory of one
 // cluster.  CTA q holds the rows of the folded slot pairs p = q, q + C, ...
@@ -1779,7 +2116,9 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
     if ((rc = cuda(cudaMemcpyAsync(S.desc.p, &J, sizeof(J), cudaMemcpyHostToDevice, s), "nj upload"))) return rc;
     if (st) cudaEventRecord(ev0, s);
     const int csm = smem_nj_cluster(n);
-    if ((rc = cuda(csm ? launch_nj_smem(S.desc.p, 1, n, csm, s) : launch_nj_cluster(S.desc.p, 1, nj_cluster_size(), s),
+    if ((rc = cuda(n <= cta_nj_max_n() ? launch_nj_cta(S.desc.p, 1, n, s)
+                   : csm               ? launch_nj_smem(S.desc.p, 1, n, csm, s)
+                                       : launch_nj_cluster(S.desc.p, 1, nj_cluster_size(), s),
                    "nj launch")))
       return rc;
     ++launches;
@@ -2058,6 +2397,25 @@ cudaError_t launch_nj_cluster(const void* d_jobs, int njobs, int C, cudaStream_t
   } else {
     nj_cluster_kernel<8><<<njobs * 8, 1024, 0, s>>>(jobs, njobs);
   }
+  return cudaGetLastError();
+}
+
+// Jobs of at most this many taxa run the join loop in one CTA
+// (nj_cta_kernel); NWG_NJ_CTA_MAX_N overrides it (0: never).
+int cta_nj_max_n() {
+  static const int v = [] {
+    const char* e = std::getenv("NWG_NJ_CTA_MAX_N");
+    return e ? std::min(std::atoi(e), kCtaNJMax) : kCtaNJMax;
+  }();
+  return v;
+}
+
+cudaError_t launch_nj_cta(const void* d_jobs, int njobs, int nmax, cudaStream_t s) {
+  if (njobs <= 0) return cudaSuccess;
+  const int bytes = (int)cta_layout(std::max(nmax, 2)).bytes;
+  cudaError_t e = cudaFuncSetAttribute(nj_cta_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e != cudaSuccess) return e;
+  nj_cta_kernel<<<njobs, kCtaThreads, bytes, s>>>(reinterpret_cast<const NJJob*>(d_jobs), njobs);
   return cudaGetLastError();
 }
 

@@ -163,6 +163,9 @@ size_t nj_job_desc_bytes();
 cudaError_t launch_encode(const char* d_src, const int64_t* d_src_off, const int64_t* d_dst_off, const int32_t* d_len,
                           int n, int8_t* d_dst, int* d_bad, cudaStream_t s);
 cudaError_t launch_nj_cluster(const void* d_jobs, int njobs, int C, cudaStream_t s);
+// jobs of at most cta_nj_max_n() taxa: the join loop in one CTA's shared memory
+int cta_nj_max_n();
+cudaError_t launch_nj_cta(const void* d_jobs, int njobs, int nmax, cudaStream_t s);
 // jobs of at most smem_nj_max_n() taxa: the join loop in the cluster's shared memory
 int smem_nj_cluster(int nmax);
 cudaError_t launch_nj_smem(const void* d_jobs, int njobs, int nmax, int C, cudaStream_t s);

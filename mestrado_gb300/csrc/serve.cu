@@ -244,22 +244,22 @@ int Server::launch_batch(Slot& S) {
       (rc = S.njws.ensure((size_t)total_ws)) || (rc = S.njdesc.ensure(desc * nj)))
     return rc;
   // pinned staging: codes, then the plan arrays, then NJ descriptors
-  // NJ descriptors grouped by launch form: jobs whose join loop runs in a
-  // cluster's shared memory first, then the rest (join loop over L2); one
-  // launch per group
-  int nmax_g[2] = {0, 0}, cnt_g[2] = {0, 0};
+  // NJ descriptors grouped by launch form: jobs whose join loop runs in one
+  // CTA, then in a cluster's shared memory, then the rest (join loop over
+  // L2); one launch per group
+  int nmax_g[3] = {0, 0, 0}, cnt_g[3] = {0, 0, 0};
   std::vector<int> form(nj);
   for (int k = 0; k < nj; ++k) {
     const int n = S.batch[k]->n;
-    form[k] = n <= kNJSmemServeMax && smem_nj_cluster(n) ? 0 : 1;
+    form[k] = n <= cta_nj_max_n() ? 0 : (n <= kNJSmemServeMax && smem_nj_cluster(n) ? 1 : 2);
     nmax_g[form[k]] = std::max(nmax_g[form[k]], n);
     ++cnt_g[form[k]];
   }
-  const int c_smem = cnt_g[0] ? smem_nj_cluster(nmax_g[0]) : 0;
+  const int c_smem = cnt_g[1] ? smem_nj_cluster(nmax_g[1]) : 0;
   std::vector<char> descs(desc * nj);
   std::vector<nwg_join*> jptr(nj);
   std::vector<unsigned long long*> sptr(nj);
-  int next_idx[2] = {0, cnt_g[0]};
+  int next_idx[3] = {0, cnt_g[0], cnt_g[0] + cnt_g[1]};
   for (int k = 0; k < nj; ++k) {
     ServeJob* J = S.batch[k];
     J->desc_idx = (size_t)next_idx[form[k]]++;
@@ -345,13 +345,16 @@ int Server::launch_batch(Slot& S) {
   }
   if ((rc = c.cuda(cudaMemcpyAsync(S.h_D.p, S.D.p, sizeof(float) * total_D, cudaMemcpyDeviceToHost, st), "serve")))
     return rc;
-  // join loops, one cluster per job, one launch per form (jobs with 256
-  // sequences or more take the device's largest cluster)
-  if (cnt_g[0] && (rc = c.cuda(launch_nj_smem(S.njdesc.p, cnt_g[0], nmax_g[0], c_smem, st), "serve nj launch")))
+  // join loops, one CTA or one cluster per job, one launch per form (jobs
+  // with 256 sequences or more take the device's largest cluster)
+  if (cnt_g[0] && (rc = c.cuda(launch_nj_cta(S.njdesc.p, cnt_g[0], nmax_g[0], st), "serve nj launch"))) return rc;
+  if (cnt_g[1] && (rc = c.cuda(launch_nj_smem((const char*)S.njdesc.p + desc * cnt_g[0], cnt_g[1], nmax_g[1], c_smem,
+                                              st),
+                               "serve nj launch")))
     return rc;
-  if (cnt_g[1]) {
-    const int csize = nmax_g[1] >= kNJWideN ? nj_cluster_size() : kNJClusterServe;
-    if ((rc = c.cuda(launch_nj_cluster((const char*)S.njdesc.p + desc * cnt_g[0], cnt_g[1], csize, st),
+  if (cnt_g[2]) {
+    const int csize = nmax_g[2] >= kNJWideN ? nj_cluster_size() : kNJClusterServe;
+    if ((rc = c.cuda(launch_nj_cluster((const char*)S.njdesc.p + desc * (cnt_g[0] + cnt_g[1]), cnt_g[2], csize, st),
                      "serve nj launch")))
       return rc;
   }

@@ -105,8 +105,10 @@ print('ok')
 
 # the three launch forms, selected by the size thresholds
 _FORMS = {
-    "smem": {},                                                        # matrix in the cluster's shared memory
-    "cluster": {"NWG_NJ_SMEM_MAX_N": "0", "NWG_NJ_CLUSTER_MAX_N": "100000"},   # one cluster over L2
+    "cta": {},                                                          # defaults: one CTA up to 160 taxa
+    "smem": {"NWG_NJ_CTA_MAX_N": "0"},                                  # matrix in a cluster's shared memory
+    "cluster": {"NWG_NJ_CTA_MAX_N": "0", "NWG_NJ_SMEM_MAX_N": "0",
+                "NWG_NJ_CLUSTER_MAX_N": "100000"},                      # one cluster over L2
     "full_gpu": {"NWG_NJ_CLUSTER_MAX_N": "0"},                          # cooperative launch over every SM
 }
 
@@ -125,11 +127,12 @@ def test_every_nj_form_matches_oracle(path):
     assert r.returncode == 0 and r.stdout.strip().endswith("ok"), r.stdout + r.stderr
 
 
-@pytest.mark.parametrize("path", ["cluster", "full_gpu"])
+@pytest.mark.parametrize("path", ["smem", "cluster", "full_gpu"])
 @pytest.mark.parametrize("case", ["cfg0", "nj300", "nj1200"])
 def test_every_nj_form_matches_reference_tree(case, path):
     # the golden reference trees through the forms the default sizes do not
-    # pick (the default run covers the shared-memory form up to 768 taxa)
+    # pick (the default run covers one CTA up to 160 taxa and a cluster's
+    # shared memory up to 768)
     import subprocess
     import sys
     code = (
