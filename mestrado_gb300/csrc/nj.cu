@@ -1251,7 +1251,21 @@ __global__ void __launch_bounds__(kCtaThreads, 1) nj_cta_kernel(const NJJob* job
         const float* row = rows + (size_t)r * ldl;
         float m1 = FLT_MAX, m2 = FLT_MAX, mag = 0.f;
         int c1 = -1;
-        for (int c = r + 1; c < n; ++c) pass_elem(row[c], Tf[c], c, tr, nm2f, m1, m2, c1, mag);
+        // columns r+1 .. up to the next multiple of 4 one by one, then 16-byte
+        // vectors (rows padded to ldl floats, the padding's row sums NaN)
+        const int v0 = (r + 4) >> 2;
+        for (int c = r + 1; c < 4 * v0 && c < n; ++c) pass_elem(row[c], Tf[c], c, tr, nm2f, m1, m2, c1, mag);
+        const float4* row4 = reinterpret_cast<const float4*>(row);
+        const float4* Tf4 = reinterpret_cast<const float4*>(Tf);
+#pragma unroll 2
+        for (int v = v0; v < (ldl >> 2); ++v) {
+          const float4 d = row4[v];
+          const float4 tc = Tf4[v];
+          pass_elem(d.x, tc.x, 4 * v, tr, nm2f, m1, m2, c1, mag);
+          pass_elem(d.y, tc.y, 4 * v + 1, tr, nm2f, m1, m2, c1, mag);
+          pass_elem(d.z, tc.z, 4 * v + 2, tr, nm2f, m1, m2, c1, mag);
+          pass_elem(d.w, tc.w, 4 * v + 3, tr, nm2f, m1, m2, c1, mag);
+        }
         grm[r] = ford(m1);
         grc[r] = make_int4(ford(m2), c1, __float_as_int(c1 >= 0 ? row[c1] : 0.f), 0);
         qmin = fminf(qmin, m1);
