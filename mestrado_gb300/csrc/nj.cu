@@ -45,10 +45,14 @@
 // rounding.  All floating-point operations use the _rn intrinsics in the
 // reference's evaluation order (no contraction).
 //
-// A team of CTAs runs a job's join loop: the whole GPU (one cooperative
-// launch per rebuild segment, more than 2048 taxa; compacted to the live
-// slots, in slot order, between segments) or one thread-block cluster (up to
-// 2048 taxa, and every serving job, one cluster per job).
+// Four launch forms run a job's whole join loop (several jobs per launch in
+// the serving loop):
+//  * one CTA with the job in its shared memory (up to 160 taxa);
+//  * one thread-block cluster with the matrix in its distributed shared
+//    memory (up to 768 taxa);
+//  * one cluster with the matrix in global memory (up to 2048 taxa);
+//  * the whole GPU, one cooperative launch per segment between compactions
+//    (compacted to the live slots, in slot order), above that.
 #include <algorithm>
 #include <cfloat>
 #include <climits>
