@@ -69,6 +69,23 @@ def test_overflow_guard_routes_to_int32(ctx):
     assert np.array_equal(D, O.score_all(long, threads=os.cpu_count()))
 
 
+def test_long_sequences_every_mode(ctx):
+    # far above the lengths of any workload: many bands per pair, int32 lanes
+    seqs = _rand_set(11, 4, 1, 3, alphabet=b"ARNDCQEGHILKMFPSTWYV")
+    seqs += _rand_set(12, 1, 16384, 16384) + _rand_set(13, 1, 9001, 9001) + _rand_set(14, 1, 4001, 4001)
+    Dref = O.score_all(seqs, threads=os.cpu_count())
+    for mode in MODES:
+        assert np.array_equal(ctx.score_all(seqs, mode=mode), Dref), mode
+
+
+def test_thousands_of_tiny_sequences_every_mode(ctx):
+    # 4.5 million pairs of 1-4 residues: the bucketing and the pair bookkeeping, not the DP
+    seqs = _rand_set(15, 3000, 1, 4, alphabet=b"ARNDCQEGHILKMFPSTWYVBZX*")
+    Dref = O.score_all(seqs, threads=os.cpu_count())
+    for mode in MODES:
+        assert np.array_equal(ctx.score_all(seqs, mode=mode), Dref), mode
+
+
 def test_cached_plan_and_graph_replay_with_new_residues(ctx):
     # same lengths, different residues: the cached plan and graph are reused
     a = _rand_set(31, 50, 20, 700)
