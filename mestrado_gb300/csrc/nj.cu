@@ -242,6 +242,7 @@ struct GridNJ {
   long long* jsum;      // [2 * grid]: per CTA integer sum and sum of magnitudes (units of 2^jexp)
   int* jexp;            // [2 * grid]: per CTA lowest and highest exponent of its values
   KCand* cand;          // the candidate list of the fallback scan
+  KCand* cbest;         // [grid]: per CTA its first candidate of the fallback scan
 };
 
 constexpr long long kBarrierSpinCycles = 4000000000ll;   // about two seconds: no phase takes a millisecond
@@ -501,6 +502,65 @@ __device__ PickOut pick_keys(int nc, Load&& load) {   // load(k) has k1, k2, a, 
   return r;
 }
 
+// More candidates than the list holds (wide exact ties, e.g. hundreds of
+// identical sequences): every CTA keeps the first of its own candidates in the
+// pick's order, the winner is the first of those, and a second scan counts the
+// ties and ambiguous pairs against it with pick_keys' rule.
+
+__device__ __forceinline__ KCand kc_none() { return KCand{LLONG_MAX, LLONG_MAX, INT_MAX, -1}; }
+
+// x before y in the pick's order: smaller q1 key, then larger b, then larger a.
+__device__ __forceinline__ bool kc_first(const KCand& x, const KCand& y) {
+  return x.k1 < y.k1 || (x.k1 == y.k1 && (x.b > y.b || (x.b == y.b && x.a > y.a)));
+}
+
+__device__ __forceinline__ KCand ld_kcand(const KCand* p) {   // written by other CTAs: from L2
+  return KCand{__ldcg(&p->k1), __ldcg(&p->k2), __ldcg(&p->a), __ldcg(&p->b)};
+}
+
+__device__ __forceinline__ KCand warp_first(KCand x) {
+  for (int o = 16; o > 0; o >>= 1) {
+    KCand y;
+    y.k1 = __shfl_xor_sync(0xffffffffu, x.k1, o);
+    y.k2 = __shfl_xor_sync(0xffffffffu, x.k2, o);
+    y.a = __shfl_xor_sync(0xffffffffu, x.a, o);
+    y.b = __shfl_xor_sync(0xffffffffu, x.b, o);
+    if (kc_first(y, x)) x = y;
+  }
+  return x;
+}
+
+// The CTA's first candidate, valid in warp 0 (sw: 32 entries of shared memory,
+// not reused before the next CTA barrier).
+__device__ KCand cta_first(KCand x, KCand* sw) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = ((int)blockDim.x + 31) >> 5;
+  x = warp_first(x);
+  if (lane == 0) sw[warp] = x;
+  __syncthreads();
+  if (warp == 0) x = warp_first(lane < nw ? sw[lane] : kc_none());
+  return x;
+}
+
+// pick_keys' tie and ambiguity rule for candidate c against the winner w.
+__device__ __forceinline__ void count_vs(const KCand& c, const KCand& w, unsigned& ties, unsigned& amb) {
+  if (min(c.k1, c.k2) > max(w.k1, w.k2)) return;
+  if (c.a == w.a && c.b == w.b) ++ties;
+  else if (w.k1 == w.k2 && c.k1 == c.k2 && c.k1 == w.k1) ++ties;
+  else ++amb;
+}
+
+// The CTA's counts into cnt[0] (ties) and cnt[1] (ambiguous pairs).
+__device__ __forceinline__ void add_counts(unsigned ties, unsigned amb, int* cnt) {
+  for (int o = 16; o > 0; o >>= 1) {
+    ties += __shfl_xor_sync(0xffffffffu, ties, o);
+    amb += __shfl_xor_sync(0xffffffffu, amb, o);
+  }
+  if ((threadIdx.x & 31) == 0 && (ties | amb)) {
+    atomicAdd(&cnt[0], (int)ties);
+    atomicAdd(&cnt[1], (int)amb);
+  }
+}
+
 // K.  Returns 1 when the winner is in *win, 0 when the fallback scan is
 // needed (the same in every CTA).
 __device__ int grid_pick_direct(const NJDev& s, const GridNJ& g, Team tm, double nm2, float nm2f, int watermark, GCand* win,
@@ -590,9 +650,11 @@ __device__ int grid_pick_direct(const NJDev& s, const GridNJ& g, Team tm, double
   return s_ok;
 }
 
-// K, fallback: this CTA's slice of the columns of every row within the
-// threshold into the candidate list.
-__device__ void grid_cand(const NJDev& s, const GridNJ& g, Team tm, float nm2f, double nm2, int watermark, float thr) {
+// K, fallback: visit(candidate) for this CTA's slice of the columns of every
+// row within the threshold (the same pairs on every call of one join).
+template <class Visit>
+__device__ void grid_cand_scan(const NJDev& s, const GridNJ& g, Team tm, float nm2f, double nm2, int watermark,
+                               float thr, Visit&& visit) {
   constexpr int kRows = 512;
   __shared__ int rows[kRows];
   __shared__ int nrows;
@@ -625,13 +687,33 @@ __device__ void grid_cand(const NJDev& s, const GridNJ& g, Team tm, float nm2f, 
       if (uc < 0) continue;
       const float q = __fsub_rn(__fsub_rn(__fmul_rn(d, nm2f), tr), tcf);
       if (q > thr) continue;
-      const int idx = atomicAdd(&s.g32[2], 1);
-      if (idx < s.cand_cap) {
-        const GCand cd = make_cand(r, c, ur, uc, Tr, Tc, d, nm2, watermark);
-        g.cand[idx] = KCand{cd.k1, cd.k2, cd.a, cd.b};
-      }
+      const GCand cd = make_cand(r, c, ur, uc, Tr, Tc, d, nm2, watermark);
+      visit(KCand{cd.k1, cd.k2, cd.a, cd.b});
     }
   }
+}
+
+// The scan into the candidate list (s.g32[2] counts every candidate, also
+// beyond the capacity); the CTA's first candidate goes to g.cbest[rank].
+__device__ void grid_cand(const NJDev& s, const GridNJ& g, Team tm, float nm2f, double nm2, int watermark, float thr) {
+  __shared__ KCand sw[32];
+  KCand first = kc_none();
+  grid_cand_scan(s, g, tm, nm2f, nm2, watermark, thr, [&](const KCand& c) {
+    const int idx = atomicAdd(&s.g32[2], 1);
+    if (idx < s.cand_cap) g.cand[idx] = c;
+    if (kc_first(c, first)) first = c;
+  });
+  first = cta_first(first, sw);
+  if (threadIdx.x == 0) g.cbest[tm.rank] = first;
+}
+
+// The overflow's second scan: ties and ambiguous pairs against the winner w
+// into s.g32[0] and s.g32[1].
+__device__ void grid_cand_count(const NJDev& s, const GridNJ& g, Team tm, float nm2f, double nm2, int watermark,
+                                float thr, const KCand& w) {
+  unsigned ties = 0, amb = 0;
+  grid_cand_scan(s, g, tm, nm2f, nm2, watermark, thr, [&](const KCand& c) { count_vs(c, w, ties, amb); });
+  add_counts(ties, amb, s.g32);
 }
 
 // J: this CTA's share of the slots (SpeciesBlock.cpp:787-841: tmp = ((Dik +
@@ -837,7 +919,7 @@ __device__ bool grid_join_apply(const NJDev& s, const GridNJ& g, Team tm, const 
       s.slot[j] = -1;
       s.slot[i] = -1;
       s.slot[next] = si;
-      s.g32[2] = 0;   // every CTA took its pick before the barrier
+      s.g32[0] = s.g32[1] = s.g32[2] = 0;   // every CTA took its pick before the barrier
       record_pick(s, pk);
     }
   }
@@ -859,24 +941,42 @@ __device__ bool team_join(const NJDev& s, const GridNJ& g, Team tm, int step, in
   if (!grid_pick_direct(s, g, tm, nm2, nm2f, watermark, &swin, &spick, &sthr)) {
     grid_cand(s, g, tm, nm2f, nm2, watermark, sthr);
     if (!team_sync<CL>(g, target)) return false;
-    if (threadIdx.x < 32) {
-      const int ncount = s.g32[2];
-      const int nc = min(ncount, s.cand_cap);
-      PickOut r = pick_keys(nc, [&](int k) { return g.cand[k]; });
-      r.error = r.error || ncount > s.cand_cap;
-      if (threadIdx.x == 0) {
-        spick = r;
-        if (!r.error) {
-          // the winner's pair again, as the scan read it (row = the smaller slot)
-          const KCand w = g.cand[r.idx];
-          const int sa = s.slot[w.a], sb = s.slot[w.b];
-          const int r0 = min(sa, sb), c0 = max(sa, sb);
-          swin = make_cand(r0, c0, s.node[r0], s.node[c0], s.T[r0], s.T[c0], s.D[(size_t)r0 * s.ld + c0], nm2,
-                           watermark);
+    // the winner's pair again, as the scan read it (row = the smaller slot)
+    auto rederive = [&](const KCand& w) {
+      const int sa = s.slot[w.a], sb = s.slot[w.b];
+      const int r0 = min(sa, sb), c0 = max(sa, sb);
+      swin = make_cand(r0, c0, s.node[r0], s.node[c0], s.T[r0], s.T[c0], s.D[(size_t)r0 * s.ld + c0], nm2,
+                       watermark);
+    };
+    const int ncount = *(volatile int*)&s.g32[2];   // the same in every CTA
+    if (ncount <= s.cand_cap) {
+      if (threadIdx.x < 32) {
+        const PickOut r = pick_keys(ncount, [&](int k) { return g.cand[k]; });
+        if (threadIdx.x == 0) {
+          spick = r;
+          if (!r.error) rederive(g.cand[r.idx]);
         }
       }
+      __syncthreads();
+    } else {
+      __shared__ KCand sfirst;
+      if (threadIdx.x < 32) {
+        const PickOut r = pick_keys(tm.size, [&](int k) { return ld_kcand(&g.cbest[k]); });
+        if (threadIdx.x == 0) sfirst = r.error ? kc_none() : ld_kcand(&g.cbest[r.idx]);
+      }
+      __syncthreads();
+      const KCand w = sfirst;
+      grid_cand_count(s, g, tm, nm2f, nm2, watermark, sthr, w);
+      if (!team_sync<CL>(g, target)) return false;
+      if (threadIdx.x == 0) {
+        spick.idx = 0;
+        spick.ties = (unsigned)__ldcg(&s.g32[0]);
+        spick.amb = (unsigned)__ldcg(&s.g32[1]);
+        spick.error = w.b < 0;
+        if (!spick.error) rederive(w);
+      }
+      __syncthreads();
     }
-    __syncthreads();
   }
   if (spick.error) {
     if (tm.rank == 0 && threadIdx.x == 0) record_pick(s, spick);
@@ -901,7 +1001,7 @@ __global__ void __launch_bounds__(1024, 1) nj_grid_kernel(NJDev s, GridNJ g, int
   if (*(volatile int*)g.abort) return;   // an earlier segment gave up: every CTA leaves
   for (int p = (int)(blockIdx.x * blockDim.x + threadIdx.x); p < s.n0; p += (int)(gridDim.x * blockDim.x))
     g.grmin[p] = 0x7F7FFFFF;   // ordered int of FLT_MAX
-  if (blockIdx.x == 0 && threadIdx.x == 0) s.g32[2] = 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) s.g32[0] = s.g32[1] = s.g32[2] = 0;
   if (!grid_barrier(g, target)) return;
   int* act = s.act;
   int* act2 = g.act2;
@@ -1076,7 +1176,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_cluster_
   for (int k = n + t0; k < s.ld; k += tstride) s.Tf[k] = __int_as_float(0x7FC00000);   // padding: NaN
   if (tm.rank == 0 && threadIdx.x == 0) {
     *s.na = n;
-    s.g32[2] = 0;
+    s.g32[0] = s.g32[1] = s.g32[2] = 0;
     s.stats[0] = s.stats[1] = s.stats[2] = s.stats[3] = s.stats[4] = 0;
   }
   cooperative_groups::this_cluster().sync();
@@ -1647,7 +1747,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
   }
   for (int k = tid; k < n; k += nth) m.grm[k] = 0x7F7FFFFF;
   if (rank == 0 && tid == 0) {
-    s.g32[2] = 0;
+    s.g32[0] = s.g32[1] = s.g32[2] = 0;
     s.stats[0] = s.stats[1] = s.stats[2] = s.stats[3] = s.stats[4] = 0;
   }
   cg::this_cluster().sync();   // every CTA's row-sum array is NaN before any broadcast lands
@@ -1876,48 +1976,79 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
     }
     __syncthreads();
     if (!s_ok) {
-      // fallback: each CTA scans its own rows within the threshold into the list
-      for (int l = 0; l < m.lr; ++l) {
-        const int r = m.slot_of(rank, l);
-        if (r < 0 || m.grm[r] > othr) continue;
-        const int ur = m.node[r];
-        const float tr = m.Tf[r];
-        const double Tr = m.Tloc[l];
-        const float* row = m.rows + (size_t)l * m.ldl;
-        for (int c = r + 1 + tid; c < n; c += nth) {
-          const int uc = m.node[c];
-          if (uc < 0) continue;
-          const float d = row[c];
-          const float q = __fsub_rn(__fsub_rn(__fmul_rn(d, nm2f), tr), m.Tf[c]);
-          if (q > thr) continue;
-          const double Tc = m.at(m.Tloc, m.owner(c))[m.local_row(c)];
-          const int idx = atomicAdd(&s.g32[2], 1);
-          if (idx < s.cand_cap) {
+      // fallback: each CTA scans its own rows within the threshold into the
+      // list (as grid_cand does; beyond the list's capacity the winner comes
+      // from the CTAs' first candidates and a second scan counts against it)
+      auto scan = [&](auto&& visit) {
+        for (int l = 0; l < m.lr; ++l) {
+          const int r = m.slot_of(rank, l);
+          if (r < 0 || m.grm[r] > othr) continue;
+          const int ur = m.node[r];
+          const float tr = m.Tf[r];
+          const double Tr = m.Tloc[l];
+          const float* row = m.rows + (size_t)l * m.ldl;
+          for (int c = r + 1 + tid; c < n; c += nth) {
+            const int uc = m.node[c];
+            if (uc < 0) continue;
+            const float d = row[c];
+            const float q = __fsub_rn(__fsub_rn(__fmul_rn(d, nm2f), tr), m.Tf[c]);
+            if (q > thr) continue;
+            const double Tc = m.at(m.Tloc, m.owner(c))[m.local_row(c)];
             const GCand cd = make_cand(r, c, ur, uc, Tr, Tc, d, nm2, watermark);
-            g.cand[idx] = KCand{cd.k1, cd.k2, cd.a, cd.b};
+            visit(KCand{cd.k1, cd.k2, cd.a, cd.b});
           }
         }
-      }
+      };
+      // the winner's pair again, as the scan read it (row = the smaller slot)
+      auto rederive = [&](const KCand& w) {
+        const int sa = m.slot[w.a], sb = m.slot[w.b];
+        const int r0 = min(sa, sb), c0 = max(sa, sb);
+        const int q = m.owner(r0), l = m.local_row(r0);
+        const double Tr = m.at(m.Tloc, q)[l], Tc = m.at(m.Tloc, m.owner(c0))[m.local_row(c0)];
+        const float d = m.at(m.rows, q)[(size_t)l * m.ldl + c0];
+        swin = make_cand(r0, c0, m.node[r0], m.node[c0], Tr, Tc, d, nm2, watermark);
+      };
+      __shared__ KCand skw[32];
+      __shared__ KCand sfirst;
+      KCand first = kc_none();
+      scan([&](const KCand& c) {
+        const int idx = atomicAdd(&s.g32[2], 1);
+        if (idx < s.cand_cap) g.cand[idx] = c;
+        if (kc_first(c, first)) first = c;
+      });
+      first = cta_first(first, skw);
+      if (tid == 0) g.cbest[rank] = first;
       cg::this_cluster().sync();
-      if (warp == 0) {
-        const int ncount = *(volatile int*)&s.g32[2];
-        const int nc = min(ncount, s.cand_cap);
-        PickOut pr = pick_keys(nc, [&](int k) { return g.cand[k]; });
-        pr.error = pr.error || ncount > s.cand_cap;
-        if (lane == 0) {
-          spick = pr;
-          if (!pr.error) {
-            const KCand w = g.cand[pr.idx];
-            const int sa = m.slot[w.a], sb = m.slot[w.b];
-            const int r0 = min(sa, sb), c0 = max(sa, sb);
-            const int q = m.owner(r0), l = m.local_row(r0);
-            const double Tr = m.at(m.Tloc, q)[l], Tc = m.at(m.Tloc, m.owner(c0))[m.local_row(c0)];
-            const float d = m.at(m.rows, q)[(size_t)l * m.ldl + c0];
-            swin = make_cand(r0, c0, m.node[r0], m.node[c0], Tr, Tc, d, nm2, watermark);
+      const int ncount = *(volatile int*)&s.g32[2];   // the same in every CTA
+      if (ncount <= s.cand_cap) {
+        if (warp == 0) {
+          const PickOut pr = pick_keys(ncount, [&](int k) { return g.cand[k]; });
+          if (lane == 0) {
+            spick = pr;
+            if (!pr.error) rederive(g.cand[pr.idx]);
           }
         }
+        __syncthreads();
+      } else {
+        if (warp == 0) {
+          const PickOut pr = pick_keys(C, [&](int k) { return ld_kcand(&g.cbest[k]); });
+          if (lane == 0) sfirst = pr.error ? kc_none() : ld_kcand(&g.cbest[pr.idx]);
+        }
+        __syncthreads();
+        const KCand w = sfirst;
+        unsigned ties = 0, amb = 0;
+        scan([&](const KCand& c) { count_vs(c, w, ties, amb); });
+        add_counts(ties, amb, s.g32);
+        cg::this_cluster().sync();
+        if (tid == 0) {
+          spick.idx = 0;
+          spick.ties = (unsigned)__ldcg(&s.g32[0]);
+          spick.amb = (unsigned)__ldcg(&s.g32[1]);
+          spick.error = w.b < 0;
+          if (!spick.error) rederive(w);
+        }
+        __syncthreads();
       }
-      __syncthreads();
       if (spick.error) {   // the same in every CTA
         if (rank == 0 && tid == 0) record_pick(s, spick);
         failed = true;
@@ -2033,7 +2164,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
       J.q = w.q1;
       J.ti = w.ta;
       J.tj = w.tb;
-      s.g32[2] = 0;
+      s.g32[0] = s.g32[1] = s.g32[2] = 0;
       record_pick(s, spick);
     }
     {
@@ -2072,10 +2203,10 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
 struct NJState {
   DevBuf D, jobws, desc;
   // large-n path: row sums, maps, compaction buffers, candidates, grid partials and barrier words
-  DevBuf T, Tf, slot, node, act, na, g32, stats, joins, cand, tv, grmin, grec, tsnap;
+  DevBuf T, Tf, slot, node, act, na, g32, stats, joins, cand, cbest, tv, grmin, grec, tsnap;
   DevBuf D2, T2, Tf2, node2, map, act2, part, jsum, jexp, gbar;
   ~NJState() {
-    for (DevBuf* b : {&D, &jobws, &desc, &T, &Tf, &slot, &node, &act, &na, &g32, &stats, &joins, &cand, &tv, &grmin,
+    for (DevBuf* b : {&D, &jobws, &desc, &T, &Tf, &slot, &node, &act, &na, &g32, &stats, &joins, &cand, &cbest, &tv, &grmin,
                       &grec, &tsnap, &D2, &T2, &Tf2, &node2, &map, &act2, &part, &jsum, &jexp, &gbar})
       b->release();
   }
@@ -2149,6 +2280,7 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
         (rc = S.act.ensure(sizeof(int) * (n + 1))) || (rc = S.na.ensure(sizeof(int))) ||
         (rc = S.g32.ensure(sizeof(int) * 4)) || (rc = S.stats.ensure(sizeof(unsigned long long) * 5)) ||
         (rc = S.joins.ensure(sizeof(nwg_join) * (n - 1))) || (rc = S.cand.ensure(sizeof(KCand) * kCandCap)) ||
+        (rc = S.cbest.ensure(sizeof(KCand) * grid)) ||
         (rc = S.tv.ensure(sizeof(float) * n)) || (rc = S.grmin.ensure(sizeof(int) * n)) ||
         (rc = S.grec.ensure(sizeof(int4) * n)) || (rc = S.tsnap.ensure(sizeof(double) * n)) || (rc = S.D2.ensure(sizeof(float) * (size_t)n * ldd)) ||
         (rc = S.T2.ensure(sizeof(double) * n)) || (rc = S.Tf2.ensure(sizeof(float) * ldd)) ||
@@ -2201,6 +2333,7 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
     g.grmin = (int*)S.grmin.p;
     g.grec = (int4*)S.grec.p;
     g.tsnap = (double*)S.tsnap.p;
+    g.cbest = (KCand*)S.cbest.p;
     g.tv = (float*)S.tv.p;
     g.part = (float*)S.part.p;
     g.jsum = (long long*)S.jsum.p;
@@ -2360,6 +2493,7 @@ static size_t job_layout(int n, int ld, char* base, NJJob* J) {
   char* jsum = take(sizeof(long long) * 2 * kC);
   char* jexp = take(sizeof(int) * 2 * kC);
   char* cand = take(sizeof(KCand) * cap);
+  char* cbest = take(sizeof(KCand) * kC);
   char* joins = take(sizeof(nwg_join) * (n > 1 ? n - 1 : 1));
   if (J) {
     J->s.T = (double*)T;
@@ -2383,6 +2517,7 @@ static size_t job_layout(int n, int ld, char* base, NJJob* J) {
     J->g.jsum = (long long*)jsum;
     J->g.jexp = (int*)jexp;
     J->g.cand = (KCand*)cand;
+    J->g.cbest = (KCand*)cbest;
     J->n = n;
   }
   return off;

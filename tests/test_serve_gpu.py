@@ -93,6 +93,22 @@ def test_serving_matches_oracle():
         assert info["nj_rebuilds"] == ost["rebuilds"]
 
 
+def test_serving_wide_exact_ties():
+    # jobs whose joins tie exactly on more pairs than the candidate list holds
+    # (420 copies of one sequence; three sequences 140 times each)
+    S = synth.family(4, 60, ps=0.02, pi=0.0, seed=41)
+    jobs = [[S[0]] * 420, [S[k] for k in (1, 2, 3) for _ in range(140)]]
+    with Server(hbm_budget=4 << 30, max_batch_jobs=4) as srv:
+        res = _run(srv, jobs)
+    for S, (D, J, info) in zip(jobs, res):
+        assert info["status"] == 0
+        assert np.array_equal(D, O.score_all(S).astype(np.float32))
+        oj, ost = O.nj(D)
+        _same_joins(J, oj)
+        assert info["nj_ambiguous_steps"] == ost["ambiguous_steps"]
+        assert info["nj_tie_steps"] == ost["tie_steps"]
+
+
 def test_serving_admission_by_footprint(ctx):
     # a budget that holds about one 300-sequence job at a time: batches stay
     # small, results do not change
