@@ -69,7 +69,7 @@ namespace nwg {
 namespace {
 
 constexpr int kNJMaxN = 8192;
-constexpr int kCandCap = 1 << 16;      // candidate list capacity per join
+constexpr int kCandCap = 1 << 14;      // candidate list capacity per join (every pair of a one-CTA job)
 
 struct NJDev {
   float* D;            // n0 x ld, slots
@@ -139,7 +139,8 @@ __device__ __forceinline__ bool sum_is_exact(double absum, int lowexp) {
 
 // Sequential row sums (buildGblRowSums): one warp per active row; the lanes'
 // any-order sum is used when it is provably exact, else lane 0 sums in order.
-__global__ void rowsum_kernel(NJDev s) {
+__global__ void rowsum_kernel(NJDev s, const int* abort) {
+  if (*(volatile const int*)abort) return;   // a segment gave up: the lists were never written
   const int na = *s.na;
   const int lane = threadIdx.x & 31;
   const int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -502,10 +503,13 @@ __device__ PickOut pick_keys(int nc, Load&& load) {   // load(k) has k1, k2, a, 
   return r;
 }
 
-// More candidates than the list holds (wide exact ties, e.g. hundreds of
-// identical sequences): every CTA keeps the first of its own candidates in the
-// pick's order, the winner is the first of those, and a second scan counts the
-// ties and ambiguous pairs against it with pick_keys' rule.
+// Long candidate lists (wide exact ties, e.g. hundreds of identical
+// sequences, whose pairs all tie): above kListPickMax candidates one warp's
+// pick over the list would be slow, and the list may overflow.  Instead every
+// CTA keeps the first of its own candidates in the pick's order, the winner is
+// the first of those, and a second scan counts the ties and ambiguous pairs
+// against it with pick_keys' rule.
+constexpr int kListPickMax = 2048;
 
 __device__ __forceinline__ KCand kc_none() { return KCand{LLONG_MAX, LLONG_MAX, INT_MAX, -1}; }
 
@@ -650,8 +654,14 @@ __device__ int grid_pick_direct(const NJDev& s, const GridNJ& g, Team tm, double
   return s_ok;
 }
 
-// K, fallback: visit(candidate) for this CTA's slice of the columns of every
-// row within the threshold (the same pairs on every call of one join).
+// K, fallback: visit(pred, candidate) for this CTA's share of the pairs of
+// every row within the threshold, called by whole warps together (pred is
+// false on lanes without a candidate in that step); the same pairs on every
+// call of one join.  Up to kSplitRows rows, the team's warps split each row's
+// columns; more rows (wide ties), one warp per row, warps numbered across the
+// team, lanes over the columns.
+constexpr int kSplitRows = 16;
+
 template <class Visit>
 __device__ void grid_cand_scan(const NJDev& s, const GridNJ& g, Team tm, float nm2f, double nm2, int watermark,
                                float thr, Visit&& visit) {
@@ -671,48 +681,80 @@ __device__ void grid_cand_scan(const NJDev& s, const GridNJ& g, Team tm, float n
   __syncthreads();
   const bool all = nrows > kRows;   // more near-minimal rows than the list holds: every row
   const int nr = all ? n0 : nrows;
-  const int cstride = tm.size * (int)blockDim.x;
-  for (int t = 0; t < nr; ++t) {
-    const int r = all ? t : rows[t];
+  const int lane = threadIdx.x & 31;
+  const int wpc = (int)blockDim.x >> 5;
+  const int gw = tm.rank * wpc + ((int)threadIdx.x >> 5), nw = tm.size * wpc;
+  // columns c0 + lane, c0 + cstep + lane, ... of row r (c0 and cstep the same in the warp)
+  auto scan_row = [&](int r, int c0, int cstep) {
     const int ur = s.node[r];
+    if (ur < 0 || g.grmin[r] > othr) return;
     const float tr = s.Tf[r];
     const double Tr = s.T[r];
-    if (ur < 0 || g.grmin[r] > othr) continue;
     const float* row = s.D + (size_t)r * s.ld;
-    for (int c = r + 1 + (int)(tm.rank * blockDim.x + threadIdx.x); c < n0; c += cstride) {
-      const int uc = s.node[c];
-      const float d = row[c];
-      const float tcf = s.Tf[c];
-      const double Tc = s.T[c];
-      if (uc < 0) continue;
-      const float q = __fsub_rn(__fsub_rn(__fmul_rn(d, nm2f), tr), tcf);
-      if (q > thr) continue;
-      const GCand cd = make_cand(r, c, ur, uc, Tr, Tc, d, nm2, watermark);
-      visit(KCand{cd.k1, cd.k2, cd.a, cd.b});
+    for (int cb = c0; cb < n0; cb += cstep) {
+      const int c = cb + lane;
+      bool pred = false;
+      KCand kc = kc_none();
+      if (c < n0) {
+        const int uc = s.node[c];
+        const float d = row[c];
+        const float q = __fsub_rn(__fsub_rn(__fmul_rn(d, nm2f), tr), s.Tf[c]);
+        if (uc >= 0 && q <= thr) {
+          const GCand cd = make_cand(r, c, ur, uc, Tr, s.T[c], d, nm2, watermark);
+          kc = KCand{cd.k1, cd.k2, cd.a, cd.b};
+          pred = true;
+        }
+      }
+      visit(pred, kc);
     }
+  };
+  if (nr <= kSplitRows) {
+    for (int t = 0; t < nr; ++t) {   // every CTA's list holds the same rows, in its own order
+      const int r = all ? t : rows[t];
+      scan_row(r, r + 1 + 32 * gw, 32 * nw);
+    }
+  } else {
+    // rows by slot (an order the same in every CTA); scan_row skips the others
+    for (int r = gw; r < n0; r += nw) scan_row(r, r + 1, 32);
   }
 }
 
-// The scan into the candidate list (s.g32[2] counts every candidate, also
-// beyond the capacity); the CTA's first candidate goes to g.cbest[rank].
-__device__ void grid_cand(const NJDev& s, const GridNJ& g, Team tm, float nm2f, double nm2, int watermark, float thr) {
-  __shared__ KCand sw[32];
-  KCand first = kc_none();
-  grid_cand_scan(s, g, tm, nm2f, nm2, watermark, thr, [&](const KCand& c) {
-    const int idx = atomicAdd(&s.g32[2], 1);
-    if (idx < s.cand_cap) g.cand[idx] = c;
-    if (kc_first(c, first)) first = c;
-  });
-  first = cta_first(first, sw);
-  if (threadIdx.x == 0) g.cbest[tm.rank] = first;
+// A warp's candidates of one scan step into the list, one atomic per warp.
+// s.g32[2] ends at the number of candidates when that is at most
+// kListPickMax, else above kListPickMax: a warp that saw the count pass it
+// stops counting (full, the same in the warp).
+__device__ __forceinline__ void list_push(const NJDev& s, const GridNJ& g, bool pred, const KCand& c, bool& full) {
+  const unsigned bal = __ballot_sync(0xffffffffu, pred);
+  if (bal == 0 || full) return;
+  const int lane = threadIdx.x & 31;
+  int base = 0;
+  if (lane == 0) base = atomicAdd(&s.g32[2], __popc(bal));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  const int idx = base + __popc(bal & ((1u << lane) - 1u));
+  if (pred && idx < s.cand_cap) g.cand[idx] = c;
+  full = base + __popc(bal) > kListPickMax;
 }
 
-// The overflow's second scan: ties and ambiguous pairs against the winner w
-// into s.g32[0] and s.g32[1].
+// The scan into the candidate list; returns this thread's first candidate
+// (reduced over the CTA only when the list is not used).
+__device__ KCand grid_cand(const NJDev& s, const GridNJ& g, Team tm, float nm2f, double nm2, int watermark, float thr) {
+  KCand first = kc_none();
+  bool full = false;
+  grid_cand_scan(s, g, tm, nm2f, nm2, watermark, thr, [&](bool pred, const KCand& c) {
+    list_push(s, g, pred, c, full);
+    if (pred && kc_first(c, first)) first = c;
+  });
+  return first;
+}
+
+// The second scan of a long list: ties and ambiguous pairs against the winner
+// w into s.g32[0] and s.g32[1].
 __device__ void grid_cand_count(const NJDev& s, const GridNJ& g, Team tm, float nm2f, double nm2, int watermark,
                                 float thr, const KCand& w) {
   unsigned ties = 0, amb = 0;
-  grid_cand_scan(s, g, tm, nm2f, nm2, watermark, thr, [&](const KCand& c) { count_vs(c, w, ties, amb); });
+  grid_cand_scan(s, g, tm, nm2f, nm2, watermark, thr, [&](bool pred, const KCand& c) {
+    if (pred) count_vs(c, w, ties, amb);
+  });
   add_counts(ties, amb, s.g32);
 }
 
@@ -939,7 +981,7 @@ __device__ bool team_join(const NJDev& s, const GridNJ& g, Team tm, int step, in
   grid_pass(s, g, tm, nm2f, (step & 1) != 0);
   if (!team_sync<CL>(g, target)) return false;
   if (!grid_pick_direct(s, g, tm, nm2, nm2f, watermark, &swin, &spick, &sthr)) {
-    grid_cand(s, g, tm, nm2f, nm2, watermark, sthr);
+    const KCand tfirst = grid_cand(s, g, tm, nm2f, nm2, watermark, sthr);
     if (!team_sync<CL>(g, target)) return false;
     // the winner's pair again, as the scan read it (row = the smaller slot)
     auto rederive = [&](const KCand& w) {
@@ -949,7 +991,7 @@ __device__ bool team_join(const NJDev& s, const GridNJ& g, Team tm, int step, in
                        watermark);
     };
     const int ncount = *(volatile int*)&s.g32[2];   // the same in every CTA
-    if (ncount <= s.cand_cap) {
+    if (ncount <= min(s.cand_cap, kListPickMax)) {
       if (threadIdx.x < 32) {
         const PickOut r = pick_keys(ncount, [&](int k) { return g.cand[k]; });
         if (threadIdx.x == 0) {
@@ -959,7 +1001,11 @@ __device__ bool team_join(const NJDev& s, const GridNJ& g, Team tm, int step, in
       }
       __syncthreads();
     } else {
+      __shared__ KCand sw[32];
       __shared__ KCand sfirst;
+      const KCand cf = cta_first(tfirst, sw);
+      if (threadIdx.x == 0) g.cbest[tm.rank] = cf;
+      if (!team_sync<CL>(g, target)) return false;
       if (threadIdx.x < 32) {
         const PickOut r = pick_keys(tm.size, [&](int k) { return ld_kcand(&g.cbest[k]); });
         if (threadIdx.x == 0) sfirst = r.error ? kc_none() : ld_kcand(&g.cbest[r.idx]);
@@ -1045,7 +1091,8 @@ __global__ void nj_lengths_kernel(nwg_join* joins, int count) {
 // Compaction, part 1 (one CTA): map[p] = new slot of live slot p (ascending),
 // T / Tf / node into the new slots, slot[v] of every live node remapped.
 __global__ void __launch_bounds__(1024) compact_map_kernel(NJDev s, int* map, double* T2, float* Tf2, int* node2,
-                                                           int nslots) {
+                                                           int nslots, const int* abort) {
+  if (*(volatile const int*)abort) return;
   __shared__ int wsum[33];
   const int n0 = s.n0;
   const int chunk = (n0 + blockDim.x - 1) / blockDim.x;
@@ -1090,7 +1137,9 @@ __global__ void __launch_bounds__(1024) compact_map_kernel(NJDev s, int* map, do
 }
 
 // Compaction, part 2: D2[map[p]][map[c]] = D[p][c] for live p, c (one block per old row).
-__global__ void __launch_bounds__(256) compact_copy_kernel(NJDev s, const int* map, float* D2, int ld2) {
+__global__ void __launch_bounds__(256) compact_copy_kernel(NJDev s, const int* map, float* D2, int ld2,
+                                                           const int* abort) {
+  if (*(volatile const int*)abort) return;
   const int p = blockIdx.x;
   const int np = map[p];
   if (np < 0) return;
@@ -1231,6 +1280,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_cluster_
 // join share's block reduction is.  The arithmetic is that of the other forms.
 
 constexpr int kCtaNJMax = 160;   // above it a cluster's shared memory is faster (measured crossover near 170)
+static_assert(kCtaNJMax * (kCtaNJMax - 1) / 2 + 1 <= kCandCap, "the one-CTA form lists every pair");
 constexpr int kCtaThreads = 256;
 
 struct CtaLayout {
@@ -1278,8 +1328,6 @@ __global__ void __launch_bounds__(kCtaThreads, 1) nj_cta_kernel(const NJJob* job
   __shared__ PickOut spick;
   __shared__ GCand swin;
   __shared__ float sthr;
-  __shared__ double s_sum;
-  __shared__ int s_exact;
   if ((int)blockIdx.x >= njobs) return;
   if (threadIdx.x == 0) sjob = jobs[blockIdx.x];
   __syncthreads();
@@ -1979,23 +2027,32 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
       // fallback: each CTA scans its own rows within the threshold into the
       // list (as grid_cand does; beyond the list's capacity the winner comes
       // from the CTAs' first candidates and a second scan counts against it)
+      // (one warp per local row, lanes over the columns; visit(pred, candidate)
+      // by whole warps as in grid_cand_scan)
       auto scan = [&](auto&& visit) {
-        for (int l = 0; l < m.lr; ++l) {
+        for (int l = warp; l < m.lr; l += nth >> 5) {
           const int r = m.slot_of(rank, l);
           if (r < 0 || m.grm[r] > othr) continue;
           const int ur = m.node[r];
           const float tr = m.Tf[r];
           const double Tr = m.Tloc[l];
           const float* row = m.rows + (size_t)l * m.ldl;
-          for (int c = r + 1 + tid; c < n; c += nth) {
-            const int uc = m.node[c];
-            if (uc < 0) continue;
-            const float d = row[c];
-            const float q = __fsub_rn(__fsub_rn(__fmul_rn(d, nm2f), tr), m.Tf[c]);
-            if (q > thr) continue;
-            const double Tc = m.at(m.Tloc, m.owner(c))[m.local_row(c)];
-            const GCand cd = make_cand(r, c, ur, uc, Tr, Tc, d, nm2, watermark);
-            visit(KCand{cd.k1, cd.k2, cd.a, cd.b});
+          for (int cb = r + 1; cb < n; cb += 32) {
+            const int c = cb + lane;
+            bool pred = false;
+            KCand kc = kc_none();
+            if (c < n) {
+              const int uc = m.node[c];
+              const float d = row[c];
+              const float q = __fsub_rn(__fsub_rn(__fmul_rn(d, nm2f), tr), m.Tf[c]);
+              if (uc >= 0 && q <= thr) {
+                const double Tc = m.at(m.Tloc, m.owner(c))[m.local_row(c)];
+                const GCand cd = make_cand(r, c, ur, uc, Tr, Tc, d, nm2, watermark);
+                kc = KCand{cd.k1, cd.k2, cd.a, cd.b};
+                pred = true;
+              }
+            }
+            visit(pred, kc);
           }
         }
       };
@@ -2011,16 +2068,14 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
       __shared__ KCand skw[32];
       __shared__ KCand sfirst;
       KCand first = kc_none();
-      scan([&](const KCand& c) {
-        const int idx = atomicAdd(&s.g32[2], 1);
-        if (idx < s.cand_cap) g.cand[idx] = c;
-        if (kc_first(c, first)) first = c;
+      bool full = false;
+      scan([&](bool pred, const KCand& c) {
+        list_push(s, g, pred, c, full);
+        if (pred && kc_first(c, first)) first = c;
       });
-      first = cta_first(first, skw);
-      if (tid == 0) g.cbest[rank] = first;
       cg::this_cluster().sync();
       const int ncount = *(volatile int*)&s.g32[2];   // the same in every CTA
-      if (ncount <= s.cand_cap) {
+      if (ncount <= min(s.cand_cap, kListPickMax)) {
         if (warp == 0) {
           const PickOut pr = pick_keys(ncount, [&](int k) { return g.cand[k]; });
           if (lane == 0) {
@@ -2030,6 +2085,9 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
         }
         __syncthreads();
       } else {
+        first = cta_first(first, skw);
+        if (tid == 0) g.cbest[rank] = first;
+        cg::this_cluster().sync();
         if (warp == 0) {
           const PickOut pr = pick_keys(C, [&](int k) { return ld_kcand(&g.cbest[k]); });
           if (lane == 0) sfirst = pr.error ? kc_none() : ld_kcand(&g.cbest[pr.idx]);
@@ -2037,7 +2095,9 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_smem_ker
         __syncthreads();
         const KCand w = sfirst;
         unsigned ties = 0, amb = 0;
-        scan([&](const KCand& c) { count_vs(c, w, ties, amb); });
+        scan([&](bool pred, const KCand& c) {
+          if (pred) count_vs(c, w, ties, amb);
+        });
         add_counts(ties, amb, s.g32);
         cg::this_cluster().sync();
         if (tid == 0) {
@@ -2345,7 +2405,7 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
         (rc = cuda(cudaMemsetAsync(S.Tf.p, 0xFF, sizeof(float) * ldd, s), "nj upload")))
       return rc;
     if (st) cudaEventRecord(ev0, s);
-    rowsum_kernel<<<(n + 7) / 8, 256, 0, s>>>(d);
+    rowsum_kernel<<<(n + 7) / 8, 256, 0, s>>>(d, g.abort);
     ++launches;
     // The reference's schedule (deterministic in n): rebuild after
     // max(n*0.5, 200) joins, then every m*0.5 joins, none below 200 active
@@ -2362,8 +2422,8 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
       const int ld2 = (na + 3) & ~3;
       int e;
       if ((e = cuda(cudaMemsetAsync(Tfalt, 0xFF, sizeof(float) * ld2, s), "nj launch"))) return e;
-      compact_map_kernel<<<1, 1024, 0, s>>>(d, (int*)S.map.p, Talt, Tfalt, nodealt, nn);
-      compact_copy_kernel<<<d.n0, 256, 0, s>>>(d, (const int*)S.map.p, Dalt, ld2);
+      compact_map_kernel<<<1, 1024, 0, s>>>(d, (int*)S.map.p, Talt, Tfalt, nodealt, nn, g.abort);
+      compact_copy_kernel<<<d.n0, 256, 0, s>>>(d, (const int*)S.map.p, Dalt, ld2, g.abort);
       launches += 2;
       std::swap(d.D, Dalt);
       std::swap(d.T, Talt);
@@ -2418,7 +2478,7 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
         }
       }
       if (rebuild) {
-        rowsum_kernel<<<(m_n + 7) / 8, 256, 0, s>>>(d);
+        rowsum_kernel<<<(m_n + 7) / 8, 256, 0, s>>>(d, g.abort);
         ++launches;
         if ((rc = compact(m_n))) return rc;
         ++stats.rebuilds;

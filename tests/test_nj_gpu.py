@@ -99,8 +99,9 @@ M = rng.integers(0, 5, size=(30, 30)).astype(np.float32)
 check(np.triu(M, 1) + np.triu(M, 1).T)
 M = rng.integers(0, 3, size=(300, 300)).astype(np.float32)
 check(np.triu(M, 1) + np.triu(M, 1).T)
-# more exactly tied pairs than the candidate list holds (65,536): 420 copies of
-# one sequence, three sequences 140 times each, a constant matrix
+# tens of thousands of exactly tied pairs per join (the pick from per-CTA
+# firsts and a counting scan): 420 copies of one sequence, three sequences
+# 140 times each, a constant matrix
 check(c.score_all([S[5]] * 420))
 check(c.score_all([S[k] for k in (1, 2, 3) for _ in range(140)]))
 M = np.full((400, 400), 5.0, dtype=np.float32)

@@ -94,8 +94,8 @@ def test_serving_matches_oracle():
 
 
 def test_serving_wide_exact_ties():
-    # jobs whose joins tie exactly on more pairs than the candidate list holds
-    # (420 copies of one sequence; three sequences 140 times each)
+    # jobs whose joins tie exactly on tens of thousands of pairs (420 copies
+    # of one sequence; three sequences 140 times each)
     S = synth.family(4, 60, ps=0.02, pi=0.0, seed=41)
     jobs = [[S[0]] * 420, [S[k] for k in (1, 2, 3) for _ in range(140)]]
     with Server(hbm_budget=4 << 30, max_batch_jobs=4) as srv:
@@ -113,7 +113,7 @@ def test_serving_admission_by_footprint(ctx):
     # a budget that holds about one 300-sequence job at a time: batches stay
     # small, results do not change
     jobs = [synth.family(n, 150, seed=30 + n) for n in (300, 280, 260, 40, 30)]
-    budget = 300 * 300 * 4 + (2 << 20)
+    budget = 300 * 300 * 4 + (1 << 20)
     with Server(hbm_budget=budget, max_batch_jobs=16) as srv:
         res = _run(srv, jobs)
     # 300 and 280 do not fit together; 260, 40 and 30 do
