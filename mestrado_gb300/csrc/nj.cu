@@ -69,7 +69,7 @@ namespace nwg {
 namespace {
 
 constexpr int kNJMaxN = 8192;
-constexpr int kCandCap = 1 << 14;      // candidate list capacity per join (every pair of a one-CTA job)
+constexpr int kCandCap = 2048;         // candidate list capacity per join (longer lists are not read)
 
 struct NJDev {
   float* D;            // n0 x ld, slots
@@ -505,11 +505,12 @@ __device__ PickOut pick_keys(int nc, Load&& load) {   // load(k) has k1, k2, a, 
 
 // Long candidate lists (wide exact ties, e.g. hundreds of identical
 // sequences, whose pairs all tie): above kListPickMax candidates one warp's
-// pick over the list would be slow, and the list may overflow.  Instead every
-// CTA keeps the first of its own candidates in the pick's order, the winner is
-// the first of those, and a second scan counts the ties and ambiguous pairs
-// against it with pick_keys' rule.
-constexpr int kListPickMax = 2048;
+// pick over the list would be slow, and the list does not hold them.  Instead
+// every CTA reduces its threads' first candidates in the pick's order, the
+// winner is the first of those, and a second scan counts the ties and
+// ambiguous pairs against it with pick_keys' rule.  (The one-CTA form always
+// picks this way, without the list.)
+constexpr int kListPickMax = kCandCap;
 
 __device__ __forceinline__ KCand kc_none() { return KCand{LLONG_MAX, LLONG_MAX, INT_MAX, -1}; }
 
@@ -1280,7 +1281,6 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(1024, 1) nj_cluster_
 // join share's block reduction is.  The arithmetic is that of the other forms.
 
 constexpr int kCtaNJMax = 160;   // above it a cluster's shared memory is faster (measured crossover near 170)
-static_assert(kCtaNJMax * (kCtaNJMax - 1) / 2 + 1 <= kCandCap, "the one-CTA form lists every pair");
 constexpr int kCtaThreads = 256;
 
 struct CtaLayout {
@@ -1486,40 +1486,61 @@ __global__ void __launch_bounds__(kCtaThreads, 1) nj_cta_kernel(const NJJob* job
     }
     __syncthreads();
     if (!s_ok) {
-      // fallback: the selected rows' pairs within the threshold into the list
-      for (int r = 0; r < n; ++r) {
-        if (grm[r] > othr) continue;
-        const int ur = node[r];
-        const float tr = Tf[r];
-        const float* row = rows + (size_t)r * ldl;
-        for (int c = r + 1 + tid; c < n; c += nth) {
-          const int uc = node[c];
-          if (uc < 0) continue;
-          const float d = row[c];
-          const float q = __fsub_rn(__fsub_rn(__fmul_rn(d, nm2f), tr), Tf[c]);
-          if (q > thr) continue;
-          const int idx = atomicAdd(&s.g32[2], 1);
-          if (idx < s.cand_cap) {
+      // fallback: the selected rows' pairs within the threshold, scanned
+      // twice: the first candidate in the pick's order (block reduction),
+      // then the ties and ambiguous pairs against it (pick_keys' rule)
+      auto scan = [&](auto&& visit) {
+        for (int r = 0; r < n; ++r) {
+          if (grm[r] > othr) continue;
+          const int ur = node[r];
+          const float tr = Tf[r];
+          const float* row = rows + (size_t)r * ldl;
+          for (int c = r + 1 + tid; c < n; c += nth) {
+            const int uc = node[c];
+            if (uc < 0) continue;
+            const float d = row[c];
+            const float q = __fsub_rn(__fsub_rn(__fmul_rn(d, nm2f), tr), Tf[c]);
+            if (q > thr) continue;
             const GCand cd = make_cand(r, c, ur, uc, T[r], T[c], d, nm2, watermark);
-            g.cand[idx] = KCand{cd.k1, cd.k2, cd.a, cd.b};
+            visit(KCand{cd.k1, cd.k2, cd.a, cd.b});
           }
         }
+      };
+      __shared__ KCand skw[32];
+      __shared__ KCand sfirst;
+      __shared__ unsigned scnt[2];
+      KCand first = kc_none();
+      scan([&](const KCand& c) {
+        if (kc_first(c, first)) first = c;
+      });
+      first = cta_first(first, skw);
+      if (tid == 0) {
+        sfirst = first;
+        scnt[0] = scnt[1] = 0;
       }
       __syncthreads();
-      if (warp == 0) {
-        const int ncount = *(volatile int*)&s.g32[2];
-        const int nc = min(ncount, s.cand_cap);
-        PickOut pr = pick_keys(nc, [&](int k) { return g.cand[k]; });
-        pr.error = pr.error || ncount > s.cand_cap;
-        if (lane == 0) {
-          spick = pr;
-          if (!pr.error) {
-            const KCand w = g.cand[pr.idx];
-            const int sa = slot[w.a], sb = slot[w.b];
-            const int r0 = min(sa, sb), c0 = max(sa, sb);
-            swin = make_cand(r0, c0, node[r0], node[c0], T[r0], T[c0], rows[(size_t)r0 * ldl + c0], nm2, watermark);
-          }
-          s.g32[2] = 0;
+      const KCand wk = sfirst;
+      unsigned ties = 0, amb = 0;
+      if (wk.b >= 0) scan([&](const KCand& c) { count_vs(c, wk, ties, amb); });
+      for (int o = 16; o > 0; o >>= 1) {
+        ties += __shfl_xor_sync(0xffffffffu, ties, o);
+        amb += __shfl_xor_sync(0xffffffffu, amb, o);
+      }
+      if (lane == 0 && (ties | amb)) {
+        atomicAdd(&scnt[0], ties);
+        atomicAdd(&scnt[1], amb);
+      }
+      __syncthreads();
+      if (tid == 0) {
+        spick.idx = 0;
+        spick.ties = scnt[0];
+        spick.amb = scnt[1];
+        spick.error = wk.b < 0;
+        if (!spick.error) {
+          // the winner's pair again, as the scan read it (row = the smaller slot)
+          const int sa = slot[wk.a], sb = slot[wk.b];
+          const int r0 = min(sa, sb), c0 = max(sa, sb);
+          swin = make_cand(r0, c0, node[r0], node[c0], T[r0], T[c0], rows[(size_t)r0 * ldl + c0], nm2, watermark);
         }
       }
       __syncthreads();

@@ -113,7 +113,7 @@ def test_serving_admission_by_footprint(ctx):
     # a budget that holds about one 300-sequence job at a time: batches stay
     # small, results do not change
     jobs = [synth.family(n, 150, seed=30 + n) for n in (300, 280, 260, 40, 30)]
-    budget = 300 * 300 * 4 + (1 << 20)
+    budget = 300 * 300 * 4 + (1 << 19)
     with Server(hbm_budget=budget, max_batch_jobs=16) as srv:
         res = _run(srv, jobs)
     # 300 and 280 do not fit together; 260, 40 and 30 do
