@@ -30,6 +30,7 @@ sys.path.insert(0, os.path.dirname(HERE))
 
 from mestrado_gb300 import synth  # noqa: E402
 import oracle_py  # noqa: E402
+from additive import random_tree_metric  # noqa: E402
 
 REF = os.environ.get("NWG_REFERENCE", "/root/reference")
 
@@ -44,8 +45,18 @@ CASES = {
     # lengths 100-300 (integer-only generator path: regenerated identically
     # on x86-64 and aarch64, so the input itself is not stored)
     "cfg3": lambda: synth.config(3),
+    # 100 sequences, each twice: 91 joins decided by the tie-break alone
+    "dup200": lambda: synth.family(100, 80, ps=0.05, pi=0.005, seed=31).subset(
+        [k for k in range(100) for _ in range(2)]),
+    # a tree metric (below) on 500 taxa: integer path lengths, exact q ties;
+    # the sequences only give the FASTA its names
+    "tree500": lambda: synth.family(500, 30, ps=0.05, pi=0.0, seed=13),
 }
 NO_INPUT = {"cfg3"}
+# cases whose matrix is not the sequences' scores
+MATRIX = {
+    "tree500": lambda S: random_tree_metric(len(S), 22)[0],
+}
 
 
 def build_ref():
@@ -61,7 +72,7 @@ def make(name: str) -> None:
     fasta = os.path.join(out, "input.fasta")
     S.to_fasta(fasta)
     keep_input = name not in NO_INPUT
-    D = oracle_py.score_all(S, threads=os.cpu_count() or 4)
+    D = MATRIX[name](S) if name in MATRIX else oracle_py.score_all(S, threads=os.cpu_count() or 4)
     ref = build_ref()
     with tempfile.TemporaryDirectory() as td:
         dpath = os.path.join(td, "D.f32")

@@ -24,11 +24,16 @@ def _same(j, ref):
         assert a["len_i"] == b["len_i"] and a["len_j"] == b["len_j"]
 
 
-@pytest.mark.parametrize("case", ["cfg0", "nj300", "nj1200"])
+@pytest.mark.parametrize("case", ["cfg0", "nj300", "nj1200", "dup200", "tree500"])
 def test_device_nj_matches_reference_tree(ctx, case):
+    # dup200 and tree500: most of the reference's tie-break decisions
     d = os.path.join(GOLD, case)
     names, seqs = read_fasta(os.path.join(d, "input.fasta"))
-    D = ctx.score_all(seqs)
+    if case == "tree500":
+        from additive import random_tree_metric
+        D = random_tree_metric(len(seqs), 22)[0]
+    else:
+        D = ctx.score_all(seqs)
     meta = json.load(open(os.path.join(d, "meta.json")))
     assert hashlib.sha256(D.tobytes()).hexdigest() == meta["D_sha256"]
     joins, st = ctx.nj(D, stats=True)

@@ -85,15 +85,28 @@ def _load_joins(path):
     return rows
 
 
-@pytest.mark.parametrize("case", ["cfg0", "nj300", "nj1200"])
+def golden_matrix(case, seqs):
+    """The matrix a golden case's joins were made on: the sequences' scores,
+    or for tree500 the tree metric of tests/additive.py (seed 22)."""
+    if case == "tree500":
+        from additive import random_tree_metric
+        return random_tree_metric(len(seqs), 22)[0]
+    return O.score_all(seqs, threads=os.cpu_count() or 2)
+
+
+@pytest.mark.parametrize("case", ["cfg0", "nj300", "nj1200", "dup200", "tree500"])
 def test_oracle_nj_matches_reference_golden(case):
+    # dup200 (every sequence twice) and tree500 (integer tree metric) pin the
+    # tie-break: 91 and 16 of their joins are exact ties in q
     d = os.path.join(GOLD, case)
     meta = json.load(open(os.path.join(d, "meta.json")))
     from fasta import read_fasta
     names, seqs = read_fasta(os.path.join(d, "input.fasta"))
-    D = O.score_all(seqs, threads=os.cpu_count() or 2)
+    D = golden_matrix(case, seqs)
     assert hashlib.sha256(D.tobytes()).hexdigest() == meta["D_sha256"]
     joins, st = O.nj(D)
+    if case in ("dup200", "tree500"):
+        assert st["tie_steps"] > 10
     ref = _load_joins(os.path.join(d, "joins.txt"))
     assert len(ref) == len(joins)
     for r, j in zip(ref, joins):

@@ -27,7 +27,7 @@ def test_reference_cherry_list_is_a_prefix():
     # buildAlign on one rank hands AlignmentMatch the first (n0-1)/3 getNodes
     # triples minus the last (SpeciesBlock.cpp:1393-1455); its vecSize==2
     # entries must be the first cherries of the full post-order list.
-    for case in ("cfg0", "nj300", "nj1200"):
+    for case in ("cfg0", "nj300", "nj1200", "dup200", "tree500"):
         left, right = _joins(case)
         n = len(left) + 1
         node, l, r = cherries(left, right, n)
