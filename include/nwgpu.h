@@ -350,7 +350,8 @@ int nwg_server_submit(nwg_server* srv, const char* ascii, const int64_t* offsets
 /* Waits up to timeout_ms (< 0: no limit; NWG_ERR_TIMEOUT when it runs out, the
  * job stays queryable) for the job, copies its n*n matrix to D and its n-1
  * joins to joins (either may be NULL) and releases it; returns the job's
- * status. */
+ * status.  A second call for a job another thread is waiting for returns
+ * NWG_ERR_INVALID at once. */
 int nwg_server_wait(nwg_server* srv, uint64_t job_id, int timeout_ms, float* D, nwg_join* joins,
                     nwg_job_info* info);
 /* Stops admitting, finishes the batches on the device, frees everything.

@@ -81,6 +81,7 @@ struct ServeJob {
   int batch_jobs = 0;
   int status = NWG_OK;
   bool done = false;
+  bool waited = false;   // a nwg_server_wait call holds the job (one waiter at a time)
   std::vector<float> D;
   std::vector<nwg_join> joins;
   unsigned long long njst[5] = {0, 0, 0, 0, 0};
@@ -547,9 +548,15 @@ int nwg_server_wait(nwg_server* srv, uint64_t job_id, int timeout_ms, float* D, 
   auto it = s->jobs.find(job_id);
   if (it == s->jobs.end()) return NWG_ERR_INVALID;
   nwg::ServeJob* J = it->second;
+  if (J->waited) return NWG_ERR_INVALID;   // another thread is waiting for it and will release it
+  J->waited = true;
   const auto pred = [&] { return J->done; };
-  if (timeout_ms < 0) s->cv_done.wait(lk, pred);
-  else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred)) return NWG_ERR_TIMEOUT;
+  if (timeout_ms < 0) {
+    s->cv_done.wait(lk, pred);
+  } else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred)) {
+    J->waited = false;
+    return NWG_ERR_TIMEOUT;
+  }
   if (D && !J->D.empty()) std::memcpy(D, J->D.data(), sizeof(float) * J->D.size());
   if (joins && !J->joins.empty()) std::memcpy(joins, J->joins.data(), sizeof(nwg_join) * J->joins.size());
   if (info) {
