@@ -1,0 +1,78 @@
+"""The oracle's neighbor joining against the reference's own buildTree
+(SpeciesBlock.cpp and TreeNode.cpp compiled unchanged through the one-rank
+shim into oracle/_ref/ref_nj) on fresh seeded matrices: sequence families,
+duplicated sequences, tree metrics, small-integer and real-valued matrices.
+The matrix is handed to the reference as its distance matrix (NWG_REF_D), so
+any matrix can be compared.  Where the oracle counts no ambiguous step the
+join lists and branch lengths are identical bit for bit.  CPU only; skipped
+where the reference checkout is absent."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle_py as O
+from additive import random_tree_metric
+from mestrado_gb300 import synth
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF = os.environ.get("NWG_REFERENCE", "/root/reference")
+
+pytestmark = pytest.mark.skipif(not os.path.isfile(os.path.join(REF, "SpeciesBlock.cpp")),
+                                reason="reference sources not present")
+
+
+@pytest.fixture(scope="module")
+def ref_nj():
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={REF}"], check=True)
+    return os.path.join(ROOT, "oracle", "_ref", "ref_nj")
+
+
+def _symmetric(M):
+    M = np.triu(M.astype(np.float32), 1)
+    return M + M.T
+
+
+def _matrix(kind, seed):
+    rng = np.random.default_rng(seed)
+    if kind == "family":
+        return O.score_all(synth.family(90, 150, ps=0.1, pi=0.01, seed=seed), threads=os.cpu_count() or 2)
+    if kind == "families":
+        S = synth.family(80, 60, ps=0.08, pi=0.005, families=3, seed=seed)
+        return O.score_all(S, threads=os.cpu_count() or 2)
+    if kind == "duplicates":
+        S = synth.family(120, 50, ps=0.05, pi=0.005, seed=seed)
+        return O.score_all(S.subset([k for k in range(120) for _ in range(2)]), threads=os.cpu_count() or 2)
+    if kind == "tree":
+        return random_tree_metric(350, seed)[0]
+    if kind == "integers":
+        return _symmetric(rng.integers(0, 50, size=(200, 200)))
+    if kind == "gaussian":
+        return _symmetric(rng.normal(0, 100, size=(300, 300)))
+    raise ValueError(kind)
+
+
+def _reference_joins(ref, D, tmp_path):
+    # the FASTA only names the taxa: the matrix comes from the file
+    fasta = tmp_path / "in.fasta"
+    fasta.write_text("".join(f">t{k}\nA\n" for k in range(len(D))))
+    dpath = tmp_path / "D.f32"
+    np.ascontiguousarray(D, dtype=np.float32).tofile(dpath)
+    env = dict(os.environ, NWG_REF_D=str(dpath))
+    subprocess.run([ref, str(fasta), str(tmp_path / "out")], check=True, cwd=tmp_path, env=env,
+                   stdout=subprocess.DEVNULL, timeout=120)
+    rows = [line.split() for line in open(tmp_path / "out.joins")]
+    return [(int(k), int(l), int(r), float.fromhex(a), float.fromhex(b)) for k, l, r, a, b in rows]
+
+
+@pytest.mark.parametrize("kind,seed", [("family", 101), ("families", 102), ("duplicates", 103), ("tree", 41),
+                                       ("tree", 42), ("integers", 104), ("gaussian", 105), ("gaussian", 106)])
+def test_oracle_nj_equals_reference_on_fresh_matrices(ref_nj, tmp_path, kind, seed):
+    D = _matrix(kind, seed)
+    joins, st = O.nj(D)
+    assert st["ambiguous_steps"] == 0
+    ref = _reference_joins(ref_nj, D, tmp_path)
+    assert len(ref) == len(joins) == len(D) - 1
+    for r, j in zip(ref, joins):
+        assert r == (j["node"], j["i"], j["j"], j["len_i"], j["len_j"])
