@@ -76,3 +76,35 @@ def test_oracle_nj_equals_reference_on_fresh_matrices(ref_nj, tmp_path, kind, se
     assert len(ref) == len(joins) == len(D) - 1
     for r, j in zip(ref, joins):
         assert r == (j["node"], j["i"], j["j"], j["len_i"], j["len_j"])
+
+
+def _reference_conversion_table():
+    # AlignmentScore::conversion (AlignmentScore.cu:10-27), read from the source
+    # text.  Its initializer lists 255 values: entry 255 is zero-filled.
+    import re
+    src = open(os.path.join(REF, "AlignmentScore.cu")).read()
+    body = src[src.index("AlignmentScore::conversion[256]"):]
+    body = body[body.index("{") + 1:body.index("}")]
+    table = [int(v) for v in re.findall(r"-?\d+", body)]
+    assert len(table) == 255
+    return table + [0]
+
+
+def test_encoding_equals_reference_table_for_every_byte():
+    from mestrado_gb300 import _native, encode
+    table = _reference_conversion_table()
+    for b in range(1, 255):   # byte 0 ends a C string: not a residue
+        if table[b] < 0:
+            with pytest.raises(_native.NWGError) as e:
+                encode([bytes([b])])
+            assert e.value.status == _native.NWG_ERR_BAD_RESIDUE
+        else:
+            codes, _ = encode([bytes([b, b, 65])])
+            assert list(codes) == [0, table[b], table[b]]   # reversed: 'A' (code 0) first
+    # byte 0xFF: the reference's zero-filled entry reads it as 'A'; it is no
+    # residue letter, and this library reports it like every byte outside the
+    # alphabet
+    assert table[255] == 0
+    with pytest.raises(_native.NWGError) as e:
+        encode([bytes([255])])
+    assert e.value.status == _native.NWG_ERR_BAD_RESIDUE
