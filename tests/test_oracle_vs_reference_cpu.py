@@ -108,3 +108,16 @@ def test_encoding_equals_reference_table_for_every_byte():
     with pytest.raises(_native.NWGError) as e:
         encode([bytes([255])])
     assert e.value.status == _native.NWG_ERR_BAD_RESIDUE
+
+
+def test_substitution_matrix_equals_reference():
+    # blosum64.txt and substitutionMatrix (definitions.cuh:96-121) of the
+    # reference, read from their text; the oracle's built-in matrix
+    import re
+    txt = [int(v) for v in re.findall(r"-?\d+", open(os.path.join(REF, "blosum64.txt")).read())]
+    src = open(os.path.join(REF, "definitions.cuh")).read()
+    body = src[src.index("substitutionMatrix[SUBSTITUTION_MATRIX_SIZE]"):]
+    body = body[body.index("{") + 1:body.index("}")]
+    cuh = [int(v) for v in re.findall(r"-?\d+", body)]
+    assert len(txt) == len(cuh) == 576 and txt == cuh
+    assert np.asarray(O.blosum(), dtype=np.int64).reshape(576).tolist() == cuh
