@@ -121,3 +121,23 @@ def test_substitution_matrix_equals_reference():
     cuh = [int(v) for v in re.findall(r"-?\d+", body)]
     assert len(txt) == len(cuh) == 576 and txt == cuh
     assert np.asarray(O.blosum(), dtype=np.int64).reshape(576).tolist() == cuh
+
+
+def test_reference_wire_blocks_and_matrix_layout(ref_nj, tmp_path):
+    # Without a precomputed matrix the harness lets SpeciesBlock build its own
+    # wire blocks (SpeciesBlock.cpp:309-322) and fill m_distances through the
+    # AlignmentScore calls of :356-363, with the oracle decoding each block and
+    # scoring each pair.  Its matrix equals score_all on the FASTA: the block
+    # format and the row/column layout are the reference's.
+    from fasta import read_fasta
+    S = synth.family(23, 40, ps=0.15, pi=0.03, families=2, seed=107)   # ragged lengths
+    fasta = tmp_path / "in.fasta"
+    S.to_fasta(str(fasta))
+    subprocess.run([ref_nj, str(fasta), str(tmp_path / "out")], check=True, cwd=tmp_path,
+                   stdout=subprocess.DEVNULL, timeout=120, env={k: v for k, v in os.environ.items()
+                                                               if k != "NWG_REF_D"})
+    n = len(S)
+    Dref = np.fromfile(tmp_path / "out.D", dtype=np.float32).reshape(n, n)
+    _, seqs = read_fasta(str(fasta))
+    assert np.array_equal(Dref, O.score_all(seqs))
+    assert len(set(len(s) for s in seqs)) > 10
