@@ -63,7 +63,10 @@ def _reference_joins(ref, D, tmp_path):
     subprocess.run([ref, str(fasta), str(tmp_path / "out")], check=True, cwd=tmp_path, env=env,
                    stdout=subprocess.DEVNULL, timeout=120)
     rows = [line.split() for line in open(tmp_path / "out.joins")]
-    return [(int(k), int(l), int(r), float.fromhex(a), float.fromhex(b)) for k, l, r, a, b in rows]
+    joins = [(int(k), int(l), int(r), float.fromhex(a), float.fromhex(b)) for k, l, r, a, b in rows]
+    tree = (tmp_path / "in.tree").read_text()
+    cherries = [tuple(int(v) for v in line.split()) for line in open(tmp_path / "out.cherries")]
+    return joins, tree, cherries
 
 
 @pytest.mark.parametrize("kind,seed", [("family", 101), ("families", 102), ("duplicates", 103), ("tree", 41),
@@ -72,10 +75,21 @@ def test_oracle_nj_equals_reference_on_fresh_matrices(ref_nj, tmp_path, kind, se
     D = _matrix(kind, seed)
     joins, st = O.nj(D)
     assert st["ambiguous_steps"] == 0
-    ref = _reference_joins(ref_nj, D, tmp_path)
+    ref, tree, ref_cherries = _reference_joins(ref_nj, D, tmp_path)
     assert len(ref) == len(joins) == len(D) - 1
     for r, j in zip(ref, joins):
         assert r == (j["node"], j["i"], j["j"], j["len_i"], j["len_j"])
+    # the .tree text (labels are the header lines, '>' included) and the
+    # cherries buildAlign hands on, a prefix of the full post-order list
+    from mestrado_gb300 import cherries, newick
+    from mestrado_gb300._native import JOIN_DTYPE
+    n = len(D)
+    lib_joins = np.zeros(len(joins), dtype=np.dtype(JOIN_DTYPE))
+    for f in joins.dtype.names:
+        lib_joins[f] = joins[f]
+    assert newick(lib_joins, [f">t{k}" for k in range(n)]) == tree
+    node, left, right = cherries(joins["i"], joins["j"], n)
+    assert ref_cherries == list(zip(node.tolist(), left.tolist(), right.tolist()))[: len(ref_cherries)]
 
 
 def _reference_conversion_table():
