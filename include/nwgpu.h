@@ -317,9 +317,10 @@ int nwg_msa_rows(nwg_ctx* ctx, char* out, int64_t row_stride);
  * A worker thread admits pending jobs while their HBM footprint
  * (n^2 floats of matrix + NJ workspace + codes) fits hbm_budget_bytes and puts
  * up to max_batch_jobs of them into one batch: one persistent launch per
- * length bucket with pairs of all the batch's jobs interleaved, then one
- * launch with a cluster of 8 CTAs per job (16 from 256 sequences on) running the whole join
- * loop.  Up to four batches
+ * length bucket with pairs of all the batch's jobs interleaved, then the
+ * join loops, one launch per form: one CTA per job up to 160 sequences, a
+ * cluster per job (8 CTAs, 16 from 256 sequences on) with the matrix in its
+ * shared memory up to 768, a cluster over L2 above.  Up to four batches
  * can be on the device at once (own streams), so jobs arriving while one batch runs
  * are admitted and overlap it, and each batch is returned as soon as it is done.  Each job's matrix and join list equal what
  * nwg_score_all and nwg_nj return for that job alone.
