@@ -38,8 +38,10 @@
 //  2. the candidates are the pairs whose float q is at most min + 3E: when
 //     each row within that threshold has one such pair (its second smallest q
 //     is beyond), they are those rows' minima; otherwise the rows are scanned
-//     again into a list.  Each candidate gets its exact double q in both
-//     roundings.
+//     again into a list (up to 2048 candidates; beyond that, as in the
+//     one-CTA form always, the CTAs reduce their first candidates and a
+//     second scan counts the ties).  Each candidate gets its exact double q in
+//     both roundings.
 // The winner follows the tie-break; the ambiguity check runs over the
 // candidates: any pair left out has q > winner + E, beyond reach of either
 // rounding.  All floating-point operations use the _rn intrinsics in the
