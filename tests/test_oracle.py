@@ -59,6 +59,19 @@ def test_score_matches_textbook_dp(seed):
         assert O.score_pair(x, y) == O.score_pair(y, x)
 
 
+@pytest.mark.parametrize("go,ge", [(5, 1), (11, 1), (20, 5), (2, 3), (0, 0)])
+def test_score_matches_textbook_dp_other_penalties(go, ge):
+    # the gap model beyond 10/2, including an extension dearer than an
+    # opening and no gap cost at all
+    rng = np.random.default_rng(go * 31 + ge)
+    letters = np.frombuffer(b"ARNDCQEGHILKMFPSTWYVBZX*", dtype=np.uint8)
+    for _ in range(30):
+        lx, ly = rng.integers(1, 40, size=2)
+        x = letters[rng.integers(0, 24, lx)].tobytes()
+        y = letters[rng.integers(0, 24, ly)].tobytes()
+        assert O.score_pair(x, y, go, ge) == _gotoh_textbook(x, y, go, ge)
+
+
 def test_traceback_known_answers():
     assert O.traceback(b"A", b"A") == (b"A", b"A", 4)
     assert O.traceback(b"AW", b"A") == (b"AW", b"A-", 2)
