@@ -53,3 +53,23 @@ def test_oracle_alignments_rescore_to_their_score():
         ax, ay, sc = O.traceback(x, y)
         assert ax.replace(b"-", b"") == x and ay.replace(b"-", b"") == y
         assert rescore(ax, ay, sub) == sc
+
+
+def test_oracle_alignments_rescore_under_other_gap_models():
+    # the same property for gap models with go >= ge (with go < ge a run of
+    # gaps is cheaper reopened than extended, which this run-cost model does
+    # not express; the reference only runs 10/2)
+    import numpy as np
+    import oracle_py as O
+    from rescore import rescore
+    letters = np.frombuffer(b"ARNDCQEGHILKMFPSTWYV", dtype=np.uint8)
+    sub = O.blosum()
+    for go, ge in ((5, 1), (11, 1), (20, 5), (6, 6)):
+        rng = np.random.default_rng(go * 7 + ge)
+        for _ in range(25):
+            x = letters[rng.integers(0, 20, rng.integers(1, 120))].tobytes()
+            y = letters[rng.integers(0, 20, rng.integers(1, 120))].tobytes()
+            ax, ay, sc = O.traceback(x, y, go, ge)
+            assert ax.replace(b"-", b"") == x and ay.replace(b"-", b"") == y
+            assert sc == O.score_pair(x, y, go, ge)
+            assert rescore(ax, ay, sub, go, ge) == sc
