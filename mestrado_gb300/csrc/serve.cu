@@ -578,7 +578,9 @@ int nwg_server_wait(nwg_server* srv, uint64_t job_id, int timeout_ms, float* D, 
     info->nj_rebuilds = (int64_t)J->njst[4];
   }
   const int st = J->status;
-  s->jobs.erase(it);
+  // By key: the wait released the lock, and a submit on another thread may
+  // have rehashed the map meanwhile, which invalidates `it`.
+  s->jobs.erase(job_id);
   delete J;
   return st;
 }

@@ -152,3 +152,43 @@ def test_serving_rejects():
         with pytest.raises(NWGError) as e:
             srv.wait(12345, 3)
         assert e.value.status == NWG_ERR_INVALID
+
+
+def test_waits_survive_rehashes_of_the_job_table(ctx):
+    # One thread submits thousands of small jobs -- each insert may rehash the
+    # server's job table -- while four threads wait on the jobs already
+    # submitted.  Every wait returns its own job's result and releases it.
+    import queue
+    jobs = [synth.family(2 + k % 4, 24, seed=5000 + k) for k in range(4000)]
+    q = queue.Queue()
+    out = [None] * len(jobs)
+    errors = []
+    with Server(max_batch_jobs=64) as srv:
+        def submitter():
+            for k, S in enumerate(jobs):
+                q.put((k, srv.submit(S)))
+            for _ in range(4):
+                q.put(None)
+
+        def waiter():
+            while True:
+                item = q.get()
+                if item is None:
+                    return
+                k, jid = item
+                try:
+                    out[k] = srv.wait(jid, len(jobs[k]))
+                except Exception as e:  # noqa: BLE001 -- reported below
+                    errors.append((k, repr(e)))
+
+        th = [threading.Thread(target=submitter)] + [threading.Thread(target=waiter) for _ in range(4)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        with pytest.raises(NWGError):
+            srv.wait(1, 2)          # released jobs are gone
+    assert not errors, errors[:5]
+    assert all(o is not None and o[2]["status"] == 0 for o in out)
+    for k in range(0, len(jobs), 20):
+        assert np.array_equal(out[k][0], ctx.score_all(jobs[k]))
