@@ -218,7 +218,10 @@ int64_t nwg_newick(const nwg_join* joins, int n, const char* const* names, char*
  * with that device current; make it before any stream capture.  All calls on
  * a device share the array and it keeps the last call's contents (nothing in
  * it needs to start at zero); calls whose kernels overlap on the GPU race on
- * it and must be serialized.  Returns once the kernel is queued. */
+ * it and must be serialized.  The looked-up address is kept for the life of
+ * the process: resetting the device (cudaDeviceReset, or a reset of the
+ * primary context) after the first call is not supported.  Returns once the
+ * kernel is queued. */
 int nwg_score_pairs_noalloc(const int8_t* d_codes, const int64_t* d_start, const int32_t* d_len,
                             const int32_t* d_pi, const int32_t* d_pj, int64_t npairs, int32_t* d_out,
                             int max_len, int gap_open, int gap_ext, const int8_t* d_sub, void* stream);

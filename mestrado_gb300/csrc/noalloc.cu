@@ -14,7 +14,9 @@
 //
 // Set-up: the first call on a device (with that device current) looks the
 // array up with cudaGetSymbolAddress once and keeps the address for that
-// device; make that first call before any stream capture begins.
+// device; make that first call before any stream capture begins.  The
+// address is kept for the life of the process, so a device reset after the
+// first call (which reloads the module) is not supported.
 //
 // Sharing: every call on a device uses the same array and it keeps the last
 // call's contents.  Nothing in it has to start at zero: each pair writes the
@@ -23,7 +25,8 @@
 #include <climits>
 #include <mutex>
 
-#include "nwg_internal.h"
+#include "nwg_matrix.h"
+#include "wave_impl.cuh"
 
 namespace nwg {
 namespace {
@@ -31,39 +34,13 @@ namespace {
 constexpr size_t kNoallocScratchBytes = size_t(32) << 20;
 constexpr int64_t kNoallocScratchCells = (int64_t)(kNoallocScratchBytes / sizeof(int2));
 constexpr int kNoallocThreads = 128;
-constexpr int kNoallocRows = 16;
 constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) int2 g_noalloc_scratch[kNoallocScratchCells];
 
 // the built-in matrix (blosum64.txt / definitions.cuh:96-121, BLOSUM62 values)
 // in static device memory, used when the caller passes no matrix
-static __device__ int8_t g_noalloc_sub[kLetters * kLetters] = {
-   4,-1,-2,-2, 0,-1,-1, 0,-2,-1,-1,-1,-1,-2,-1, 1, 0,-3,-2, 0,-2,-1, 0,-4,
-  -1, 5, 0,-2,-3, 1, 0,-2, 0,-3,-2, 2,-1,-3,-2,-1,-1,-3,-2,-3,-1, 0,-1,-4,
-  -2, 0, 6, 1,-3, 0, 0, 0, 1,-3,-3, 0,-2,-3,-2, 1, 0,-4,-2,-3, 3, 0,-1,-4,
-  -2,-2, 1, 6,-3, 0, 2,-1,-1,-3,-4,-1,-3,-3,-1, 0,-1,-4,-3,-3, 4, 1,-1,-4,
-   0,-3,-3,-3, 9,-3,-4,-3,-3,-1,-1,-3,-1,-2,-3,-1,-1,-2,-2,-1,-3,-3,-2,-4,
-  -1, 1, 0, 0,-3, 5, 2,-2, 0,-3,-2, 1, 0,-3,-1, 0,-1,-2,-1,-2, 0, 3,-1,-4,
-  -1, 0, 0, 2,-4, 2, 5,-2, 0,-3,-3, 1,-2,-3,-1, 0,-1,-3,-2,-2, 1, 4,-1,-4,
-   0,-2, 0,-1,-3,-2,-2, 6,-2,-4,-4,-2,-3,-3,-2, 0,-2,-2,-3,-3,-1,-2,-1,-4,
-  -2, 0, 1,-1,-3, 0, 0,-2, 8,-3,-3,-1,-2,-1,-2,-1,-2,-2, 2,-3, 0, 0,-1,-4,
-  -1,-3,-3,-3,-1,-3,-3,-4,-3, 4, 2,-3, 1, 0,-3,-2,-1,-3,-1, 3,-3,-3,-1,-4,
-  -1,-2,-3,-4,-1,-2,-3,-4,-3, 2, 4,-2, 2, 0,-3,-2,-1,-2,-1, 1,-4,-3,-1,-4,
-  -1, 2, 0,-1,-3, 1, 1,-2,-1,-3,-2, 5,-1,-3,-1, 0,-1,-3,-2,-2, 0, 1,-1,-4,
-  -1,-1,-2,-3,-1, 0,-2,-3,-2, 1, 2,-1, 5, 0,-2,-1,-1,-1,-1, 1,-3,-1,-1,-4,
-  -2,-3,-3,-3,-2,-3,-3,-3,-1, 0, 0,-3, 0, 6,-4,-2,-2, 1, 3,-1,-3,-3,-1,-4,
-  -1,-2,-2,-1,-3,-1,-1,-2,-2,-3,-3,-1,-2,-4, 7,-1,-1,-4,-3,-2,-2,-1,-2,-4,
-   1,-1, 1, 0,-1, 0, 0, 0,-1,-2,-2, 0,-1,-2,-1, 4, 1,-3,-2,-2, 0, 0, 0,-4,
-   0,-1, 0,-1,-1,-1,-1,-2,-2,-1,-1,-1,-1,-2,-1, 1, 5,-2,-2, 0,-1,-1, 0,-4,
-  -3,-3,-4,-4,-2,-2,-3,-2,-2,-3,-2,-3,-1, 1,-4,-3,-2,11, 2,-3,-4,-3,-2,-4,
-  -2,-2,-2,-3,-2,-1,-2,-3, 2,-1,-1,-2,-1, 3,-3,-2,-2, 2, 7,-1,-3,-2,-1,-4,
-   0,-3,-3,-3,-1,-2,-2,-3,-3, 3, 1,-2, 1,-1,-2,-2, 0,-3,-1, 4,-3,-2,-1,-4,
-  -2,-1, 3, 4,-3, 0, 1,-1, 0,-3,-4, 0,-3,-3,-2, 0,-1,-4,-3,-3, 4, 1,-1,-4,
-  -1, 0, 0, 1,-3, 3, 4,-2, 0,-3,-3, 1,-1,-3,-1, 0,-1,-3,-2,-2, 1, 4,-1,-4,
-   0,-1,-1,-1,-2,-1,-1,-1,-1,-1,-1,-1,-1,-1,-2, 0, 0,-2,-1,-1,-1,-1,-1,-4,
-  -4,-4,-4,-4,-4,-4,-4,-4,-4,-4,-4,-4,-4,-4,-4,-4,-4,-4,-4,-4,-4,-4,-4, 1,
-};
+static __device__ int8_t g_noalloc_sub[kLetters * kLetters] = {NWG_BLOSUM64_VALUES};
 
 struct DeviceSetup {
   std::mutex mu;
@@ -77,14 +54,11 @@ DeviceSetup& setup_state() {
   return s;
 }
 
-__device__ __forceinline__ unsigned nclamp(int c) {
-  const unsigned u = (unsigned)c;
-  return u < (unsigned)kLetters ? u : (unsigned)(kLetters - 1);
-}
-
-// One pair per thread, int32, 16-row register strip; the (H, F) row between
-// strips lives in the static array at stride `stride` (NeedlemanWunsch.cu:
-// 22-161 with the strips widened to 16 rows).
+// One pair per thread through the plain form's per-thread scorer (int32,
+// 16-row register strip, NeedlemanWunsch.cu:22-161 with the strips widened to
+// 16 rows); the (H, F) row between strips lives in the static array at stride
+// `stride`.  A thread scores pairs k, k + stride, ... in turn and reuses its
+// column of the array for each.
 __global__ void __launch_bounds__(kNoallocThreads)
 noalloc_pairs_kernel(const int8_t* __restrict__ codes, const int64_t* __restrict__ start,
                      const int32_t* __restrict__ len, const int32_t* __restrict__ pi,
@@ -102,43 +76,7 @@ noalloc_pairs_kernel(const int8_t* __restrict__ codes, const int64_t* __restrict
       out[k] = INT_MIN;
       continue;
     }
-    const int8_t* X = codes + start[i];
-    const int8_t* Y = codes + start[j];
-    for (int c = 0; c < Lx; ++c) sc[(int64_t)c * stride] = make_int2(-ge * (c + 1), kShortMin + ge);
-    int hc = 0;
-    for (int y0 = 0; y0 < Ly; y0 += kNoallocRows) {
-      int yl[kNoallocRows], Hs[kNoallocRows], Es[kNoallocRows];
-#pragma unroll
-      for (int r = 0; r < kNoallocRows; ++r) {
-        yl[r] = (y0 + r < Ly) ? (int)nclamp(Y[y0 + r]) * kLetters : 0;
-        Hs[r] = -ge * (y0 + r + 1);
-        Es[r] = kShortMin + ge;
-      }
-      int upleft = -ge * y0;
-      const int ymin = min(kNoallocRows, Ly - y0);
-      for (int c = 0; c < Lx; ++c) {
-        int diag = upleft;
-        const int2 af = sc[(int64_t)c * stride];
-        hc = af.x;
-        upleft = af.x;
-        int f = af.y;
-        const unsigned xc = nclamp(X[c]);
-#pragma unroll
-        for (int r = 0; r < kNoallocRows; ++r) {
-          if (r < ymin) {
-            const int s = s_sub[yl[r] + xc];
-            f = max(f - ge, hc - go);
-            const int e = max(Es[r] - ge, Hs[r] - go);
-            hc = max(max(e, f), s + diag);
-            diag = Hs[r];
-            Hs[r] = hc;
-            Es[r] = e;
-          }
-        }
-        sc[(int64_t)c * stride] = make_int2(hc, f);
-      }
-    }
-    out[k] = hc;
+    out[k] = wave::score_thread(codes + start[i], Lx, codes + start[j], Ly, go, ge, s_sub, sc, stride);
   }
 }
 

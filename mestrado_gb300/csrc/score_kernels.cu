@@ -26,52 +26,9 @@ namespace {
 using wave::Lanes;
 using wave::clamp_code;
 using wave::put_score;
+using wave::score_thread;
 
 // ---- plain form ------------------------------------------------------------
-
-// One pair per thread, int32, 16-row register strip; the (H, F) row between
-// strips lives in global scratch, one int2 per X column at stride `stride`
-// (consecutive threads adjacent: coalesced).  Same loop structure as
-// NeedlemanWunschGlobalScoreKernel with its 12-row strips widened to 16.
-__device__ __forceinline__ int score_thread(const int8_t* __restrict__ X, int Lx,
-                                            const int8_t* __restrict__ Y, int Ly, int go, int ge,
-                                            const int8_t* s_sub, int2* sc, int64_t stride) {
-  for (int c = 0; c < Lx; ++c) sc[(int64_t)c * stride] = make_int2(-ge * (c + 1), kShortMin + ge);
-  int hc = 0;
-  for (int y0 = 0; y0 < Ly; y0 += kPlainRows) {
-    int yl[kPlainRows], Hs[kPlainRows], Es[kPlainRows];
-#pragma unroll
-    for (int r = 0; r < kPlainRows; ++r) {
-      yl[r] = (y0 + r < Ly) ? (int)clamp_code(Y[y0 + r]) * kLetters : 0;
-      Hs[r] = -ge * (y0 + r + 1);
-      Es[r] = kShortMin + ge;
-    }
-    int upleft = -ge * y0;
-    const int ymin = min(kPlainRows, Ly - y0);
-    for (int c = 0; c < Lx; ++c) {
-      int diag = upleft;
-      const int2 af = sc[(int64_t)c * stride];
-      hc = af.x;
-      upleft = af.x;
-      int f = af.y;
-      const unsigned xc = clamp_code(X[c]);
-#pragma unroll
-      for (int r = 0; r < kPlainRows; ++r) {
-        if (r < ymin) {
-          const int s = s_sub[yl[r] + xc];
-          f = max(f - ge, hc - go);
-          const int e = max(Es[r] - ge, Hs[r] - go);
-          hc = max(max(e, f), s + diag);
-          diag = Hs[r];
-          Hs[r] = hc;
-          Es[r] = e;
-        }
-      }
-      sc[(int64_t)c * stride] = make_int2(hc, f);
-    }
-  }
-  return hc;
-}
 
 __global__ void __launch_bounds__(kPlainThreads) plain_kernel(const PlainArgs a) {
   __shared__ int8_t s_sub[kLetters * kLetters];

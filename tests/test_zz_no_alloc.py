@@ -69,3 +69,99 @@ def test_noalloc_rejects_sizes_beyond_its_maximum():
     assert f(1, 1, 1, 1, 1, 1, 1, 32769, 10, 2, None, None) == NWG_ERR_INVALID
     assert f(1, 1, 1, 1, 1, 1, 1, 0, 10, 2, None, None) == NWG_ERR_INVALID
     assert f(None, None, None, None, None, 0, None, 100, 10, 2, None, None) == NWG_OK
+
+
+def _dev_arrays(codes, start, lens, pi, pj):
+    import torch
+    return (torch.from_numpy(codes).cuda(), torch.from_numpy(start).cuda(), torch.from_numpy(lens).cuda(),
+            torch.from_numpy(pi).cuda(), torch.from_numpy(pj).cuda(),
+            torch.full((len(pi),), -7, dtype=torch.int32, device="cuda"))
+
+
+def _call(f, arrs, max_len, stream=None):
+    d_codes, d_start, d_len, d_pi, d_pj, d_out = arrs
+    return f(d_codes.data_ptr(), d_start.data_ptr(), d_len.data_ptr(), d_pi.data_ptr(), d_pj.data_ptr(),
+             len(d_pi), d_out.data_ptr(), max_len, 10, 2, None, stream)
+
+
+def test_noalloc_each_thread_scores_many_pairs():
+    # max_len 32768 leaves room for 128 concurrent pairs: one block of 128
+    # threads, so every thread walks the grid-stride loop about 25 times and
+    # reuses its scratch column, once for a 30,000-residue X
+    import torch
+    f = _entry()
+    seqs = _set(103, 40, 1, 400) + _set(104, 1, 30000, 30000)
+    codes, off = encode(seqs)
+    lens = np.diff(off).astype(np.int32)
+    rng = np.random.default_rng(5)
+    pi = rng.integers(0, 40, 3200).astype(np.int32)
+    pj = rng.integers(0, 40, 3200).astype(np.int32)
+    pi[:3], pj[:3] = 40, (0, 1, 2)          # the long sequence as X
+    pi[3:6], pj[3:6] = (3, 4, 5), 40        # and as Y
+    with Context(10, 2) as ctx:
+        expect = ctx.score_pairs(codes, off, pi, pj)
+    arrs = _dev_arrays(codes, off[:-1].copy(), lens, pi, pj)
+    for call in range(2):
+        arrs[-1].fill_(-7)
+        torch.cuda.synchronize()
+        assert _call(f, arrs, 32768) == NWG_OK
+        torch.cuda.synchronize()
+        assert np.array_equal(arrs[-1].cpu().numpy(), expect), f"call {call}: scores differ"
+
+
+def test_noalloc_skips_pairs_outside_the_declared_size():
+    # X longer than max_len, and an empty sequence on either side: INT_MIN,
+    # no scratch access; every other pair is scored as usual
+    import torch
+    f = _entry()
+    seqs = _set(105, 30, 1, 600)
+    codes, off = encode(seqs)
+    lens = np.diff(off).astype(np.int32)
+    start = off[:-1].copy()
+    # sequence 30: empty (length 0, starting at the end of the codes)
+    lens = np.append(lens, np.int32(0))
+    start = np.append(start, np.int64(off[-1]))
+    rng = np.random.default_rng(9)
+    pi = rng.integers(0, 31, 2500).astype(np.int32)
+    pj = rng.integers(0, 31, 2500).astype(np.int32)
+    pi[0], pj[0] = 30, 1
+    pi[1], pj[1] = 2, 30
+    max_len = 300
+    bad = (lens[pi] > max_len) | (lens[pi] == 0) | (lens[pj] == 0)
+    assert bad.sum() > 100 and (~bad).sum() > 100
+    with Context(10, 2) as ctx:
+        good = ctx.score_pairs(codes, off, pi[~bad], pj[~bad])
+    arrs = _dev_arrays(codes, start, lens, pi, pj)
+    torch.cuda.synchronize()
+    assert _call(f, arrs, max_len) == NWG_OK
+    torch.cuda.synchronize()
+    got = arrs[-1].cpu().numpy()
+    assert np.all(got[bad] == np.iinfo(np.int32).min)
+    assert np.array_equal(got[~bad], good)
+
+
+def test_noalloc_call_leaves_free_device_memory_unchanged():
+    # After the first call on the device (set-up, and the module's own load),
+    # a call takes no device memory: the free amount the driver reports is the
+    # same before and after it.
+    import torch
+    f = _entry()
+    seqs = _set(106, 50, 1, 500)
+    codes, off = encode(seqs)
+    lens = np.diff(off).astype(np.int32)
+    rng = np.random.default_rng(3)
+    pi = rng.integers(0, 50, 4000).astype(np.int32)
+    pj = rng.integers(0, 50, 4000).astype(np.int32)
+    arrs = _dev_arrays(codes, off[:-1].copy(), lens, pi, pj)
+    assert _call(f, arrs, int(lens.max())) == NWG_OK
+    torch.cuda.synchronize()
+    first = arrs[-1].cpu().numpy()
+    free0, _ = torch.cuda.mem_get_info()
+    arrs[-1].fill_(-7)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert _call(f, arrs, int(lens.max())) == NWG_OK
+    torch.cuda.synchronize()
+    free2, _ = torch.cuda.mem_get_info()
+    assert free1 == free0 and free2 == free1
+    assert np.array_equal(arrs[-1].cpu().numpy(), first)
