@@ -32,7 +32,7 @@ from mestrado_gb300 import synth  # noqa: E402
 import oracle_py  # noqa: E402
 from additive import random_tree_metric  # noqa: E402
 
-REF = os.environ.get("NWG_REFERENCE", "/root/reference")
+REF = os.environ.get("NWG_REFERENCE") or os.path.normpath(os.path.join(ROOT, os.pardir, "reference"))
 
 CASES = {
     # benchmark configuration 0: 64 sequences, one family, root 300

@@ -11,7 +11,7 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("NWG_REFERENCE", "/root/reference")
+from refsrc import REF
 
 pytestmark = pytest.mark.skipif(not os.path.isfile(os.path.join(REF, "SpeciesBlock.cpp")),
                                 reason="reference sources not present")
