@@ -92,6 +92,20 @@ typedef struct {
  * modified in place.  joins must hold n-1 records. */
 void nwo_nj(float* D, int n, nwo_join* joins, nwo_nj_stats* stats);
 
+typedef struct {
+  int64_t rebuilds;          /* row-sum and bin rebuilds                                          */
+  int64_t pq_triggers;       /* rebuilds started by the heap occupancy check                      */
+  int64_t out_of_range_bins; /* bin bounds the reference reads past its T vector (below 29 taxa)  */
+} nwo_nj_model_stats;
+
+/* Neighbor joining as SpeciesBlock::buildTree runs it (SpeciesBlock.cpp:
+ * 426-1343): bins, bin heaps, candidate list, the eight kept candidates and
+ * the prediction array, so that each join is valued in the rounding the
+ * reference applies to it, with the reference's own standard containers and
+ * algorithms (nj_model.cpp).  D (n x n, row-major float) is modified in place;
+ * joins must hold n-1 records. */
+void nwo_nj_model(float* D, int n, nwo_join* joins, nwo_nj_model_stats* stats);
+
 /* Progressive alignment along the guide tree (this build's definition: the
  * reference's AlignmentMatch::computeMSA, AlignmentMatch.cu:320-434, is an
  * empty loop -- parity unpinned).  Internal node n+k joins left[k] (X,

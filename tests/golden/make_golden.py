@@ -48,6 +48,10 @@ CASES = {
     # 100 sequences, each twice: 91 joins decided by the tie-break alone
     "dup200": lambda: synth.family(100, 80, ps=0.05, pi=0.005, seed=31).subset(
         [k for k in range(100) for _ in range(2)]),
+    # 100 sequences, each three times: the reference's bin heaps and its cut to
+    # eight candidates decide 58 joins (the exact argmin departs at join 22)
+    "dup300": lambda: synth.family(100, 80, ps=0.05, pi=0.005, seed=31).subset(
+        [k for k in range(100) for _ in range(3)]),
     # a tree metric (below) on 500 taxa: integer path lengths, exact q ties;
     # the sequences only give the FASTA its names
     "tree500": lambda: synth.family(500, 30, ps=0.05, pi=0.0, seed=13),

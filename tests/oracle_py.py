@@ -167,3 +167,27 @@ def nj(D: np.ndarray):
     dt = np.dtype([("i", "i4"), ("j", "i4"), ("node", "i4"), ("n", "i4"), ("d", "f4"), ("q", "f8"),
                    ("ti", "f8"), ("tj", "f8"), ("len_i", "f8"), ("len_j", "f8")])
     return np.array(rows, dtype=dt), {k: getattr(st, k) for k, _ in NJStats._fields_}
+
+
+class NJModelStats(ctypes.Structure):
+    _fields_ = [("rebuilds", ctypes.c_int64), ("pq_triggers", ctypes.c_int64),
+                ("out_of_range_bins", ctypes.c_int64)]
+
+
+def nj_model(D: np.ndarray):
+    """buildTree with its bins, bin heaps, candidate list and prediction array,
+    on the reference's own standard containers (oracle/nj_model.cpp): the
+    reference's joins, ties and roundings included.  Returns (joins
+    structured array, stats)."""
+    D = np.array(D, dtype=np.float32, copy=True, order="C")
+    n = D.shape[0]
+    joins = (Join * max(n - 1, 1))()
+    st = NJModelStats()
+    L = lib()
+    L.nwo_nj_model.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    L.nwo_nj_model(_p(D, ctypes.c_float), n, ctypes.cast(joins, ctypes.c_void_p),
+                   ctypes.cast(ctypes.byref(st), ctypes.c_void_p))
+    rows = [(j.i, j.j, j.node, j.n, j.d, j.q, j.ti, j.tj, j.len_i, j.len_j) for j in joins][: max(n - 1, 0)]
+    dt = np.dtype([("i", "i4"), ("j", "i4"), ("node", "i4"), ("n", "i4"), ("d", "f4"), ("q", "f8"),
+                   ("ti", "f8"), ("tj", "f8"), ("len_i", "f8"), ("len_j", "f8")])
+    return np.array(rows, dtype=dt), {k: getattr(st, k) for k, _ in NJModelStats._fields_}

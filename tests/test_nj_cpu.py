@@ -20,7 +20,7 @@ def golden_joins(case):
     return j
 
 
-@pytest.mark.parametrize("case", ["cfg0", "nj300", "nj1200", "dup200", "tree500"])
+@pytest.mark.parametrize("case", ["cfg0", "nj300", "nj1200", "dup200", "dup300", "tree500"])
 def test_newick_text_matches_reference(case):
     names, _ = read_fasta(os.path.join(GOLD, case, "input.fasta"))
     text = newick(golden_joins(case), names)
