@@ -175,7 +175,9 @@ typedef struct {
   int64_t pq_trigger_open;  /* heap-size rebuild checks that could not be excluded                */
   double device_ms;         /* device time of the join loop                                       */
   int32_t launches;
-  int32_t pad;
+  int32_t reference_identical; /* 1: no ambiguous step and no open heap-size check -- every join
+                                  is the one the reference's buildTree makes on this matrix;
+                                  0: at least one join may differ from the reference's (see below) */
 } nwg_nj_stats;
 
 /* Replaces SpeciesBlock::buildTree on one rank (SpeciesBlock.cpp:845-1343):
@@ -183,7 +185,19 @@ typedef struct {
  * leading dimension ld; the caller's matrix is not modified) in the
  * reference's order, with its FP32 matrix updates, FP64 row sums and
  * q = d*(n-2) - T_i - T_j, and its tie-break (larger max(i,j), then larger
- * min(i,j)).  joins must hold n-1 records.  n <= 8192. */
+ * min(i,j)).  joins must hold n-1 records.  n <= 8192.
+ *
+ * Each join is the exact argmin of q.  The reference instead values a pair
+ * as (d(n-2) - T_i) - T_j in its candidate list and as d(n-2) - (T_i + T_j)
+ * when it pops the pair from a bin heap, and cuts its candidates to eight
+ * with std::nth_element (SpeciesBlock.cpp:1019-1180).  When no other pair
+ * comes within those two roundings of the winner and at most four pairs tie
+ * exactly, both give the same join; otherwise the step is counted in
+ * stats.ambiguous_steps, and the reference's pick there depends on its heap
+ * layouts and on which tied candidates its library's cut keeps (duplicated
+ * sequences: tens of tied pairs).  stats.reference_identical is 1 exactly
+ * when no step was ambiguous, i.e. when the returned tree is guaranteed to be
+ * the reference's. */
 int nwg_nj(nwg_ctx* ctx, const float* D, int64_t ld, int n, nwg_join* joins, nwg_nj_stats* stats);
 
 /* Same with D already on the device (d_D). */
@@ -335,7 +349,7 @@ typedef struct {
   int32_t n;                   /* sequences                                        */
   int32_t status;              /* NWG_OK or the job's error                         */
   int32_t batch_jobs;          /* jobs in the batch it ran in                       */
-  int32_t pad;
+  int32_t nj_reference_identical; /* as nwg_nj_stats.reference_identical            */
   double queue_ms;             /* submit -> admitted to a batch                     */
   double latency_ms;           /* submit -> results on the host                     */
   int64_t cells;               /* DP cells of the job's off-diagonal pairs          */

@@ -157,7 +157,8 @@ class Join(ctypes.Structure):
 class NJStats(ctypes.Structure):
     _fields_ = [("ambiguous_steps", ctypes.c_int64), ("tie_steps", ctypes.c_int64),
                 ("rebuilds", ctypes.c_int64), ("pq_trigger_open", ctypes.c_int64),
-                ("device_ms", ctypes.c_double), ("launches", ctypes.c_int32), ("pad", ctypes.c_int32)]
+                ("device_ms", ctypes.c_double), ("launches", ctypes.c_int32),
+                ("reference_identical", ctypes.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
@@ -168,7 +169,7 @@ JOIN_DTYPE = [("i", "i4"), ("j", "i4"), ("node", "i4"), ("n", "i4"), ("d", "f4")
 
 class JobInfo(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int32), ("status", ctypes.c_int32), ("batch_jobs", ctypes.c_int32),
-                ("pad", ctypes.c_int32), ("queue_ms", ctypes.c_double), ("latency_ms", ctypes.c_double),
+                ("nj_reference_identical", ctypes.c_int32), ("queue_ms", ctypes.c_double), ("latency_ms", ctypes.c_double),
                 ("cells", ctypes.c_int64), ("nj_ambiguous_steps", ctypes.c_int64),
                 ("nj_tie_steps", ctypes.c_int64), ("nj_rebuilds", ctypes.c_int64)]
 

@@ -2318,6 +2318,7 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
   nwg_nj_stats stats;
   std::memset(&stats, 0, sizeof(stats));
   if (n == 1) {
+    stats.reference_identical = 1;
     if (st) *st = stats;
     return NWG_OK;
   }
@@ -2536,6 +2537,7 @@ int Ctx::nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, n
     stats.pq_trigger_open = (int64_t)dst[3];
     stats.rebuilds = (int64_t)dst[4];
   }
+  stats.reference_identical = stats.ambiguous_steps == 0 && stats.pq_trigger_open == 0;
   if (st) {
     float ms = 0;
     cudaEventElapsedTime(&ms, ev0, ev1);

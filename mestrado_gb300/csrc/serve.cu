@@ -576,6 +576,7 @@ int nwg_server_wait(nwg_server* srv, uint64_t job_id, int timeout_ms, float* D, 
     info->nj_ambiguous_steps = (int64_t)J->njst[0];
     info->nj_tie_steps = (int64_t)J->njst[1];
     info->nj_rebuilds = (int64_t)J->njst[4];
+    info->nj_reference_identical = J->njst[0] == 0 && J->njst[3] == 0;
   }
   const int st = J->status;
   // By key: the wait released the lock, and a submit on another thread may

@@ -40,6 +40,27 @@ def test_device_nj_matches_reference_tree(ctx, case):
     _same(joins, golden_joins(case))
     assert newick(joins, names) == open(os.path.join(d, "tree.nwk")).read()
     assert st["ambiguous_steps"] == 0 and st["pq_trigger_open"] == 0
+    assert st["reference_identical"] == 1
+
+
+def test_device_nj_flags_trees_the_reference_may_build_differently(ctx):
+    # dup300: 100 sequences three times.  The reference's bin heaps and its
+    # cut to eight candidates decide 58 joins, and its tree departs from the
+    # exact argmin at join 22 (tests/test_nj_model_cpu.py).  The device
+    # returns the exact-argmin tree, counts the ambiguous steps and reports
+    # the tree as not guaranteed to be the reference's.
+    d = os.path.join(GOLD, "dup300")
+    _, seqs = read_fasta(os.path.join(d, "input.fasta"))
+    D = ctx.score_all(seqs)
+    joins, st = ctx.nj(D, stats=True)
+    oj, ost = O.nj(D)
+    for a, b in zip(joins, oj):
+        assert (a["i"], a["j"], a["len_i"], a["len_j"], a["q"]) == (b["i"], b["j"], b["len_i"], b["len_j"], b["q"])
+    assert st["ambiguous_steps"] == ost["ambiguous_steps"] > 0
+    assert st["reference_identical"] == 0
+    ref = golden_joins("dup300")
+    assert [(int(a["i"]), int(a["j"])) for a in joins[:22]] == [(int(b["i"]), int(b["j"])) for b in ref[:22]]
+    assert (int(joins[22]["i"]), int(joins[22]["j"])) != (int(ref[22]["i"]), int(ref[22]["j"]))
 
 
 @pytest.mark.parametrize("seed,n", [(1, 2), (2, 3), (3, 17), (4, 64), (5, 257), (6, 600)])
@@ -67,6 +88,7 @@ def test_device_nj_ties_and_duplicates(ctx):
     for a, b in zip(joins, oj):
         assert (a["i"], a["j"], a["len_i"], a["len_j"]) == (b["i"], b["j"], b["len_i"], b["len_j"])
     assert st["tie_steps"] == ost["tie_steps"] and st["ambiguous_steps"] == ost["ambiguous_steps"]
+    assert st["reference_identical"] == (1 if st["ambiguous_steps"] == 0 else 0)
     rng = np.random.default_rng(0)
     M = rng.integers(0, 5, size=(30, 30)).astype(np.float32)
     M = np.triu(M, 1) + np.triu(M, 1).T

@@ -109,3 +109,18 @@ def test_model_equals_exact_argmin_where_unambiguous(kind, seed):
     for a, b in zip(joins, ex):
         assert (a["i"], a["j"], a["q"], a["ti"], a["tj"], a["len_i"], a["len_j"]) == \
                (b["i"], b["j"], b["q"], b["ti"], b["tj"], b["len_i"], b["len_j"])
+
+
+def test_exact_argmin_flags_where_reference_departs():
+    # dup300: the exact argmin counts ambiguous steps, and its tree departs
+    # from the reference's (golden) at join 22, where the model follows it
+    d = os.path.join(GOLD, "dup300")
+    _, seqs = read_fasta(os.path.join(d, "input.fasta"))
+    D = O.score_all(seqs, threads=os.cpu_count() or 2)
+    ex, st = O.nj(D)
+    ref = golden_joins("dup300")
+    assert st["ambiguous_steps"] > 0
+    first = next(t for t in range(len(ref)) if (ex[t]["i"], ex[t]["j"]) != (ref[t]["i"], ref[t]["j"]))
+    assert first == 22
+    joins, _ = O.nj_model(D)
+    _same(joins, ref)

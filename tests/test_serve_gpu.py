@@ -59,7 +59,7 @@ def test_serving_mix_equals_alone_and_context(ctx):
         assert np.array_equal(Dm, D)
         if len(S) > 1:
             _same_joins(Jm, ctx.nj(D))
-        assert im["nj_ambiguous_steps"] == 0
+        assert im["nj_ambiguous_steps"] == 0 and im["nj_reference_identical"] == 1
 
 
 def test_serving_batch_with_both_join_forms(ctx):
@@ -107,6 +107,7 @@ def test_serving_wide_exact_ties():
         _same_joins(J, oj)
         assert info["nj_ambiguous_steps"] == ost["ambiguous_steps"]
         assert info["nj_tie_steps"] == ost["tie_steps"]
+        assert info["nj_reference_identical"] == (1 if ost["ambiguous_steps"] == 0 else 0)
 
 
 def test_serving_admission_by_footprint(ctx):
