@@ -534,9 +534,16 @@ def main():
     # kernel choice per length class (cached per device after the first run)
     tuning = ctx.autotune()
 
-    # roofline denominator: the bare DPX cell update on every SM
-    peak16 = ctx.dpx_peak(True)
-    peak32 = ctx.dpx_peak(False)
+    # roofline denominator: the ALU pipe, which executes the DPX max
+    # operations, at its full rate.  The int32 cell-update form 2 (4 DPX + 1
+    # add per cell, registers only, every SM) keeps that pipe 99.98 % busy
+    # (ncu), so its cells/s x 4 is the pipe's lane-op rate in this run; the
+    # leanest cell update needs 1.5 ALU lane-ops per int16x2 cell (2 viaddmax +
+    # 1 vimax3 per two-cell word) and 3 per int32 cell.
+    alu_lane_ops = ctx.dpx_peak(False, form=2) * 4.0
+    peak16 = alu_lane_ops / 1.5
+    peak32 = alu_lane_ops / 3.0
+    micro16 = ctx.dpx_peak(True)    # the fastest complete cell update, for reference
 
     for _ in range(args.warmup):
         ctx.score_all_dev(d_codes.data_ptr(), off, d_D.data_ptr(), n, MODE_BATCHED)
@@ -645,9 +652,12 @@ def main():
                 "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
                 "kernel": kname,
                 "launch_ms": dom["ms"], "launch_cells": dom["cells"],
-                "peak_source": "nwg_dpx_peak: the 5-instruction cell update (faster of the two forms the "
-                               "kernels use) on every SM, registers only, measured in this run",
-                "peak_int32_gcups": peak32 / 1e9}
+                "peak_source": "ALU-pipe ceiling measured in this run: nwg_dpx_peak_form(int32, form 2) "
+                               "saturates the ALU pipe (ncu 99.98 %), x 4 ALU lane-ops per cell = the pipe's "
+                               "lane-op rate, / 1.5 ALU lane-ops per int16x2 cell of the leanest update",
+                "peak_int32_gcups": peak32 / 1e9,
+                "alu_lane_ops_per_s": alu_lane_ops,
+                "cell_update_microbenchmark_gcups": micro16 / 1e9}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": tot_s_max / args.steps * 1e3, "higher_is_better": True,
