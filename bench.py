@@ -13,7 +13,8 @@ second) with codes and matrix resident in HBM; e2e = the same metric through
 the host-buffer C ABI call (nwg_score_all: codes host->device, matrix
 device->host inside the timed region).  The line also carries the serving
 run (Poisson job arrivals, continuous batching): p50/p99 job latency and
-sustained GCUPS beside the same jobs run one by one, and the configuration-3
+sustained GCUPS beside the same jobs run one by one, then a sweep of the
+arrival rate (500-4000 jobs/s) to where the server stops keeping up, and the configuration-3
 pipeline (matrix -> neighbor joining -> cherry traceback of 8,000 sequences,
 checked against the reference's own tree) with the NJ and traceback
 rooflines.  --impl reference times the
@@ -195,24 +196,12 @@ def cpu_baseline(S, target_s: float, threads: int, seed: int = 7):
             "one_core": {"value": c1 / d1 / 1e9, "pairs": len(qi), "seconds": d1}}
 
 
-def serving_leg(seconds: float, rate: float = 200.0, sample_jobs: int = 200):
-    """The serving workload: Poisson arrivals at `rate` jobs/s for `seconds`
-    (each job a family of log-uniform 8-512 sequences, lognormal root length
-    median 250, sigma 0.5, clipped 30-2000), submitted at their arrival times
-    to one Server; latency = submit -> matrix and tree on the host.  Beside it,
-    the first `sample_jobs` jobs run job by job through a context (plain
-    per-pair form, and the batched form), scoring + NJ, host buffers."""
+def _serve_arrivals(srv, jobs, keep=()):
+    """Submit `jobs` ((arrival_s, seqs) pairs) to `srv` at their arrival times
+    and wait for each from a second thread; returns (infos, kept results,
+    wall seconds from the first arrival, largest submit lag)."""
     import queue
-
-    from mestrado_gb300 import MODE_BATCHED, MODE_PLAIN, Context, Server, synth
-    count = max(1, int(seconds * rate))
-    jobs = synth.serving_jobs(count, rate)
-    warm = synth.serving_jobs(16, rate, seed=99)
-    cells = np.array([S.cells() for _, S in jobs], dtype=np.float64)
-    check = set(np.random.default_rng(5).choice(count, size=min(count, 24), replace=False).tolist())
-    srv = Server(10, 2, hbm_budget=16 << 30, max_batch_jobs=256)
-    for _, S in warm:
-        srv.wait(srv.submit(S), len(S))
+    count = len(jobs)
     q: "queue.Queue" = queue.Queue()
     infos = [None] * count
     kept = {}
@@ -222,7 +211,7 @@ def serving_leg(seconds: float, rate: float = 200.0, sample_jobs: int = 200):
             k, jid = q.get()
             D, J, info = srv.wait(jid, len(jobs[k][1]))
             infos[k] = info
-            if k in check:
+            if k in keep:
                 kept[k] = (D, J)
 
     th = threading.Thread(target=waiter)
@@ -237,7 +226,57 @@ def serving_leg(seconds: float, rate: float = 200.0, sample_jobs: int = 200):
             lag = max(lag, -dt)
         q.put((k, srv.submit(S)))
     th.join()
-    wall = time.perf_counter() - t0
+    return infos, kept, time.perf_counter() - t0, lag
+
+
+def serving_sweep(rates=(500.0, 1000.0, 2000.0, 3000.0, 4000.0), seconds: float = 5.0):
+    """The serving workload at higher Poisson rates, `seconds` of arrivals
+    each (one Server, warmed): per rate the latency percentiles, the mean
+    batch size and the sustained against the offered cell rate.  A rate is
+    kept up with when the last job returns within a second of the last
+    arrival and sustained >= 0.95 x offered."""
+    from mestrado_gb300 import Server, synth
+    out = []
+    srv = Server(10, 2, hbm_budget=16 << 30, max_batch_jobs=256)
+    for _, S in synth.serving_jobs(16, 200.0, seed=99):
+        srv.wait(srv.submit(S), len(S))
+    for rate in rates:
+        jobs = synth.serving_jobs(max(1, int(seconds * rate)), rate, seed=1000 + int(rate))
+        cells = float(sum(S.cells() for _, S in jobs))
+        infos, _, wall, lag = _serve_arrivals(srv, jobs)
+        lat = np.array([i["latency_ms"] for i in infos])
+        batch = np.array([i["batch_jobs"] for i in infos])
+        span = jobs[-1][0]
+        offered = cells / span / 1e9
+        sustained = cells / wall / 1e9
+        out.append({"rate_jobs_per_s": rate, "jobs": len(jobs),
+                    "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                                   "max": float(lat.max())},
+                    "batch_jobs_mean": float(batch.mean()), "batch_jobs_max": int(batch.max()),
+                    "offered_gcups": offered, "sustained_gcups": sustained,
+                    "kept_up": bool(wall - span < 1.0 and sustained >= 0.95 * offered),
+                    "submit_lag_max_s": lag, "ok": all(i["status"] == 0 for i in infos)})
+    srv.close()
+    return out
+
+
+def serving_leg(seconds: float, rate: float = 200.0, sample_jobs: int = 200, sweep: bool = True):
+    """The serving workload: Poisson arrivals at `rate` jobs/s for `seconds`
+    (each job a family of log-uniform 8-512 sequences, lognormal root length
+    median 250, sigma 0.5, clipped 30-2000), submitted at their arrival times
+    to one Server; latency = submit -> matrix and tree on the host.  Beside it,
+    the first `sample_jobs` jobs run job by job through a context (plain
+    per-pair form, and the batched form), scoring + NJ, host buffers."""
+    from mestrado_gb300 import MODE_BATCHED, MODE_PLAIN, Context, Server, synth
+    count = max(1, int(seconds * rate))
+    jobs = synth.serving_jobs(count, rate)
+    warm = synth.serving_jobs(16, rate, seed=99)
+    cells = np.array([S.cells() for _, S in jobs], dtype=np.float64)
+    check = set(np.random.default_rng(5).choice(count, size=min(count, 24), replace=False).tolist())
+    srv = Server(10, 2, hbm_budget=16 << 30, max_batch_jobs=256)
+    for _, S in warm:
+        srv.wait(srv.submit(S), len(S))
+    infos, kept, wall, lag = _serve_arrivals(srv, jobs, check)
     srv.close()
     lat = np.array([i["latency_ms"] for i in infos])
     qms = np.array([i["queue_ms"] for i in infos])
@@ -289,6 +328,8 @@ def serving_leg(seconds: float, rate: float = 200.0, sample_jobs: int = 200):
         "job_by_job": {"jobs": m, **jbj},
         "serving_over_plain_job_by_job": served / jbj["plain"]["gcups_with_nj"],
         "exact": parity, "checked_jobs": len(kept),
+        "reference_identical_jobs": int(sum(i["nj_reference_identical"] for i in infos)),
+        "rate_sweep": serving_sweep() if sweep else None,
     }
 
 
@@ -499,6 +540,8 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=60.0,
                     help="length of the serving run (Poisson arrivals at 200 jobs/s, configuration 4: "
                          "60 s); 0 skips it")
+    ap.add_argument("--no-serve-sweep", action="store_true",
+                    help="skip the sweep of the serving arrival rate (500-4000 jobs/s, 5 s each)")
     ap.add_argument("--quick", action="store_true",
                     help="device-resident timing only (no e2e, plain, CPU or parity legs); for profiling runs")
     args = ap.parse_args()
@@ -639,7 +682,7 @@ def main():
     if rank != 0:
         return
     config1 = None if args.no_plain else config1_leg()
-    serving = serving_leg(args.serve_seconds) if args.serve_seconds > 0 else None
+    serving = serving_leg(args.serve_seconds, sweep=not args.no_serve_sweep) if args.serve_seconds > 0 else None
     pipeline = None if args.no_pipeline else pipeline_leg()
     roof = None
     if dom is not None:
