@@ -525,6 +525,54 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def run_shard(args, world, rank, local):
+    """--shard: ONE configuration-2 matrix split over the ranks (strong
+    scaling): rank k scores its cell-balanced row block against the columns
+    from its first row on (nwg_score_block), the blocks are all-gathered
+    over the process group (host buffers) and mirrored into the full matrix
+    on every rank (mestrado_gb300/shard.py).  value = the matrix's cells per
+    step / the slowest rank's step time; the timed region includes the
+    host-side gather, so value and e2e are the same measurement."""
+    import torch
+    torch.cuda.set_device(local)
+    from mestrado_gb300 import Context, shard, synth
+    S = synth.generate(synth.config_spec(CONFIG), replica_seed(0))
+    if args.subset:
+        S = S.subset(range(min(args.subset, len(S))))
+    seqs = [S[i] for i in range(len(S))]
+    n, cells = len(seqs), S.cells()
+    ctx = Context(10, 2)
+    ctx.autotune()
+    for _ in range(args.warmup):
+        D = shard.sharded_score_all(ctx, seqs, rank, world, device="cpu")
+    clocks = ClockSampler(local)
+    clocks.start()
+    _barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        D = shard.sharded_score_all(ctx, seqs, rank, world, device="cpu")
+    _barrier(world)
+    t = _max_over_ranks(world, time.perf_counter() - t0)
+    clk = clocks.stop()
+    b = shard.tile_plan([len(s) for s in seqs], world)
+    value = cells * args.steps / t / 1e9
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "strong", "vs_baseline": None, "dtype": "int16x2+int32", "data": "synthetic",
+            "config": {"workload": f"configuration {CONFIG}: one {n} x {n} matrix split over {world} rank(s) by "
+                                   "cell-balanced row blocks, all-gathered on the host",
+                       "cells_per_step": cells, "parallelism": f"row-block split over {world} GPU(s)",
+                       "row_bounds": [int(x) for x in b],
+                       "block_cells": [float(c) for c in shard.block_cells([len(s) for s in seqs], b)]},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": int(sum(len(s) for s in seqs)),
+                    "d2h_bytes_per_step": int(4 * (b[rank + 1] - b[rank]) * (n - b[rank]))},
+            "matrix_symmetric": bool(np.array_equal(D, D.T)),
+            "gpu_launches": None, "clocks": clk}), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -540,6 +588,8 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=60.0,
                     help="length of the serving run (Poisson arrivals at 200 jobs/s, configuration 4: "
                          "60 s); 0 skips it")
+    ap.add_argument("--shard", action="store_true",
+                    help="N>1: split ONE configuration-2 matrix over the ranks (strong scaling) instead of replicas")
     ap.add_argument("--no-serve-sweep", action="store_true",
                     help="skip the sweep of the serving arrival rate (500-4000 jobs/s, 5 s each)")
     ap.add_argument("--quick", action="store_true",
@@ -548,6 +598,9 @@ def main():
     world, rank, local = _dist()
     if args.impl == "reference":
         run_reference(args, world, rank)
+        return
+    if args.shard:
+        run_shard(args, world, rank, local)
         return
 
     import torch
