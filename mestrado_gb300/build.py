@@ -36,8 +36,8 @@ def _nvcc() -> str:
 
 
 def _headers():
-    return glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(INCLUDE, "*.h")) + \
-        glob.glob(os.path.join(INCLUDE, "*.hpp"))
+    return glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) + \
+        glob.glob(os.path.join(INCLUDE, "*.h")) + glob.glob(os.path.join(INCLUDE, "*.hpp"))
 
 
 def _stale(obj: str, src: str) -> bool:

@@ -307,7 +307,10 @@ int nwg_ctx_create(int gap_open, int gap_ext, const int8_t* sub, nwg_ctx** out) 
     return rc;
   }
   c->stream = c->own_stream;
-  for (int k = 0; k < nwg::kTuneClasses; ++k) c->tune[k] = nwg::kDefaultTune[k];
+  for (int k = 0; k < nwg::kTuneClasses; ++k) {
+    c->tune[k] = nwg::kDefaultTune[k];
+    c->tune_wave[k] = nwg::kDefaultTuneWave[k];
+  }
   for (int k = 0; k < 2; ++k) {
     cudaStream_t b;
     cudaEvent_t e;

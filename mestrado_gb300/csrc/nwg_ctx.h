@@ -33,8 +33,8 @@ const char* letter_order();
 
 struct TuneChoice {
   int R;   // rows per lane (4, 8, 12, 16, 20, 24, 32)
-  int V;   // register layout (0, 1, 2)
-  int W;   // lanes per wavefront (32, 16, 8): band of W*R rows
+  int V;   // register layout (0 to 5)
+  int W;   // lanes per wavefront (32, 16, 8): band of W*R rows; 1: one pair per thread, bands of R rows
 };
 // The same band on full-width fronts, for groups that run on int32 lanes
 // (the narrow fronts exist for int16x2 lanes only).
@@ -50,8 +50,16 @@ constexpr int kTuneClasses = NWG_TUNE_CLASSES;
 // Upper bound of the Y rows of each class; the last class takes every longer Y.
 constexpr int kClassRows[kTuneClasses] = {64,  96,  128, 160, 192, 224, 256,  320,
                                           384, 448, 512, 640, 768, 1024, 1536, 1 << 30};
+// Defaults before tuning (the table measured on a GB300): one pair per
+// thread (W = 1) for the classes up to 96 rows, wavefronts above.
 constexpr TuneChoice kDefaultTune[kTuneClasses] = {
-    {4, 2, 32},  {4, 2, 32},  {4, 2, 32},  {8, 0, 32},  {8, 0, 32},  {8, 0, 32},  {8, 0, 32},  {12, 0, 32},
+    {32, 4, 1},  {32, 4, 1},  {4, 2, 32},  {8, 0, 32},  {8, 0, 32},  {8, 0, 32},  {8, 0, 32},  {12, 0, 32},
+    {12, 0, 32}, {16, 2, 32}, {16, 2, 32}, {20, 2, 32}, {24, 2, 32}, {32, 2, 32}, {24, 2, 32}, {24, 2, 32}};
+// The best wavefront (W >= 8) per class before tuning, for latency-bound
+// callers: one pair per thread needs 256 X per CTA and streams a Y in bands,
+// so it wins on throughput over many X but lengthens a small job.
+constexpr TuneChoice kDefaultTuneWave[kTuneClasses] = {
+    {8, 5, 8},   {12, 3, 8},  {4, 2, 32},  {8, 0, 32},  {8, 0, 32},  {8, 0, 32},  {8, 0, 32},  {12, 0, 32},
     {12, 0, 32}, {16, 2, 32}, {16, 2, 32}, {20, 2, 32}, {24, 2, 32}, {32, 2, 32}, {24, 2, 32}, {24, 2, 32}};
 int tune_class(int rows);
 
@@ -72,10 +80,18 @@ struct Ctx {
   // Kernel choice per length class of the Y rows (rows <= kClassRows[k]):
   // rows per lane and register layout, set by the autotuner (tune.cu).
   TuneChoice tune[kTuneClasses];
+  // The fastest wavefront (W >= 8) per class, for the serving loop, whose
+  // small jobs are latency-bound (one pair per thread lengthens them).
+  TuneChoice tune_wave[kTuneClasses];
   // The choice for Y groups of this many rows; layout 4 is exact only when
   // go >= ge and falls back to layout 2 otherwise.
   TuneChoice choice(int rows) const {
     TuneChoice t = tune[tune_class(rows)];
+    if (t.V == 4 && go < ge) t.V = 2;
+    return t;
+  }
+  TuneChoice choice_wave(int rows) const {
+    TuneChoice t = tune_wave[tune_class(rows)];
     if (t.V == 4 && go < ge) t.V = 2;
     return t;
   }

@@ -180,7 +180,7 @@ int Server::launch_batch(Slot& S) {
     const int certain = maxs > 0 ? c.i16.max_h / maxs : 1 << 30;
     for (int y = 0; y < n;) {
       const int gyi = (int)base + y;
-      const TuneChoice tc = c.choice(len[gyi]);
+      const TuneChoice tc = c.choice_wave(len[gyi]);   // latency first: wavefronts only
       if (!long_set && len[gyi] <= certain) {
         const int y2 = y + 1 < n ? gyi + 1 : -1;
         const int last = y2 >= 0 ? y + 1 : y;

@@ -4,8 +4,10 @@
 // For class k a probe workload is built from uniform random residues: 128 Y
 // sequences of the class's representative length and enough X sequences
 // (10% longer) for ~2e10 cells, scored in block mode so every pair lands in
-// that class.  Each candidate (R, V) runs once to warm up and once timed with
-// CUDA events; the fastest wins.  The table is written to a cache file per
+// that class.  Each candidate (R, V, W) runs once to warm up and once timed
+// with CUDA events; the fastest wins.  Candidates: wavefronts of W = 32, 16
+// or 8 lanes whose band holds the class in one to three bands, and, for the
+// classes up to 512 rows, one pair per thread (W = 1, bands of 16-32 rows).  The table is written to a cache file per
 // device (name + SM count) and read back by later contexts.
 #include <sys/stat.h>
 
@@ -48,7 +50,7 @@ const int kCandR[] = {4, 8, 12, 16, 20, 24, 32};
 // probe holds every Y of the class); the open last class probes 2000 rows.
 int representative_rows(int k) { return k == kTuneClasses - 1 ? 2000 : kClassRows[k]; }
 
-const char kCacheTag[] = "nwgpu-tune-3";
+const char kCacheTag[] = "nwgpu-tune-5";
 
 }  // namespace
 
@@ -58,15 +60,17 @@ bool Ctx::tune_from_cache(nwg_tune_result* res) {
   FILE* f = std::fopen(path.c_str(), "r");
   if (!f) return false;
   int ok = 0;
-  TuneChoice t[kTuneClasses];
+  TuneChoice t[kTuneClasses], tw[kTuneClasses];
   double g[kTuneClasses];
   char tag[32] = {0};
   if (std::fscanf(f, "%31s", tag) == 1 && std::strcmp(tag, kCacheTag) == 0) {
     for (int k = 0; k < kTuneClasses; ++k) {
-      int kk, R, V, W;
+      int kk, R, V, W, Rw, Vw, Ww;
       double gc;
-      if (std::fscanf(f, "%d %d %d %d %lf", &kk, &R, &V, &W, &gc) == 5 && kk == k && wave_exists(R, 2, V, W)) {
+      if (std::fscanf(f, "%d %d %d %d %lf %d %d %d", &kk, &R, &V, &W, &gc, &Rw, &Vw, &Ww) == 8 && kk == k &&
+          wave_exists(R, 2, V, W) && Ww >= 8 && wave_exists(Rw, 2, Vw, Ww)) {
         t[k] = {R, V, W};
+        tw[k] = {Rw, Vw, Ww};
         g[k] = gc;
         ++ok;
       }
@@ -76,6 +80,7 @@ bool Ctx::tune_from_cache(nwg_tune_result* res) {
   if (ok != kTuneClasses) return false;
   for (int k = 0; k < kTuneClasses; ++k) {
     tune[k] = t[k];
+    tune_wave[k] = tw[k];
     if (res) {
       res->rows_per_lane[k] = t[k].R;
       res->variant[k] = t[k].V;
@@ -137,12 +142,17 @@ int Ctx::autotune(bool force, nwg_tune_result* out) {
       dD = (float*)((char*)probe.p + ((total + 255) / 256) * 256);
     }
     if ((rc = cuda(cudaMemcpy(dcodes, codes.data(), total, cudaMemcpyHostToDevice), "autotune upload"))) break;
-    double best = -1.0;
-    TuneChoice pick = kDefaultTune[k];
-    for (int W : {32, 16, 8})
+    double best = -1.0, best_wave = -1.0;
+    TuneChoice pick = kDefaultTune[k], pick_wave = kDefaultTuneWave[k];
+    for (int W : {32, 16, 8, 1})
     for (int R : kCandR) {
       const int band = W * R;
-      if (band * 3 < Ly || band > 2 * Ly + 128) continue;   // at most 3 bands, at most ~half idle
+      if (W == 1) {
+        // one pair per thread: bands of R rows; for the classes up to 512 rows
+        if (R < 16 || Ly > 512) continue;
+      } else if (band * 3 < Ly || band > 2 * Ly + 128) {
+        continue;   // at most 3 bands, at most ~half idle
+      }
       for (int V = 0; V <= 5; ++V) {
         if (!wave_exists(R, 2, V, W) || (V == 4 && go < ge)) continue;
         tune[k] = {R, V, W};
@@ -163,10 +173,15 @@ int Ctx::autotune(bool force, nwg_tune_result* out) {
           best = g;
           pick = {R, V, W};
         }
+        if (W >= 8 && g > best_wave) {
+          best_wave = g;
+          pick_wave = {R, V, W};
+        }
       }
       if (rc) break;
     }
     tune[k] = pick;
+    tune_wave[k] = pick_wave;
     res.rows_per_lane[k] = pick.R;
     res.variant[k] = pick.V;
     res.lanes[k] = pick.W;
@@ -177,7 +192,10 @@ int Ctx::autotune(bool force, nwg_tune_result* out) {
   use_graphs = saved_graphs;
   ++tune_version;
   if (rc) {
-    for (int k = 0; k < kTuneClasses; ++k) tune[k] = kDefaultTune[k];
+    for (int k = 0; k < kTuneClasses; ++k) {
+      tune[k] = kDefaultTune[k];
+      tune_wave[k] = kDefaultTuneWave[k];
+    }
     return rc;
   }
   tuned = true;
@@ -186,7 +204,8 @@ int Ctx::autotune(bool force, nwg_tune_result* out) {
   if (FILE* f = std::fopen(path.c_str(), "w")) {
     std::fprintf(f, "%s\n", kCacheTag);
     for (int k = 0; k < kTuneClasses; ++k)
-      std::fprintf(f, "%d %d %d %d %.3f\n", k, tune[k].R, tune[k].V, tune[k].W, res.gcups[k]);
+      std::fprintf(f, "%d %d %d %d %.3f %d %d %d\n", k, tune[k].R, tune[k].V, tune[k].W, res.gcups[k],
+                   tune_wave[k].R, tune_wave[k].V, tune_wave[k].W);
     std::fclose(f);
   }
   if (out) *out = res;
@@ -206,7 +225,11 @@ extern "C" int nwg_set_tuning_lanes(nwg_ctx* ctx, const int32_t* rows_per_lane, 
   nwg::Ctx* c = reinterpret_cast<nwg::Ctx*>(ctx);
   for (int k = 0; k < nwg::kTuneClasses; ++k)
     if (!nwg::wave_exists(rows_per_lane[k], 2, variant[k], lanes ? lanes[k] : 32)) return NWG_ERR_INVALID;
-  for (int k = 0; k < nwg::kTuneClasses; ++k) c->tune[k] = {rows_per_lane[k], variant[k], lanes ? lanes[k] : 32};
+  for (int k = 0; k < nwg::kTuneClasses; ++k) {
+    c->tune[k] = {rows_per_lane[k], variant[k], lanes ? lanes[k] : 32};
+    // a forced table drives the serving loop too where it names wavefronts
+    if (c->tune[k].W >= 8) c->tune_wave[k] = c->tune[k];
+  }
   ++c->tune_version;
   c->tuned = true;
   return NWG_OK;

@@ -190,6 +190,28 @@ __device__ __forceinline__ void queue_rerun(const WaveArgs& a, int i, int y) {
   if (k < (unsigned long long)a.rerun_cap) a.rerun[k] = make_int2(i, y);
 }
 
+// Shared-memory score profile of one band: per letter, Q = R/4 groups of
+// four rows, each group one uint4 per front lane.  With W = 1 (one pair per
+// thread) the 32 lanes of a warp read different letters at once, so each
+// letter's row of groups is padded by one uint4 to spread them over the banks.
+template <int R, int W>
+struct Profile {
+  static constexpr int Q = R / 4;
+  static constexpr int kLetterStride = W == 1 ? Q + 1 : Q * W;        // uint4 per letter
+  static constexpr int kWords = kLetters * kLetterStride * 4;         // 32-bit words
+  static constexpr size_t kBytes = sizeof(uint32_t) * (size_t)kWords;
+  static __device__ __forceinline__ int index(int x, int row) {       // word of (letter, band row)
+    const int k = row / R, r = row - k * R;
+    return ((x * kLetterStride + (r >> 2) * W + k)) * 4 + (r & 3);
+  }
+};
+
+// Words between the band-boundary entries of consecutive columns of one
+// front: with W = 1 the CTA's 256 fronts interleave column by column, so a
+// warp's 32 fronts read and write 32 consecutive words per column.
+template <int W>
+constexpr int scratch_stride() { return W == 1 ? kWaveThreads : 1; }
+
 template <int V>
 struct Layout {
   static constexpr int K = V == 5 ? 2 : 1;    // X per front
@@ -356,6 +378,8 @@ __device__ __forceinline__ void wave_band(const WaveArgs& a, int sl, int b, int 
   // E[r][-1] = F[-1][c] = -32768 + ge; layouts 2 and 4 keep them shifted by go
   const uint32_t SENT = L::splat(kShortMin + a.ge + ((VL == 2 || VL == 4) ? a.go : 0));
 
+  constexpr int SST = scratch_stride<W>();
+  constexpr int LS = Profile<R, W>::kLetterStride;
   BandState<R, P, VL> s[K];
   const int rowbase = b * BAND + sl * R;
   const int gsh = VL == 3 ? a.go : 0;               // layout 3 carries T = H - go instead of H
@@ -379,8 +403,8 @@ __device__ __forceinline__ void wave_band(const WaveArgs& a, int sl, int b, int 
     hprev[k] = L::splat(-a.ge * rowbase - gsh);     // H[rowbase-1][-1]: diag of column 0
     hbot[k] = fbot[k] = 0;
     work[k] = Lx[k] > 0;
-    rd[k] = scratch + (size_t)k * 4 * a.scratch_cols + ((b + 1) & 1) * 2 * a.scratch_cols;   // band b-1
-    wr[k] = scratch + (size_t)k * 4 * a.scratch_cols + (b & 1) * 2 * a.scratch_cols;
+    rd[k] = scratch + ((size_t)k * 4 * a.scratch_cols + ((b + 1) & 1) * 2 * a.scratch_cols) * SST;   // band b-1
+    wr[k] = scratch + ((size_t)k * 4 * a.scratch_cols + (b & 1) * 2 * a.scratch_cols) * SST;
     xnext[k] = (sl == 0 && work[k]) ? (int)X[k][0] : 0;
   }
   uint32_t hb = L::splat(-a.ge - gsh);              // H[-1][c] of the column lane 0 works on (band 0)
@@ -394,8 +418,13 @@ __device__ __forceinline__ void wave_band(const WaveArgs& a, int sl, int b, int 
     bool on[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-      hin[k] = __shfl_up_sync(0xffffffffu, hbot[k], 1, W);
-      fin[k] = __shfl_up_sync(0xffffffffu, fbot[k], 1, W);
+      if constexpr (W > 1) {
+        hin[k] = __shfl_up_sync(0xffffffffu, hbot[k], 1, W);
+        fin[k] = __shfl_up_sync(0xffffffffu, fbot[k], 1, W);
+      } else {
+        hin[k] = hbot[k];   // every lane is lane 0 of its own front: read from the band above below
+        fin[k] = fbot[k];
+      }
       xl[k] = xnext[k];
       if (kChecked) {
         if (c + 1 >= 0 && c + 1 < Lx[k]) xnext[k] = X[k][c + 1];
@@ -404,8 +433,8 @@ __device__ __forceinline__ void wave_band(const WaveArgs& a, int sl, int b, int 
       }
       on[k] = kChecked ? (c >= 0 && c < Lx[k]) : ((W == 32 && K == 1) || work[k]);
       if (on[k] && sl == 0) {
-        hin[k] = top ? hb : (uint32_t)rd[k][2 * c];
-        fin[k] = top ? SENT : (uint32_t)rd[k][2 * c + 1];
+        hin[k] = top ? hb : (uint32_t)rd[k][(size_t)(2 * c) * SST];
+        fin[k] = top ? SENT : (uint32_t)rd[k][(size_t)(2 * c + 1) * SST];
       }
     }
     if (!kChecked || c >= 0) hb = L::add(hb, NGEA);
@@ -417,7 +446,7 @@ __device__ __forceinline__ void wave_band(const WaveArgs& a, int sl, int b, int 
         uint32_t f[2] = {fin[0], fin[1]};
         hprev[0] = hin[0];
         hprev[1] = hin[1];
-        strip_column_pair<R, P, W>(s, pl + clamp_code(xl[0]) * (Q * W), pl + clamp_code(xl[1]) * (Q * W), diag, hin,
+        strip_column_pair<R, P, W>(s, pl + clamp_code(xl[0]) * LS, pl + clamp_code(xl[1]) * LS, diag, hin,
                                    f, NGE, NGO);
         fbot[0] = f[0];
         fbot[1] = f[1];
@@ -432,7 +461,7 @@ __device__ __forceinline__ void wave_band(const WaveArgs& a, int sl, int b, int 
         if (!on[k]) continue;
         const uint32_t diag = hprev[k];
         hprev[k] = hin[k];
-        fbot[k] = strip_column<R, P, VL, W>(s[k], pl + clamp_code(xl[k]) * (Q * W), diag, hin[k], fin[k], NGE, NGO,
+        fbot[k] = strip_column<R, P, VL, W>(s[k], pl + clamp_code(xl[k]) * LS, diag, hin[k], fin[k], NGE, NGO,
                                             NGOP);
         hbot[k] = s[k].H[R - 1];
       }
@@ -441,8 +470,8 @@ __device__ __forceinline__ void wave_band(const WaveArgs& a, int sl, int b, int 
 #pragma unroll
       for (int k = 0; k < K; ++k)
         if (on[k]) {
-          wr[k][2 * c] = (int32_t)hbot[k];
-          wr[k][2 * c + 1] = (int32_t)fbot[k];
+          wr[k][(size_t)(2 * c) * SST] = (int32_t)hbot[k];
+          wr[k][(size_t)(2 * c + 1) * SST] = (int32_t)fbot[k];
         }
     }
   };
@@ -490,8 +519,9 @@ __global__ void __launch_bounds__(kWaveThreads, (MinBlocks<R, P, V>::value)) wav
   constexpr int BAND = W * R;
   constexpr int Q = R / 4;
   static_assert(R % 4 == 0, "rows per lane must be a multiple of 4");
-  static_assert(W == 8 || W == 16 || W == 32, "front width");
-  extern __shared__ __align__(16) uint32_t prof[];   // [letter][Q][front lane][4]
+  static_assert(W == 1 || W == 8 || W == 16 || W == 32, "front width");
+  static_assert(W > 1 || K == 1, "one pair per thread holds one X per front");
+  extern __shared__ __align__(16) uint32_t prof[];   // Profile<R, W>: [letter][Q][front lane][4]
   __shared__ int8_t s_sub[kLetters * kLetters];
   __shared__ long long s_job;
 
@@ -500,8 +530,11 @@ __global__ void __launch_bounds__(kWaveThreads, (MinBlocks<R, P, V>::value)) wav
   const int sl = lane % W;                 // lane within the front
   const int seg = lane / W;                // front within the warp
   for (int e = threadIdx.x; e < kLetters * kLetters; e += blockDim.x) s_sub[e] = a.sub[e];
+  // band-boundary scratch of the front: its own block of 4 x scratch_cols
+  // words per X, or (W = 1) one column of the CTA's interleaved block
   int32_t* scratch =
-      a.scratch + ((size_t)(blockIdx.x * kWaveWarps + warp) * S + seg) * K * 4 * (size_t)a.scratch_cols;
+      W == 1 ? a.scratch + (size_t)blockIdx.x * kWaveThreads * K * 4 * (size_t)a.scratch_cols + threadIdx.x
+             : a.scratch + ((size_t)(blockIdx.x * kWaveWarps + warp) * S + seg) * K * 4 * (size_t)a.scratch_cols;
 
   for (;;) {
     __syncthreads();
@@ -582,7 +615,7 @@ __global__ void __launch_bounds__(kWaveThreads, (MinBlocks<R, P, V>::value)) wav
         } else {
           w = (uint32_t)sa;
         }
-        prof[((x * Q + (r >> 2)) * W + k) * 4 + (r & 3)] = w;
+        prof[Profile<R, W>::index(x, row)] = w;
       }
       __syncthreads();
       if (Lmax > 0)
@@ -594,20 +627,20 @@ __global__ void __launch_bounds__(kWaveThreads, (MinBlocks<R, P, V>::value)) wav
 
 template <int R, int P, int V, int W>
 void prepare_one() {
-  const size_t smem = (size_t)kLetters * W * R * sizeof(uint32_t);
+  const size_t smem = Profile<R, W>::kBytes;
   cudaFuncSetAttribute(wave_kernel<R, P, V, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
 template <int R, int P, int V, int W>
 cudaError_t launch_one(const WaveArgs& a, int grid, cudaStream_t s) {
-  const size_t smem = (size_t)kLetters * W * R * sizeof(uint32_t);
+  const size_t smem = Profile<R, W>::kBytes;
   wave_kernel<R, P, V, W><<<grid, kWaveThreads, smem, s>>>(a);
   return cudaGetLastError();
 }
 
 template <int R, int P, int V, int W>
 int occupancy_one() {
-  const size_t smem = (size_t)kLetters * W * R * sizeof(uint32_t);
+  const size_t smem = Profile<R, W>::kBytes;
   cudaFuncSetAttribute(wave_kernel<R, P, V, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int n = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, wave_kernel<R, P, V, W>, kWaveThreads, smem) != cudaSuccess)
@@ -616,9 +649,12 @@ int occupancy_one() {
 }
 
 // The (P, V, W) combinations that exist: W = 32 with every P and V; the
-// narrow fronts (W = 16, 8) on int16x2 lanes with V = 0, 2, 3, 4 or 5.
+// narrow fronts (W = 16, 8) on int16x2 lanes with V = 0, 2, 3, 4 or 5; one
+// pair per thread (W = 1: every lane its own front, bands of R rows) on
+// int16x2 lanes with V = 0, 2, 3 or 4.
 inline bool wave_variant_exists(int P, int V, int W) {
   if (W == 32) return (P == 1 || P == 2) && V >= 0 && V <= 5;
+  if (W == 1) return P == 2 && (V == 0 || V == 2 || V == 3 || V == 4);
   return (W == 16 || W == 8) && P == 2 && (V == 0 || V == 2 || V == 3 || V == 4 || V == 5);
 }
 
@@ -628,7 +664,9 @@ struct Entry {
   template <int P, int W, class Fn>
   static auto with_v(int V, Fn&& fn) {
     using std::integral_constant;
-    if (V == 5) return fn(integral_constant<int, P>{}, integral_constant<int, 5>{}, integral_constant<int, W>{});
+    if constexpr (W > 1) {
+      if (V == 5) return fn(integral_constant<int, P>{}, integral_constant<int, 5>{}, integral_constant<int, W>{});
+    }
     if (V == 4) return fn(integral_constant<int, P>{}, integral_constant<int, 4>{}, integral_constant<int, W>{});
     if (V == 3) return fn(integral_constant<int, P>{}, integral_constant<int, 3>{}, integral_constant<int, W>{});
     if (V == 2) return fn(integral_constant<int, P>{}, integral_constant<int, 2>{}, integral_constant<int, W>{});
@@ -639,6 +677,7 @@ struct Entry {
   }
   template <class Fn>
   static auto with(int P, int V, int W, Fn&& fn) {
+    if (W == 1) return with_v<2, 1>(V, fn);
     if (W == 16) return with_v<2, 16>(V, fn);
     if (W == 8) return with_v<2, 8>(V, fn);
     if (P == 2) return with_v<2, 32>(V, fn);

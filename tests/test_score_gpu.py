@@ -165,11 +165,14 @@ def test_config1_full_size_properties_and_sample(ctx):
 
 @pytest.mark.parametrize("R", [4, 8, 12, 16, 20, 24, 32])
 @pytest.mark.parametrize("V,W", [(0, 32), (1, 32), (2, 32), (3, 32), (4, 32), (5, 32), (0, 16), (2, 16), (3, 16),
-                                 (4, 16), (5, 16), (0, 8), (2, 8), (3, 8), (4, 8), (5, 8)])
+                                 (4, 16), (5, 16), (0, 8), (2, 8), (3, 8), (4, 8), (5, 8),
+                                 (0, 1), (2, 1), (3, 1), (4, 1)])
 def test_every_kernel_template_matches_oracle(R, V, W):
     # the autotuner may pick any (rows per lane, register layout, front width)
     # for any length class: every template must be exact, single- and
-    # multi-band, with fronts of one warp finishing at different columns
+    # multi-band, with fronts of one warp finishing at different columns.
+    # W = 1 is one pair per thread (each lane its own front, bands of R rows,
+    # up to 225 bands here)
     from mestrado_gb300 import Context
     seqs = _rand_set(40 + R, 26, 1, 900)
     ref = O.score_all(seqs, threads=os.cpu_count())
