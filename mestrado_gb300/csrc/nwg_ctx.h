@@ -32,14 +32,20 @@ const int8_t* builtin_matrix();
 const char* letter_order();
 
 struct TuneChoice {
-  int R;   // rows per lane (4, 8, 12, 16, 20, 24, 32)
+  int R;   // rows per lane (4 to 32, even; not a multiple of 4, or 28: layouts 2 to 4 on int16x2 lanes only)
   int V;   // register layout (0 to 5)
   int W;   // lanes per wavefront (32, 16, 8): band of W*R rows; 1: one pair per thread, bands of R rows
 };
+// Rows a Y of `rows` residues occupies under choice t (whole bands).
+inline int padded_rows(const TuneChoice& t, int rows) {
+  const int band = t.W * t.R;
+  return (rows + band - 1) / band * band;
+}
 // The same band on full-width fronts, for groups that run on int32 lanes
-// (the narrow fronts exist for int16x2 lanes only).
+// (the narrow fronts and the rows per lane that are not multiples of 4 exist
+// for int16x2 lanes only).
 inline TuneChoice int32_choice(TuneChoice t) {
-  if (t.W == 32) return t;
+  if (t.W == 32 && t.R % 4 == 0 && t.R != 28) return t;
   const int band = t.W * t.R;
   int R = 32;
   for (int r : {4, 8, 12, 16, 20, 24, 32})
@@ -83,10 +89,31 @@ struct Ctx {
   // The fastest wavefront (W >= 8) per class, for the serving loop, whose
   // small jobs are latency-bound (one pair per thread lengthens them).
   TuneChoice tune_wave[kTuneClasses];
-  // The choice for Y groups of this many rows; layout 4 is exact only when
-  // go >= ge and falls back to layout 2 otherwise.
+  // Every candidate the autotuner timed per class, with its rate in computed
+  // cells per second (band-padded rows x columns / time).  Empty when the
+  // table was set by hand or not tuned: tune[] is then used as it is.
+  struct Cand {
+    TuneChoice t;
+    double rate;
+  };
+  std::vector<Cand> cands[kTuneClasses];
+  // The choice for a Y group of this many rows: the class's candidate with
+  // the least estimated time (its padded rows / its rate), the class's
+  // fastest at the class bound unless another is estimated 2 % faster.
+  // Layout 4 is exact only when go >= ge and falls back to layout 2.
   TuneChoice choice(int rows) const {
-    TuneChoice t = tune[tune_class(rows)];
+    const int k = tune_class(rows);
+    TuneChoice t = tune[k], fastest = t;
+    double pick_est = 0.0, min_est = 0.0;
+    for (const Cand& c : cands[k]) {
+      const double est = padded_rows(c.t, rows) / c.rate;
+      if (c.t.R == t.R && c.t.V == t.V && c.t.W == t.W) pick_est = est;
+      if (min_est == 0.0 || est < min_est) {
+        min_est = est;
+        fastest = c.t;
+      }
+    }
+    if (pick_est > 0.0 && min_est < 0.98 * pick_est) t = fastest;
     if (t.V == 4 && go < ge) t.V = 2;
     return t;
   }

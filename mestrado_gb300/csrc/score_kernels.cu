@@ -222,7 +222,7 @@ int wave_max_ctas_per_sm(int R, int P, int V, int W) {
 
 #define NWG_CASE(r) (R == r) ||
 bool wave_exists(int R, int P, int V, int W) {
-  return (NWG_WAVE_ROWS(NWG_CASE) false) && wave::wave_variant_exists(P, V, W);
+  return (NWG_WAVE_ROWS(NWG_CASE) false) && wave::wave_variant_exists(R, P, V, W);
 }
 #undef NWG_CASE
 

@@ -1,14 +1,18 @@
 // tune.cu -- autotuner of the batched form: per length class of the Y rows,
 // the rows-per-lane template and register layout of the wave kernel.
 //
-// For class k a probe workload is built from uniform random residues: 128 Y
-// sequences of the class's representative length and enough X sequences
-// (10% longer) for ~2e10 cells, scored in block mode so every pair lands in
-// that class.  Each candidate (R, V, W) runs once to warm up and once timed
-// with CUDA events; the fastest wins.  Candidates: wavefronts of W = 32, 16
-// or 8 lanes whose band holds the class in one to three bands, and, for the
-// classes up to 512 rows, one pair per thread (W = 1, bands of 16-32 rows).  The table is written to a cache file per
-// device (name + SM count) and read back by later contexts.
+// For class k (Y rows in (lo, hi]) a probe workload is built from uniform
+// random residues: 128 Y sequences and enough X sequences of hi + 10 %
+// residues for ~1e10 cells, scored in block mode.  Candidates: wavefronts of
+// W = 32, 16 or 8 lanes with one, two or three bands whose rows land in
+// (lo, hi + hi/8], and, for the classes up to 512 rows, one pair per thread
+// (W = 1, bands of 16-32 rows).  Each runs once to warm up and once timed
+// with CUDA events, on Y of the longest whole number of its bands in the
+// class (else hi), which gives its rate in computed (band-padded) cells per
+// second.  The class's pick is the least estimated time at hi (padded rows /
+// rate); every candidate's rate is kept, so that a plan can pick per Y group
+// the candidate whose bands fit that group best.  The table is written to a
+// cache file per device (name + SM count) and read back by later contexts.
 #include <sys/stat.h>
 
 #include <algorithm>
@@ -44,13 +48,27 @@ void make_parent_dirs(const std::string& file) {
     if (file[k] == '/') mkdir(file.substr(0, k).c_str(), 0755);   // existing levels just fail
 }
 
-const int kCandR[] = {4, 8, 12, 16, 20, 24, 32};
+const int kCandR[] = {4, 8, 12, 16, 18, 20, 22, 24, 26, 28, 30, 32};
 
-// Probe length of a class: its longest Y (so a candidate whose band holds the
-// probe holds every Y of the class); the open last class probes 2000 rows.
+// Upper bound of a class's Y rows for the probes: its longest Y; the open last
+// class probes 2000 rows.
 int representative_rows(int k) { return k == kTuneClasses - 1 ? 2000 : kClassRows[k]; }
+int class_floor(int k) { return k == 0 ? 0 : kClassRows[k - 1]; }
 
-const char kCacheTag[] = "nwgpu-tune-5";
+// Y rows a candidate is probed on in class k, or 0 if it is no candidate there.
+int probe_rows(int k, const TuneChoice& t) {
+  const int hi = representative_rows(k), lo = class_floor(k);
+  const int band = t.W * t.R;
+  if (t.W == 1) return (t.R >= 16 && hi <= 512) ? hi : 0;
+  if (k == kTuneClasses - 1) return (band * 3 >= hi && band <= 2 * hi + 128) ? hi : 0;
+  bool useful = false;
+  for (int m = 1; m <= 3; ++m) useful |= lo < m * band && m * band <= hi + hi / 8;
+  if (!useful) return 0;
+  const int whole = hi / band * band;
+  return whole > lo ? whole : hi;
+}
+
+const char kCacheTag[] = "nwgpu-tune-6";
 
 }  // namespace
 
@@ -62,18 +80,27 @@ bool Ctx::tune_from_cache(nwg_tune_result* res) {
   int ok = 0;
   TuneChoice t[kTuneClasses], tw[kTuneClasses];
   double g[kTuneClasses];
+  std::vector<Cand> cc[kTuneClasses];
   char tag[32] = {0};
   if (std::fscanf(f, "%31s", tag) == 1 && std::strcmp(tag, kCacheTag) == 0) {
     for (int k = 0; k < kTuneClasses; ++k) {
-      int kk, R, V, W, Rw, Vw, Ww;
+      int kk, R, V, W, Rw, Vw, Ww, n;
       double gc;
-      if (std::fscanf(f, "%d %d %d %d %lf %d %d %d", &kk, &R, &V, &W, &gc, &Rw, &Vw, &Ww) == 8 && kk == k &&
-          wave_exists(R, 2, V, W) && Ww >= 8 && wave_exists(Rw, 2, Vw, Ww)) {
-        t[k] = {R, V, W};
-        tw[k] = {Rw, Vw, Ww};
-        g[k] = gc;
-        ++ok;
+      if (std::fscanf(f, "%d %d %d %d %lf %d %d %d %d", &kk, &R, &V, &W, &gc, &Rw, &Vw, &Ww, &n) != 9 || kk != k ||
+          !wave_exists(R, 2, V, W) || Ww < 8 || !wave_exists(Rw, 2, Vw, Ww) || n < 0 || n > 1000)
+        break;
+      bool good = true;
+      for (int e = 0; e < n && good; ++e) {
+        Cand c;
+        good = std::fscanf(f, "%d %d %d %lf", &c.t.R, &c.t.V, &c.t.W, &c.rate) == 4 &&
+               wave_exists(c.t.R, 2, c.t.V, c.t.W) && c.rate > 0.0;
+        cc[k].push_back(c);
       }
+      if (!good) break;
+      t[k] = {R, V, W};
+      tw[k] = {Rw, Vw, Ww};
+      g[k] = gc;
+      ++ok;
     }
   }
   std::fclose(f);
@@ -81,6 +108,7 @@ bool Ctx::tune_from_cache(nwg_tune_result* res) {
   for (int k = 0; k < kTuneClasses; ++k) {
     tune[k] = t[k];
     tune_wave[k] = tw[k];
+    cands[k] = std::move(cc[k]);
     if (res) {
       res->rows_per_lane[k] = t[k].R;
       res->variant[k] = t[k].V;
@@ -114,6 +142,8 @@ int Ctx::autotune(bool force, nwg_tune_result* out) {
   };
   int rc = NWG_OK;
   DevBuf probe;
+  for (int k = 0; k < kTuneClasses; ++k) cands[k].clear();   // the probes run tune[k] as it is
+  std::vector<Cand> found[kTuneClasses];
   for (int k = 0; k < kTuneClasses && rc == NWG_OK; ++k) {
     const int Ly = representative_rows(k);
     const int Lx = Ly + Ly / 10;
@@ -142,20 +172,16 @@ int Ctx::autotune(bool force, nwg_tune_result* out) {
       dD = (float*)((char*)probe.p + ((total + 255) / 256) * 256);
     }
     if ((rc = cuda(cudaMemcpy(dcodes, codes.data(), total, cudaMemcpyHostToDevice), "autotune upload"))) break;
-    double best = -1.0, best_wave = -1.0;
+    double best = 0.0, best_wave = 0.0;   // least estimated time at Ly (padded rows / rate)
     TuneChoice pick = kDefaultTune[k], pick_wave = kDefaultTuneWave[k];
     for (int W : {32, 16, 8, 1})
     for (int R : kCandR) {
-      const int band = W * R;
-      if (W == 1) {
-        // one pair per thread: bands of R rows; for the classes up to 512 rows
-        if (R < 16 || Ly > 512) continue;
-      } else if (band * 3 < Ly || band > 2 * Ly + 128) {
-        continue;   // at most 3 bands, at most ~half idle
-      }
       for (int V = 0; V <= 5; ++V) {
-        if (!wave_exists(R, 2, V, W) || (V == 4 && go < ge)) continue;
-        tune[k] = {R, V, W};
+        const TuneChoice cand{R, V, W};
+        const int Lyc = probe_rows(k, cand);
+        if (Lyc == 0 || !wave_exists(R, 2, V, W) || (V == 4 && go < ge)) continue;
+        for (int j = 0; j <= ny; ++j) yoff[j] = (int64_t)nx * Lx + (int64_t)j * Lyc;
+        tune[k] = cand;
         ++tune_version;
         float ms = 0.f;
         for (int rep = 0; rep < 2 && rc == NWG_OK; ++rep) {
@@ -168,14 +194,16 @@ int Ctx::autotune(bool force, nwg_tune_result* out) {
           cudaEventElapsedTime(&ms, ev0, ev1);
         }
         if (rc) break;
-        const double g = (double)nx * ny * Ly * Lx / (ms * 1e-3) / 1e9;
-        if (g > best) {
-          best = g;
-          pick = {R, V, W};
+        const double rate = (double)nx * ny * padded_rows(cand, Lyc) * Lx / (ms * 1e-3);
+        found[k].push_back({cand, rate});
+        const double est = padded_rows(cand, Ly) / rate;
+        if (best == 0.0 || est < best) {
+          best = est;
+          pick = cand;
         }
-        if (W >= 8 && g > best_wave) {
-          best_wave = g;
-          pick_wave = {R, V, W};
+        if (W >= 8 && (best_wave == 0.0 || est < best_wave)) {
+          best_wave = est;
+          pick_wave = cand;
         }
       }
       if (rc) break;
@@ -185,7 +213,7 @@ int Ctx::autotune(bool force, nwg_tune_result* out) {
     res.rows_per_lane[k] = pick.R;
     res.variant[k] = pick.V;
     res.lanes[k] = pick.W;
-    res.gcups[k] = best;
+    res.gcups[k] = best > 0.0 ? (double)Ly / best / 1e9 : 0.0;   // the pick's GCUPS on Y of the class bound
   }
   probe.release();
   destroy_plans(this);   // the probe plans are of no further use
@@ -198,14 +226,18 @@ int Ctx::autotune(bool force, nwg_tune_result* out) {
     }
     return rc;
   }
+  for (int k = 0; k < kTuneClasses; ++k) cands[k] = std::move(found[k]);
   tuned = true;
   res.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   make_parent_dirs(path);
   if (FILE* f = std::fopen(path.c_str(), "w")) {
     std::fprintf(f, "%s\n", kCacheTag);
-    for (int k = 0; k < kTuneClasses; ++k)
-      std::fprintf(f, "%d %d %d %d %.3f %d %d %d\n", k, tune[k].R, tune[k].V, tune[k].W, res.gcups[k],
-                   tune_wave[k].R, tune_wave[k].V, tune_wave[k].W);
+    for (int k = 0; k < kTuneClasses; ++k) {
+      std::fprintf(f, "%d %d %d %d %.3f %d %d %d %d", k, tune[k].R, tune[k].V, tune[k].W, res.gcups[k],
+                   tune_wave[k].R, tune_wave[k].V, tune_wave[k].W, (int)cands[k].size());
+      for (const Cand& c : cands[k]) std::fprintf(f, " %d %d %d %.6g", c.t.R, c.t.V, c.t.W, c.rate);
+      std::fprintf(f, "\n");
+    }
     std::fclose(f);
   }
   if (out) *out = res;
@@ -227,6 +259,7 @@ extern "C" int nwg_set_tuning_lanes(nwg_ctx* ctx, const int32_t* rows_per_lane, 
     if (!nwg::wave_exists(rows_per_lane[k], 2, variant[k], lanes ? lanes[k] : 32)) return NWG_ERR_INVALID;
   for (int k = 0; k < nwg::kTuneClasses; ++k) {
     c->tune[k] = {rows_per_lane[k], variant[k], lanes ? lanes[k] : 32};
+    c->cands[k].clear();   // a forced table is used as it is
     // a forced table drives the serving loop too where it names wavefronts
     if (c->tune[k].W >= 8) c->tune_wave[k] = c->tune[k];
   }

@@ -196,7 +196,7 @@ __device__ __forceinline__ void queue_rerun(const WaveArgs& a, int i, int y) {
 // letter's row of groups is padded by one uint4 to spread them over the banks.
 template <int R, int W>
 struct Profile {
-  static constexpr int Q = R / 4;
+  static constexpr int Q = (R + 3) / 4;                               // uint4 per lane (last one partly used)
   static constexpr int kLetterStride = W == 1 ? Q + 1 : Q * W;        // uint4 per letter
   static constexpr int kWords = kLetters * kLetterStride * 4;         // 32-bit words
   static constexpr size_t kBytes = sizeof(uint32_t) * (size_t)kWords;
@@ -233,7 +233,7 @@ __device__ __forceinline__ uint32_t strip_column(BandState<R, P, V>& s, const ui
                                                  uint32_t diag, uint32_t hin, uint32_t fin, uint32_t NGE,
                                                  uint32_t NGO, uint32_t NGOP) {
   using L = Lanes<P>;
-  constexpr int Q = R / 4;
+  constexpr int Q = (R + 3) / 4;   // 4-row profile quads; rows past R of the last one are skipped
   uint32_t f = fin;
   if (V == 3) {
     // s.H holds T = H - go; hin is T of the row above; sv is S + go
@@ -245,6 +245,7 @@ __device__ __forceinline__ uint32_t strip_column(BandState<R, P, V>& s, const ui
 #pragma unroll
       for (int w = 0; w < 4; ++w) {
         const int r = q * 4 + w;
+        if (r >= R) continue;
         f = L::addmax(f, NGE, tup);                                      // F[r][c]
         const uint32_t e = L::addmax(s.E[r], NGE, s.H[r]);               // E[r][c]
         const uint32_t h = L::max3(e, f, L::add(diag, sv[w]));           // H[r][c]
@@ -266,6 +267,7 @@ __device__ __forceinline__ uint32_t strip_column(BandState<R, P, V>& s, const ui
 #pragma unroll
       for (int w = 0; w < 4; ++w) {
         const int r = q * 4 + w;
+        if (r >= R) continue;
         f = L::addmax(f, NGE, up);                                       // F'[r][c]
         const uint32_t e = L::addmax(s.E[r], NGE, s.H[r]);               // E'[r][c]
         const uint32_t m = L::addmax(e, NGOP, L::add(diag, sv[w]));      // max(E, diag + S)
@@ -287,6 +289,7 @@ __device__ __forceinline__ uint32_t strip_column(BandState<R, P, V>& s, const ui
 #pragma unroll
       for (int w = 0; w < 4; ++w) {
         const int r = q * 4 + w;
+        if (r >= R) continue;
         f = L::addmax(f, NGE, hup);                                      // F'[r][c]
         const uint32_t e = L::addmax(s.E[r], NGE, s.H[r]);               // E'[r][c]
         const uint32_t m = L::addmax(e, NGOP, L::add(diag, sv[w]));      // max(E, diag + S)
@@ -307,6 +310,7 @@ __device__ __forceinline__ uint32_t strip_column(BandState<R, P, V>& s, const ui
 #pragma unroll
     for (int w = 0; w < 4; ++w) {
       const int r = q * 4 + w;
+      if (r >= R) continue;
       f = L::addmax(f, NGE, tup);                                        // F[r][c]
       const uint32_t tl = (V == 0) ? s.T[(V == 0) ? r : 0] : L::add(s.H[r], NGO);
       const uint32_t e = L::addmax(s.E[r], NGE, tl);                     // E[r][c]
@@ -329,7 +333,7 @@ __device__ __forceinline__ void strip_column_pair(BandState<R, P, 3> (&s)[2], co
                                                   const uint32_t (&hin)[2], uint32_t (&f)[2], uint32_t NGE,
                                                   uint32_t NGO) {
   using L = Lanes<P>;
-  constexpr int Q = R / 4;
+  constexpr int Q = (R + 3) / 4;
   uint32_t tup[2] = {hin[0], hin[1]};
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
@@ -338,6 +342,7 @@ __device__ __forceinline__ void strip_column_pair(BandState<R, P, 3> (&s)[2], co
 #pragma unroll
     for (int w = 0; w < 4; ++w) {
       const int r = q * 4 + w;
+      if (r >= R) continue;
 #pragma unroll
       for (int k = 0; k < 2; ++k) {
         f[k] = L::addmax(f[k], NGE, tup[k]);
@@ -370,7 +375,6 @@ __device__ __forceinline__ void wave_band(const WaveArgs& a, int sl, int b, int 
   constexpr int K = Layout<V>::K;
   constexpr int VL = Layout<V>::L;
   constexpr int BAND = W * R;
-  constexpr int Q = R / 4;
   const uint32_t NGE = L::packed(-a.ge);        // per-half operand of addmax
   const uint32_t NGO = L::arith(-a.go, -a.go);   // word added to H to get H - go
   const uint32_t NGOP = L::packed(-a.go);        // per-half operand: - go
@@ -517,8 +521,7 @@ __global__ void __launch_bounds__(kWaveThreads, (MinBlocks<R, P, V>::value)) wav
   constexpr int S = 32 / W;                // fronts per warp
   constexpr int K = Layout<V>::K;          // X per front
   constexpr int BAND = W * R;
-  constexpr int Q = R / 4;
-  static_assert(R % 4 == 0, "rows per lane must be a multiple of 4");
+  static_assert(R % 2 == 0 && R >= 4 && R <= 32, "rows per lane: even, 4 to 32");
   static_assert(W == 1 || W == 8 || W == 16 || W == 32, "front width");
   static_assert(W > 1 || K == 1, "one pair per thread holds one X per front");
   extern __shared__ __align__(16) uint32_t prof[];   // Profile<R, W>: [letter][Q][front lane][4]
@@ -604,7 +607,6 @@ __global__ void __launch_bounds__(kWaveThreads, (MinBlocks<R, P, V>::value)) wav
       for (int e = threadIdx.x; e < kLetters * BAND; e += kWaveThreads) {
         const int x = e / BAND;
         const int row = e - x * BAND;
-        const int k = row / R, r = row - k * R;
         const int grow = b * BAND + row;
         const int gsh = Layout<V>::L == 3 ? a.go : 0;   // layout 3 adds the profile to T = H - go
         const int sa = (grow < LyA ? (int)s_sub[clamp_code(YA[grow]) * kLetters + x] : 0) + gsh;
@@ -648,11 +650,17 @@ int occupancy_one() {
   return n > 0 ? n : 1;
 }
 
-// The (P, V, W) combinations that exist: W = 32 with every P and V; the
-// narrow fronts (W = 16, 8) on int16x2 lanes with V = 0, 2, 3, 4 or 5; one
-// pair per thread (W = 1: every lane its own front, bands of R rows) on
-// int16x2 lanes with V = 0, 2, 3 or 4.
-inline bool wave_variant_exists(int P, int V, int W) {
+// Rows per lane that exist only in the most used forms (int16x2 wavefronts,
+// layouts 2 to 4): they refine the band sizes between the multiples of 4.
+constexpr bool extra_rows(int R) { return R % 4 != 0 || R == 28; }
+
+// The (P, V, W) combinations that exist for R rows per lane.  For R a multiple
+// of 4 (not 28): W = 32 with every P and V; the narrow fronts (W = 16, 8) on
+// int16x2 lanes with V = 0, 2, 3, 4 or 5; one pair per thread (W = 1: every
+// lane its own front, bands of R rows) on int16x2 lanes with V = 0, 2, 3 or 4.
+// The other R: int16x2 wavefronts of 32, 16 or 8 lanes with V = 2, 3 or 4.
+inline bool wave_variant_exists(int R, int P, int V, int W) {
+  if (extra_rows(R)) return P == 2 && (W == 32 || W == 16 || W == 8) && V >= 2 && V <= 4;
   if (W == 32) return (P == 1 || P == 2) && V >= 0 && V <= 5;
   if (W == 1) return P == 2 && (V == 0 || V == 2 || V == 3 || V == 4);
   return (W == 16 || W == 8) && P == 2 && (V == 0 || V == 2 || V == 3 || V == 4 || V == 5);
@@ -661,43 +669,54 @@ inline bool wave_variant_exists(int P, int V, int W) {
 // Entry points of one rows-per-lane template (every existing P, V, W).
 template <int R>
 struct Entry {
+  static constexpr bool kExtra = extra_rows(R);
   template <int P, int W, class Fn>
   static auto with_v(int V, Fn&& fn) {
     using std::integral_constant;
-    if constexpr (W > 1) {
+    if constexpr (W > 1 && !kExtra) {
       if (V == 5) return fn(integral_constant<int, P>{}, integral_constant<int, 5>{}, integral_constant<int, W>{});
     }
     if (V == 4) return fn(integral_constant<int, P>{}, integral_constant<int, 4>{}, integral_constant<int, W>{});
     if (V == 3) return fn(integral_constant<int, P>{}, integral_constant<int, 3>{}, integral_constant<int, W>{});
-    if (V == 2) return fn(integral_constant<int, P>{}, integral_constant<int, 2>{}, integral_constant<int, W>{});
-    if constexpr (W == 32) {
-      if (V == 1) return fn(integral_constant<int, P>{}, integral_constant<int, 1>{}, integral_constant<int, W>{});
+    if constexpr (kExtra) {
+      return fn(integral_constant<int, P>{}, integral_constant<int, 2>{}, integral_constant<int, W>{});
+    } else {
+      if (V == 2) return fn(integral_constant<int, P>{}, integral_constant<int, 2>{}, integral_constant<int, W>{});
+      if constexpr (W == 32) {
+        if (V == 1) return fn(integral_constant<int, P>{}, integral_constant<int, 1>{}, integral_constant<int, W>{});
+      }
+      return fn(integral_constant<int, P>{}, integral_constant<int, 0>{}, integral_constant<int, W>{});
     }
-    return fn(integral_constant<int, P>{}, integral_constant<int, 0>{}, integral_constant<int, W>{});
   }
   template <class Fn>
   static auto with(int P, int V, int W, Fn&& fn) {
-    if (W == 1) return with_v<2, 1>(V, fn);
-    if (W == 16) return with_v<2, 16>(V, fn);
-    if (W == 8) return with_v<2, 8>(V, fn);
-    if (P == 2) return with_v<2, 32>(V, fn);
-    return with_v<1, 32>(V, fn);
+    if constexpr (kExtra) {
+      if (W == 16) return with_v<2, 16>(V, fn);
+      if (W == 8) return with_v<2, 8>(V, fn);
+      return with_v<2, 32>(V, fn);
+    } else {
+      if (W == 1) return with_v<2, 1>(V, fn);
+      if (W == 16) return with_v<2, 16>(V, fn);
+      if (W == 8) return with_v<2, 8>(V, fn);
+      if (P == 2) return with_v<2, 32>(V, fn);
+      return with_v<1, 32>(V, fn);
+    }
   }
   static cudaError_t launch(int P, int V, int W, const WaveArgs& a, int grid, cudaStream_t s) {
-    if (!wave_variant_exists(P, V, W)) return cudaErrorInvalidValue;
+    if (!wave_variant_exists(R, P, V, W)) return cudaErrorInvalidValue;
     return with(P, V, W, [&](auto p, auto v, auto w) {
       return launch_one<R, decltype(p)::value, decltype(v)::value, decltype(w)::value>(a, grid, s);
     });
   }
   static void prepare(int P, int V, int W) {
-    if (!wave_variant_exists(P, V, W)) return;
+    if (!wave_variant_exists(R, P, V, W)) return;
     with(P, V, W, [&](auto p, auto v, auto w) {
       prepare_one<R, decltype(p)::value, decltype(v)::value, decltype(w)::value>();
       return 0;
     });
   }
   static int occupancy(int P, int V, int W) {
-    if (!wave_variant_exists(P, V, W)) return 1;
+    if (!wave_variant_exists(R, P, V, W)) return 1;
     return with(P, V, W, [&](auto p, auto v, auto w) {
       return occupancy_one<R, decltype(p)::value, decltype(v)::value, decltype(w)::value>();
     });
@@ -707,7 +726,7 @@ struct Entry {
 }  // namespace wave
 
 // Per-template dispatch tables (one translation unit per R).
-#define NWG_WAVE_ROWS(X) X(4) X(8) X(12) X(16) X(20) X(24) X(32)
+#define NWG_WAVE_ROWS(X) X(4) X(8) X(12) X(16) X(18) X(20) X(22) X(24) X(26) X(28) X(30) X(32)
 #define NWG_DECL_WAVE(r)                                                                         \
   cudaError_t wave_launch_r##r(int P, int V, int W, const WaveArgs& a, int grid, cudaStream_t s); \
   void wave_prepare_r##r(int P, int V, int W);                                                  \

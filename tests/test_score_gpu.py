@@ -173,6 +173,18 @@ def test_every_kernel_template_matches_oracle(R, V, W):
     # multi-band, with fronts of one warp finishing at different columns.
     # W = 1 is one pair per thread (each lane its own front, bands of R rows,
     # up to 225 bands here)
+    _check_template(R, V, W)
+
+
+@pytest.mark.parametrize("R", [18, 22, 26, 28, 30])
+@pytest.mark.parametrize("V,W", [(2, 32), (3, 32), (4, 32), (2, 16), (3, 16), (4, 16), (2, 8), (3, 8), (4, 8)])
+def test_finer_band_templates_match_oracle(R, V, W):
+    # rows per lane that are not multiples of 4 (the lane's last 4-row profile
+    # load is partly used) and 28: int16x2 wavefronts with layouts 2 to 4
+    _check_template(R, V, W)
+
+
+def _check_template(R, V, W):
     from mestrado_gb300 import Context
     seqs = _rand_set(40 + R, 26, 1, 900)
     ref = O.score_all(seqs, threads=os.cpu_count())
