@@ -141,6 +141,13 @@ int nwg_align_pairs(nwg_ctx* ctx, const int8_t* codes, const int64_t* offsets, i
                     const int32_t* px, const int32_t* py, int npairs, char* outx, char* outy,
                     int64_t stride, int32_t* len, int32_t* score, nwg_stats* stats);
 
+/* Front width of the traceback kernel: lanes per pair (32, 16 or 8; 32/W
+ * pairs per warp, bands of 8W rows), or 0 (the default) for the width with
+ * the least estimated cost for the call's pairs (rows x columns computed,
+ * and the walks of a warp's pairs, which run one after another).  Results
+ * do not depend on it.  Not part of the reference's interface. */
+int nwg_set_trace_lanes(nwg_ctx* ctx, int lanes);
+
 /* Guide-tree cherries (AlignmentMatch.cu:167-186 over TreeNode::getNodes,
  * TreeNode.cpp:91-117): internal node n_leaves+k joins left[k] and right[k]
  * (node ids: leaves 0..n_leaves-1, internal nodes in creation order).  Lists

@@ -190,6 +190,7 @@ EXTRA_SIGS: dict = {
     "nwg_align_pairs": ([ctypes.c_void_p, c_i8p, c_i64p, ctypes.c_int, c_i32p, c_i32p, ctypes.c_int,
                          ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int64, c_i32p, c_i32p, P(Stats)],
                         ctypes.c_int),
+    "nwg_set_trace_lanes": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "nwg_cherries": ([c_i32p, c_i32p, ctypes.c_int, c_i32p, c_i32p, c_i32p], ctypes.c_int),
     "nwg_dpx_peak": ([ctypes.c_void_p, ctypes.c_int, P(ctypes.c_double)], ctypes.c_int),
     "nwg_dpx_peak_form": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int, P(ctypes.c_double)], ctypes.c_int),

@@ -160,6 +160,7 @@ struct Ctx {
           int64_t* msa_len, nwg_stats* st);
   int msa_rows(char* out, int64_t stride);
   int nj(const float* D, int64_t ld, int n, bool device_D, nwg_join* joins, nwg_nj_stats* st);
+  int trace_lanes_forced = 0;   // front width of the traceback kernel (0: chosen per call)
   int align_pairs(const int8_t* codes, const int64_t* offsets, int n, const int32_t* px, const int32_t* py,
                   int npairs, char* outx, char* outy, int64_t stride, int32_t* outlen, int32_t* score,
                   nwg_stats* st);

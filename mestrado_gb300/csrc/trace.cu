@@ -5,23 +5,31 @@
 // 184-365), NeedlemanWunschGlobalBackKernel (:393-494) and
 // reorderMatchesMemory (:496-563).
 //
-// match_kernel: one warp per pair, int32 lanes, the wavefront of the score
-//   kernel (lane k owns 8 rows, one column behind lane k-1, bottom (H, F)
-//   passed by __shfl_up_sync).  Every cell yields the reference's 4-bit flags
+// match_kernel<W>: a wavefront of W lanes per pair (W = 32, 16 or 8: 32/W
+//   pairs per warp), int32 lanes; lane k of a front owns 8 rows of a band of
+//   8W rows, one column behind lane k-1, bottom (H, F) passed by
+//   __shfl_up_sync within the front.  Narrow fronts cut the rows computed
+//   past the end of Y (the last band) and the ramp of W-1 columns per band.
+//   Every cell yields the reference's 4-bit flags
 //     bit3 L  = (H==E && H!=F) || H==diag        (:330)
 //     bit2 U  = H==F || H==diag                  (:332)
 //     bit1 cU = F == F_up - ge                   (:315-316, :334)
 //     bit0 cL = E == E_left - ge                 (:336)
-//   A lane's 8 rows of one column make one 32-bit word; the 32 lanes of a
-//   step store 32 consecutive words (one 128-byte line): word (b*(Lx+31) + t)
-//   *32 + k holds rows b*256 + 8k .. +7 at column t-k, row r in bits 4r..4r+3.
-// The walk runs in lane 0 of the same warp right after the pair's last band,
-//   while its flags are still in L2: one thread per pair walks from (Lx-1, Ly-1) with the
-//   reference's rule set (continue flags of the previous move first, then up,
-//   then left, else diagonal), row -1 reads as left+continue, column -1 as
-//   up+continue, and an up move out of row 0 ends the walk (the reference's
-//   word reload at :456-457 never fires for row -1).  Characters come out in
-//   forward order, so the reorder/byte-swap pass is not needed.
+//   from the predicates of four DPX maxima (__vibmax_s32).
+//   A lane's 8 rows of one column make one 32-bit word; the W lanes of a
+//   front store W consecutive words per step: word (b*(Lx+W-1) + t)*W + k
+//   holds rows b*8W + 8k .. +7 at column t-k, row r in bits 4r..4r+3.
+// The walk runs in the same warp right after the pairs' last bands, while
+//   their flags are still in L2, from (Lx-1, Ly-1) with the reference's rule
+//   set (continue flags of the previous move first, then up, then left, else
+//   diagonal); row -1 reads as left+continue, column -1 as up+continue, and
+//   an up move out of row 0 ends the walk (the reference's word reload at
+//   :456-457 never fires for row -1).  Each front stages the flags of a
+//   window of 32 columns x 40 rows ending at its walk's cell in shared memory
+//   (one load round trip), with the window's residue codes, and its lane 0
+//   walks inside it; a walk leaves a window after 32 to 72 steps.
+//   Characters come out in forward order, so the reorder/byte-swap pass is
+//   not needed.
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -32,9 +40,9 @@ namespace nwg {
 
 namespace {
 
-constexpr int kTR = 8;             // rows per lane
-constexpr int kTBand = 32 * kTR;   // rows per band
-constexpr int kTWarps = 4;         // warps (pairs) per CTA (6 KB profile per warp)
+constexpr int kTR = 8;                               // rows per lane
+constexpr int kTWarps = 4;                           // warps per CTA
+constexpr int kTProfBytes = kLetters * 32 * kTR;     // profile bytes per warp (6 KB, every W)
 
 struct TraceArgs {
   const int8_t* codes;
@@ -42,6 +50,7 @@ struct TraceArgs {
   const int32_t* len;
   const int32_t* px;
   const int32_t* py;
+  const int32_t* order;     // slot -> pair: pairs of similar lengths share a warp
   const int64_t* nib_off;   // per pair: first word of its nibble array
   uint32_t* nib;
   int32_t* scratch;         // per pair slot: 2 buffers x 2 ints x maxlen
@@ -65,90 +74,177 @@ __constant__ char c_dec[kLetters + 1] = "ARNDCQEGHILKMFPSTWYVBZX*";   // code ->
 
 static_assert(kTR == 8, "a lane's scores of one column are one 8-byte load");
 
-__device__ __forceinline__ unsigned nibble_at(const uint32_t* nib, int Lx, int x, int y) {
-  if (y < 0) return x < 0 ? 0u : 9u;     // row -1: left + continue-left; corner: stop
-  if (x < 0) return 6u;                  // column -1: up + continue-up
-  const int b = y / kTBand, yy = y - b * kTBand, k = yy / kTR;
-  const uint32_t w = nib[((size_t)b * (Lx + 31) + (x + k)) * 32 + k];
-  return (w >> (4 * (yy - k * kTR))) & 15u;
-}
+// Shared memory of one front's walk: the flag words of the window (row group
+// g0+gi of column x0-j at gi*32 + j) and its residue codes.
+struct WalkWindow {
+  uint32_t flags[5 * 32];
+  int8_t xs[32];   // X[x0 - j]
+  int8_t ys[40];   // Y[8*g0 + i]
+};
 
-// The backtrace of pair p from its flags (one thread).
-__device__ void walk_pair(const TraceArgs& a, int p) {
-  const int ix = a.px[p], iy = a.py[p];
-  const int8_t* X = a.codes + a.start[ix];
-  const int8_t* Y = a.codes + a.start[iy];
-  const int Lx = a.len[ix], Ly = a.len[iy];
-  const uint32_t* nib = a.nib + a.nib_off[p];
-  char* ox = a.outx + (size_t)p * a.stride;
-  char* oy = a.outy + (size_t)p * a.stride;
-  int x = Lx - 1, y = Ly - 1, k = 0;
-  unsigned prev = 12u;
-  unsigned cell = nibble_at(nib, Lx, x, y);
-  const int cap = Lx + Ly;
-  while ((cell & 12u) && k < cap) {
-    unsigned todo;
-    if (((prev & 12u) == 4u) && (prev & 2u)) todo = 4u;
-    else if (((prev & 12u) == 8u) && (prev & 1u)) todo = 8u;
-    else if ((cell & 12u) == 4u) todo = 4u;
-    else if ((cell & 12u) == 8u) todo = 8u;
-    else todo = 12u;
-    // a well-formed matrix never asks for a move off the -1 row/column other
-    // than the ones handled below; stop rather than read outside the inputs
-    if ((todo != 4u && x < 0) || (todo != 8u && y < 0)) break;
-    bool stop = false;
-    if (todo == 8u) {
-      ox[k] = c_dec[tclamp(X[x])];
-      oy[k] = '-';
-      --x;
-    } else if (todo == 4u) {
-      ox[k] = '-';
-      oy[k] = c_dec[tclamp(Y[y])];
-      --y;
-      stop = y < 0;     // no word reload for row -1 after an up move
-    } else {
-      ox[k] = c_dec[tclamp(X[x])];
-      oy[k] = c_dec[tclamp(Y[y])];
-      --x;
-      --y;
-    }
-    prev = todo | (cell & 3u);
-    ++k;
-    cell = stop ? 0u : nibble_at(nib, Lx, x, y);
+// The backtraces of the warp's fronts (every lane calls it; p < 0: the
+// front has no pair).  Lane 0 of each front walks; all lanes of a front load
+// its windows.
+template <int W>
+__device__ void walk_pairs(const TraceArgs& a, int p, int lane, WalkWindow& w) {
+  const int sl = lane % W, lead = lane - sl;
+  const int8_t* X = nullptr;
+  const int8_t* Y = nullptr;
+  const uint32_t* nib = nullptr;
+  char* ox = nullptr;
+  char* oy = nullptr;
+  int Lx = 0, Ly = 0;
+  if (p >= 0) {
+    const int ix = a.px[p], iy = a.py[p];
+    X = a.codes + a.start[ix];
+    Y = a.codes + a.start[iy];
+    Lx = a.len[ix];
+    Ly = a.len[iy];
+    nib = a.nib + a.nib_off[p];
+    ox = a.outx + (size_t)p * a.stride;
+    oy = a.outy + (size_t)p * a.stride;
   }
-  ox[k] = 0;
-  oy[k] = 0;
-  a.outlen[p] = k;
+  const int cap = Lx + Ly;
+  // walk state (meaningful in the front's lane 0): 1 = needs a window, 2 = done
+  int state = p >= 0 ? 1 : 2;
+  int x = Lx - 1, y = Ly - 1, k = 0;
+  unsigned prev = 12u, cell = 0u;
+  bool have_cell = false, stop = false;
+  for (;;) {
+    const int st = __shfl_sync(0xffffffffu, state, lead);
+    if (__all_sync(0xffffffffu, st == 2)) break;
+    // (re)load the window ending at (x, y) of the fronts that need one; x, y >= 0 there
+    const int x0 = __shfl_sync(0xffffffffu, x, lead);
+    const int g0 = (__shfl_sync(0xffffffffu, y, lead) >> 3) - 4;
+    if (st == 1) {
+#pragma unroll
+      for (int j = 0; j < 32 / W; ++j) {
+        const int col = sl + j * W, c = x0 - col;
+#pragma unroll
+        for (int gi = 0; gi < 5; ++gi) {
+          const int g = g0 + gi;
+          uint32_t v = 0u;
+          if (g >= 0 && c >= 0) v = nib[((size_t)(g / W) * (Lx + W - 1) + (c + g % W)) * W + g % W];
+          w.flags[gi * 32 + col] = v;
+        }
+        w.xs[col] = c >= 0 ? X[c] : (int8_t)0;
+      }
+      for (int i = sl; i < 40; i += W) {
+        const int r = 8 * g0 + i;
+        w.ys[i] = (r >= 0 && r < Ly) ? Y[r] : (int8_t)0;
+      }
+    }
+    __syncwarp();
+    if (sl == 0 && st == 1) {
+      for (;;) {
+        if (!have_cell) {
+          if (stop) {
+            cell = 0u;   // no word reload for row -1 after an up move
+          } else if (y < 0) {
+            cell = x < 0 ? 0u : 9u;   // row -1: left + continue-left; corner: stop
+          } else if (x < 0) {
+            cell = 6u;                // column -1: up + continue-up
+          } else if (x0 - x < 32 && (y >> 3) >= g0) {
+            cell = (w.flags[((y >> 3) - g0) * 32 + (x0 - x)] >> (4 * (y & 7))) & 15u;
+          } else {
+            state = 1;
+            break;
+          }
+          have_cell = true;
+        }
+        if (!((cell & 12u) && k < cap)) {
+          state = 2;
+          break;
+        }
+        unsigned todo;
+        if (((prev & 12u) == 4u) && (prev & 2u)) todo = 4u;
+        else if (((prev & 12u) == 8u) && (prev & 1u)) todo = 8u;
+        else if ((cell & 12u) == 4u) todo = 4u;
+        else if ((cell & 12u) == 8u) todo = 8u;
+        else todo = 12u;
+        // a well-formed matrix never asks for a move off the -1 row/column
+        // other than the ones handled here; stop rather than read outside
+        if ((todo != 4u && x < 0) || (todo != 8u && y < 0)) {
+          state = 2;
+          break;
+        }
+        // residue codes: from the window inside it, else (the runs along row
+        // -1 and column -1) from the sequences
+        const bool xin = x >= 0 && x0 - x < 32;
+        const bool yin = y >= 8 * g0 && y - 8 * g0 < 40;
+        if (todo == 8u) {
+          ox[k] = c_dec[tclamp(xin ? w.xs[x0 - x] : X[x])];
+          oy[k] = '-';
+          --x;
+        } else if (todo == 4u) {
+          ox[k] = '-';
+          oy[k] = c_dec[tclamp(yin ? w.ys[y - 8 * g0] : Y[y])];
+          --y;
+          stop = y < 0;
+        } else {
+          ox[k] = c_dec[tclamp(xin ? w.xs[x0 - x] : X[x])];
+          oy[k] = c_dec[tclamp(yin ? w.ys[y - 8 * g0] : Y[y])];
+          --x;
+          --y;
+        }
+        prev = todo | (cell & 3u);
+        ++k;
+        have_cell = false;
+      }
+      if (state == 2) {
+        ox[k] = 0;
+        oy[k] = 0;
+        a.outlen[p] = k;
+      }
+    }
+    __syncwarp();   // the walkers are done with the windows before they are overwritten
+  }
 }
 
+template <int W>
 __global__ void __launch_bounds__(32 * kTWarps) match_kernel(const TraceArgs a) {
+  constexpr int S = 32 / W;         // fronts (pairs) per warp
+  constexpr int BAND = W * kTR;     // rows per band
   __shared__ int8_t s_sub[kLetters * kLetters];
-  __shared__ __align__(8) int8_t s_prof[kTWarps][kLetters * kTBand];   // per-warp profile [letter][row]
+  __shared__ __align__(16) int8_t s_prof[kTWarps][kTProfBytes];   // per front [letter][band row]
   for (int e = threadIdx.x; e < kLetters * kLetters; e += blockDim.x) s_sub[e] = a.sub[e];
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
-  const int p = blockIdx.x * kTWarps + warp;
-  if (p >= a.npairs) return;
-  const int ix = a.px[p], iy = a.py[p];
-  const int8_t* X = a.codes + a.start[ix];
-  const int8_t* Y = a.codes + a.start[iy];
-  const int Lx = a.len[ix], Ly = a.len[iy];
+  const int front = lane / W, sl = lane % W;
+  const int wslot = (blockIdx.x * kTWarps + warp) * S;
+  if (wslot >= a.npairs) return;    // the whole warp is idle
+  const int slot = wslot + front;
+  const int p = slot < a.npairs ? a.order[slot] : -1;
+  const int8_t* X = nullptr;
+  const int8_t* Y = nullptr;
+  int Lx = 0, Ly = 0;
+  if (p >= 0) {
+    const int ix = a.px[p], iy = a.py[p];
+    X = a.codes + a.start[ix];
+    Y = a.codes + a.start[iy];
+    Lx = a.len[ix];
+    Ly = a.len[iy];
+  }
   const int go = a.go, ge = a.ge;
-  const int nb = (Ly + kTBand - 1) / kTBand;
-  int8_t* prof = s_prof[warp];
-  int32_t* scr = a.scratch + (size_t)p * 4 * a.scratch_cols;
-  uint32_t* nib = a.nib + a.nib_off[p];
+  const int nb = (Ly + BAND - 1) / BAND;
+  const int nb_max = __reduce_max_sync(0xffffffffu, (unsigned)nb);
+  const int lx_max = __reduce_max_sync(0xffffffffu, (unsigned)Lx);
+  int8_t* prof = s_prof[warp] + front * (kLetters * BAND);
+  int32_t* scr = p >= 0 ? a.scratch + (size_t)p * 4 * a.scratch_cols : nullptr;
+  uint32_t* nib = p >= 0 ? a.nib + a.nib_off[p] : nullptr;
   const int kSent = kShortMin + ge;
   int H[kTR], E[kTR];
-  for (int b = 0; b < nb; ++b) {
+  for (int b = 0; b < nb_max; ++b) {
+    const bool band_on = b < nb;
     __syncwarp();
-    for (int e = lane; e < kLetters * kTBand; e += 32) {
-      const int x = e / kTBand, row = e - x * kTBand, grow = b * kTBand + row;
-      prof[e] = grow < Ly ? s_sub[tclamp(Y[grow]) * kLetters + x] : (int8_t)0;
-    }
+    if (band_on)
+      for (int e = sl; e < kLetters * BAND; e += W) {
+        const int x = e / BAND, row = e - x * BAND, grow = b * BAND + row;
+        prof[e] = grow < Ly ? s_sub[tclamp(Y[grow]) * kLetters + x] : (int8_t)0;
+      }
     __syncwarp();
-    const int rowbase = b * kTBand + lane * kTR;
+    const int rowbase = b * BAND + sl * kTR;
 #pragma unroll
     for (int r = 0; r < kTR; ++r) {
       H[r] = -ge * (rowbase + r + 1);
@@ -158,13 +254,13 @@ __global__ void __launch_bounds__(32 * kTWarps) match_kernel(const TraceArgs a) 
     int hbot = 0, fbot = 0;
     const int32_t* rd = scr + ((b + 1) & 1) * 2 * a.scratch_cols;
     int32_t* wr = scr + (b & 1) * 2 * a.scratch_cols;
-    uint32_t* nb_base = nib + (size_t)b * (Lx + 31) * 32;
-    for (int t = 0; t < Lx + 31; ++t) {
-      const int c = t - lane;
-      int hin = __shfl_up_sync(0xffffffffu, hbot, 1);
-      int fin = __shfl_up_sync(0xffffffffu, fbot, 1);
-      if (c >= 0 && c < Lx) {
-        if (lane == 0) {
+    uint32_t* nb_base = nib + (size_t)b * (Lx + W - 1) * W;
+    for (int t = 0; t < lx_max + W - 1; ++t) {
+      const int c = t - sl;
+      int hin = __shfl_up_sync(0xffffffffu, hbot, 1, W);
+      int fin = __shfl_up_sync(0xffffffffu, fbot, 1, W);
+      if (band_on && c >= 0 && c < Lx) {
+        if (sl == 0) {
           if (b == 0) {
             hin = -ge * (c + 1);
             fin = kSent;
@@ -174,64 +270,106 @@ __global__ void __launch_bounds__(32 * kTWarps) match_kernel(const TraceArgs a) 
           }
         }
         // the lane's 8 scores of column c: one 8-byte load
-        const uint2 pw = *reinterpret_cast<const uint2*>(prof + tclamp(X[c]) * kTBand + lane * kTR);
+        const uint2 pw = *reinterpret_cast<const uint2*>(prof + tclamp(X[c]) * BAND + sl * kTR);
         int diag = hprev;
         hprev = hin;
         int f = fin, hup = hin;
         uint32_t word = 0;
 #pragma unroll
         for (int r = 0; r < kTR; ++r) {
-          const int fo = f - ge;
-          f = max(fo, hup - go);
-          const int eo = E[r] - ge;
-          const int e = max(eo, H[r] - go);
+          // DPX max with the comparison as a predicate (pred = first >= second):
+          // cu = (F == F_up - ge), cl = (E == E_left - ge), pf = (F >= E),
+          // psim = (H == diag + S); then U = psim || pf and L = psim || !pf,
+          // since with H = max(F, E) otherwise H == F <=> pf and
+          // (H == E && H != F) <=> !pf.
+          bool cu, cl, pf, psim;
+          f = __vibmax_s32(f - ge, hup - go, &cu);
+          const int e = __vibmax_s32(E[r] - ge, H[r] - go, &cl);
           const int sv = (int)(int8_t)((r < 4 ? pw.x : pw.y) >> (8 * (r & 3)));
-          const int sim = diag + sv;
-          int h = max(e, f);
-          h = max(h, sim);
-          const uint32_t L = ((h == e) && (h != f)) || (h == sim);
-          const uint32_t U = (h == f) || (h == sim);
-          const uint32_t cu = (f == fo);
-          const uint32_t cl = (e == eo);
-          word |= ((L << 3) | (U << 2) | (cu << 1) | cl) << (4 * r);
+          const int t2 = __vibmax_s32(f, e, &pf);
+          const int h = __vibmax_s32(diag + sv, t2, &psim);
+          const uint32_t dir = psim ? 12u : (pf ? 4u : 8u);
+          word |= (dir | (cu ? 2u : 0u) | (cl ? 1u : 0u)) << (4 * r);
           diag = H[r];
           H[r] = h;
           E[r] = e;
           hup = h;
         }
-        nb_base[(size_t)t * 32 + lane] = word;
+        nb_base[(size_t)t * W + sl] = word;
         hbot = H[kTR - 1];
         fbot = f;
-        if (lane == 31 && b + 1 < nb) {
+        if (sl == W - 1 && b + 1 < nb) {
           wr[2 * c] = hbot;
           wr[2 * c + 1] = fbot;
         }
       }
     }
-    const int rr = (Ly - 1) - b * kTBand;
-    if (rr >= 0 && rr < kTBand && lane == rr / kTR) {
-      int v = 0;
+    if (band_on) {
+      const int rr = (Ly - 1) - b * BAND;
+      if (rr >= 0 && rr < BAND && sl == rr / kTR) {
+        int v = 0;
 #pragma unroll
-      for (int r = 0; r < kTR; ++r)
-        if (r == rr % kTR) v = H[r];
-      a.score[p] = v;
+        for (int r = 0; r < kTR; ++r)
+          if (r == rr % kTR) v = H[r];
+        a.score[p] = v;
+      }
     }
   }
-  // the walk, while the pair's flags are still in L2 (the warp's stores are
-  // visible to lane 0 after the warp barrier)
+  // the walks, while the pairs' flags are still in L2 (the warp's stores are
+  // visible to the warp after the warp barrier); their windows take the
+  // place of the fronts' profiles
   __syncwarp();
-  if (lane == 0) walk_pair(a, p);
+  static_assert(S * sizeof(WalkWindow) <= kTProfBytes, "walk windows fit the profile's space");
+  walk_pairs<W>(a, p, lane, reinterpret_cast<WalkWindow*>(s_prof[warp])[front]);
 }
 
 }  // namespace
 
 struct TraceState {
-  DevBuf codes, start, len, px, py, off, nib, scratch, score, outx, outy, outlen;
+  DevBuf codes, start, len, px, py, order, off, nib, scratch, score, outx, outy, outlen;
   ~TraceState() {
-    for (DevBuf* b : {&codes, &start, &len, &px, &py, &off, &nib, &scratch, &score, &outx, &outy, &outlen})
+    for (DevBuf* b : {&codes, &start, &len, &px, &py, &order, &off, &nib, &scratch, &score, &outx, &outy, &outlen})
       b->release();
   }
 };
+
+namespace {
+
+// Front width of the match kernel for a set of pairs: the least estimated
+// cost, in cells, of the rows x columns computed (whole bands of 8W rows,
+// ramps of W-1 columns) plus the walks, which run one after another for the
+// 32/W fronts of a warp (a walk step costs about as much as kWalkStep cells:
+// fitted to the kernel's times at W = 32, 16 and 8 on 3,640 pairs of 100-300
+// residues on a GB300: 0.436, 0.422 and 0.652 ms).
+constexpr double kWalkStep = 38.0;
+int trace_lanes(const std::vector<int32_t>& len, const int32_t* px, const int32_t* py, int npairs) {
+  int best = 32;
+  double best_cost = 0.0;
+  for (int W : {32, 16, 8}) {
+    const int band = 8 * W;
+    double cost = 0.0;
+    for (int k = 0; k < npairs; ++k) {
+      const int Lx = len[px[k]], Ly = len[py[k]];
+      cost += (double)((Ly + band - 1) / band) * band * (Lx + W - 1) + kWalkStep * (32 / W) * (Lx + Ly);
+    }
+    if (W == 32 || cost < best_cost) {
+      best = W;
+      best_cost = cost;
+    }
+  }
+  return best;
+}
+
+cudaError_t launch_match(int W, const TraceArgs& a, cudaStream_t s) {
+  const int per_cta = kTWarps * (32 / W);
+  const int grid = (a.npairs + per_cta - 1) / per_cta;
+  if (W == 8) match_kernel<8><<<grid, 32 * kTWarps, 0, s>>>(a);
+  else if (W == 16) match_kernel<16><<<grid, 32 * kTWarps, 0, s>>>(a);
+  else match_kernel<32><<<grid, 32 * kTWarps, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace
 
 void Ctx::extra_release() {
   delete reinterpret_cast<TraceState*>(trace_state);
@@ -276,9 +414,17 @@ int Ctx::align_pairs(const int8_t* codes, const int64_t* offsets, int n, const i
     return rc;
   // batches bounded by the nibble memory (~1 GiB of words per batch)
   const int64_t kBudgetWords = (int64_t)1 << 28;
-  const double t0 = st ? 0.0 : 0.0;
-  (void)t0;
-  if (st) cudaEventRecord(ev0, s);
+  // statistics: kernel_ms = the match kernels alone, d2h_ms = the downloads
+  cudaEvent_t ev_copied = nullptr;
+  if (st && (rc = cuda(cudaEventCreate(&ev_copied), "traceback event"))) return rc;
+  struct EventGuard {
+    cudaEvent_t e;
+    ~EventGuard() {
+      if (e) cudaEventDestroy(e);
+    }
+  } guard{ev_copied};
+  const int W = trace_lanes_forced ? trace_lanes_forced : trace_lanes(len, px, py, npairs);
+  const int band = 8 * W;
   int k0 = 0;
   while (k0 < npairs) {
     std::vector<int64_t> off;
@@ -286,14 +432,23 @@ int Ctx::align_pairs(const int8_t* codes, const int64_t* offsets, int n, const i
     int k1 = k0;
     while (k1 < npairs) {
       const int Lx = len[px[k1]], Ly = len[py[k1]];
-      const int64_t w = (int64_t)((Ly + kTBand - 1) / kTBand) * (Lx + 31) * 32;
+      const int64_t w = (int64_t)((Ly + band - 1) / band) * (Lx + W - 1) * W;
       if (k1 > k0 && words + w > kBudgetWords) break;
       off.push_back(words);
       words += w;
       ++k1;
     }
     const int m = k1 - k0;
+    // pairs of similar band counts and X lengths share a warp
+    std::vector<int32_t> order((size_t)m);
+    for (int k = 0; k < m; ++k) order[(size_t)k] = k;
+    std::stable_sort(order.begin(), order.end(), [&](int u, int v) {
+      const int bu = (len[py[k0 + u]] + band - 1) / band, bv = (len[py[k0 + v]] + band - 1) / band;
+      if (bu != bv) return bu > bv;
+      return len[px[k0 + u]] > len[px[k0 + v]];
+    });
     if ((rc = T.px.ensure(sizeof(int32_t) * m)) || (rc = T.py.ensure(sizeof(int32_t) * m)) ||
+        (rc = T.order.ensure(sizeof(int32_t) * m)) ||
         (rc = T.off.ensure(sizeof(int64_t) * m)) || (rc = T.nib.ensure(sizeof(uint32_t) * (size_t)words)) ||
         (rc = T.scratch.ensure(sizeof(int32_t) * 4 * (size_t)m * maxlen)) ||
         (rc = T.score.ensure(sizeof(int32_t) * m)) || (rc = T.outx.ensure((size_t)m * stride)) ||
@@ -301,7 +456,9 @@ int Ctx::align_pairs(const int8_t* codes, const int64_t* offsets, int n, const i
       return fail(rc, "traceback allocation");
     if ((rc = cuda(cudaMemcpyAsync(T.px.p, px + k0, sizeof(int32_t) * m, cudaMemcpyHostToDevice, s), "upload")) ||
         (rc = cuda(cudaMemcpyAsync(T.py.p, py + k0, sizeof(int32_t) * m, cudaMemcpyHostToDevice, s), "upload")) ||
-        (rc = cuda(cudaMemcpyAsync(T.off.p, off.data(), sizeof(int64_t) * m, cudaMemcpyHostToDevice, s), "upload")))
+        (rc = cuda(cudaMemcpyAsync(T.off.p, off.data(), sizeof(int64_t) * m, cudaMemcpyHostToDevice, s), "upload")) ||
+        (rc = cuda(cudaMemcpyAsync(T.order.p, order.data(), sizeof(int32_t) * m, cudaMemcpyHostToDevice, s),
+                   "upload")))
       return rc;
     TraceArgs a{};
     a.codes = (const int8_t*)T.codes.p;
@@ -309,6 +466,7 @@ int Ctx::align_pairs(const int8_t* codes, const int64_t* offsets, int n, const i
     a.len = (const int32_t*)T.len.p;
     a.px = (const int32_t*)T.px.p;
     a.py = (const int32_t*)T.py.p;
+    a.order = (const int32_t*)T.order.p;
     a.nib_off = (const int64_t*)T.off.p;
     a.nib = (uint32_t*)T.nib.p;
     a.scratch = (int32_t*)T.scratch.p;
@@ -322,9 +480,10 @@ int Ctx::align_pairs(const int8_t* codes, const int64_t* offsets, int n, const i
     a.go = go;
     a.ge = ge;
     a.sub = (const int8_t*)b_sub.p;
-    match_kernel<<<(m + kTWarps - 1) / kTWarps, 32 * kTWarps, 0, s>>>(a);
+    if (st) cudaEventRecord(ev0, s);
     ++launches;
-    if ((rc = cuda(cudaGetLastError(), "traceback launch"))) return rc;
+    if ((rc = cuda(launch_match(W, a, s), "traceback launch"))) return rc;
+    if (st) cudaEventRecord(ev1, s);
     if ((rc = cuda(cudaMemcpyAsync(outx + (size_t)k0 * stride, T.outx.p, (size_t)m * stride, cudaMemcpyDeviceToHost, s),
                    "download")) ||
         (rc = cuda(cudaMemcpyAsync(outy + (size_t)k0 * stride, T.outy.p, (size_t)m * stride, cudaMemcpyDeviceToHost, s),
@@ -335,18 +494,19 @@ int Ctx::align_pairs(const int8_t* codes, const int64_t* offsets, int n, const i
     if (score &&
         (rc = cuda(cudaMemcpyAsync(score + k0, T.score.p, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, s), "download")))
       return rc;
+    if (st) cudaEventRecord(ev_copied, s);
     if ((rc = cuda(cudaStreamSynchronize(s), "traceback sync"))) return rc;
     if (st) {
       for (int k = k0; k < k1; ++k) st->cells += (int64_t)len[px[k]] * len[py[k]];
+      float ms = 0.f, ms2 = 0.f;
+      cudaEventElapsedTime(&ms, ev0, ev1);
+      cudaEventElapsedTime(&ms2, ev1, ev_copied);
+      st->kernel_ms += ms;
+      st->d2h_ms += ms2;
     }
     k0 = k1;
   }
   if (st) {
-    cudaEventRecord(ev1, s);
-    cudaEventSynchronize(ev1);
-    float ms = 0;
-    cudaEventElapsedTime(&ms, ev0, ev1);
-    st->kernel_ms = ms;
     st->pairs = npairs;
     st->pairs_int32 = npairs;
   }
@@ -402,6 +562,12 @@ extern "C" int nwg_cherries(const int32_t* left, const int32_t* right, int nleav
     if (left[k] < 0 || right[k] < 0 || left[k] >= nleaves + k || right[k] >= nleaves + k) return -NWG_ERR_INVALID;
   }
   return cherries(left, right, nleaves, node, l, r);
+}
+
+extern "C" int nwg_set_trace_lanes(nwg_ctx* ctx, int lanes) {
+  if (!ctx || !(lanes == 0 || lanes == 8 || lanes == 16 || lanes == 32)) return NWG_ERR_INVALID;
+  reinterpret_cast<nwg::Ctx*>(ctx)->trace_lanes_forced = lanes;
+  return NWG_OK;
 }
 
 extern "C" int nwg_align_pairs(nwg_ctx* ctx, const int8_t* codes, const int64_t* offsets, int n, const int32_t* px,

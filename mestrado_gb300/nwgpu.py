@@ -181,6 +181,11 @@ class Context:
                                               D.strides[0] // 4, r0, mode, ctypes.byref(st)))
         return (D, st.as_dict()) if stats else D
 
+    def set_trace_lanes(self, lanes: int):
+        """Front width of the traceback kernel (32, 16 or 8 lanes per pair;
+        0: chosen per call)."""
+        self._check(self._lib.nwg_set_trace_lanes(self.h, int(lanes)))
+
     def align_pairs(self, codes, offsets, px, py, stats: bool = False):
         """Gapped alignments (X = px[k] columns, Y = py[k] rows): list of
         (aligned_x, aligned_y, score) in forward order."""

@@ -66,3 +66,27 @@ def test_device_alignments_rescore_to_their_score(ctx):
     for (ax, ay, sc), i, j in zip(ctx.align_pairs(codes, off, px, py), px, py):
         assert ax.replace(b"-", b"") == seqs[i] and ay.replace(b"-", b"") == seqs[j]
         assert rescore(ax, ay, sub) == sc
+
+
+@pytest.mark.parametrize("lanes", [32, 16, 8])
+def test_every_front_width_matches_oracle(lanes):
+    # 1, 2 or 4 pairs per warp, bands of 256, 128 or 64 rows: fronts of one
+    # warp with different band counts and X lengths, single- and multi-band,
+    # related pairs (long diagonal runs) and tiny ones
+    from mestrado_gb300 import Context
+    seqs = _rand_set(40 + lanes, 40, 1, 700) + _rand_set(41, 6, 1, 9)
+    S = synth.family(12, 260, ps=0.1, pi=0.03, seed=lanes)
+    seqs += [S[i] for i in range(len(S))]
+    rng = np.random.default_rng(lanes)
+    n = len(seqs)
+    px = np.concatenate([rng.integers(0, n, 70), np.arange(n - 12, n - 1)]).astype(np.int32)
+    py = np.concatenate([rng.integers(0, n, 70), np.arange(n - 11, n)]).astype(np.int32)
+    with Context(10, 2) as c:
+        c.set_trace_lanes(lanes)
+        _check(c, seqs, px, py)
+
+
+def test_trace_lanes_rejects_other_widths(ctx):
+    from mestrado_gb300._native import NWGError
+    with pytest.raises(NWGError):
+        ctx.set_trace_lanes(4)
