@@ -15,10 +15,10 @@
 //     bit2 U  = H==F || H==diag                  (:332)
 //     bit1 cU = F == F_up - ge                   (:315-316, :334)
 //     bit0 cL = E == E_left - ge                 (:336)
-//   from the predicates of four DPX maxima (__vibmax_s32).
+//   from the sign bits of four differences, appended by funnel shifts.
 //   A lane's 8 rows of one column make one 32-bit word; the W lanes of a
 //   front store W consecutive words per step: word (b*(Lx+W-1) + t)*W + k
-//   holds rows b*8W + 8k .. +7 at column t-k, row r in bits 4r..4r+3.
+//   holds rows b*8W + 8k .. +7 at column t-k, row r in bits 4(7-r)..4(7-r)+3.
 // The walk runs in the same warp right after the pairs' last bands, while
 //   their flags are still in L2, from (Lx-1, Ly-1) with the reference's rule
 //   set (continue flags of the previous move first, then up, then left, else
@@ -145,7 +145,7 @@ __device__ void walk_pairs(const TraceArgs& a, int p, int lane, WalkWindow& w) {
           } else if (x < 0) {
             cell = 6u;                // column -1: up + continue-up
           } else if (x0 - x < 32 && (y >> 3) >= g0) {
-            cell = (w.flags[((y >> 3) - g0) * 32 + (x0 - x)] >> (4 * (y & 7))) & 15u;
+            cell = (w.flags[((y >> 3) - g0) * 32 + (x0 - x)] >> (4 * (7 - (y & 7)))) & 15u;
           } else {
             state = 1;
             break;
@@ -277,19 +277,29 @@ __global__ void __launch_bounds__(32 * kTWarps) match_kernel(const TraceArgs a) 
         uint32_t word = 0;
 #pragma unroll
         for (int r = 0; r < kTR; ++r) {
-          // DPX max with the comparison as a predicate (pred = first >= second):
-          // cu = (F == F_up - ge), cl = (E == E_left - ge), pf = (F >= E),
-          // psim = (H == diag + S); then U = psim || pf and L = psim || !pf,
-          // since with H = max(F, E) otherwise H == F <=> pf and
-          // (H == E && H != F) <=> !pf.
-          bool cu, cl, pf, psim;
-          f = __vibmax_s32(f - ge, hup - go, &cu);
-          const int e = __vibmax_s32(E[r] - ge, H[r] - go, &cl);
+          // Each flag is the sign bit of one difference (a - b - 1 < 0 <=> a <= b):
+          // cu = (F_up - ge >= H_up - go), cl = (E_left - ge >= H_left - go),
+          // pf = (F >= E), ps = (diag + S >= max(F, E)), i.e. H == diag + S;
+          // then U = ps || pf and L = ps || !pf, since otherwise H = max(F, E)
+          // and H == F <=> pf, (H == E && H != F) <=> !pf.  The bits are
+          // appended to the word by funnel shifts: L, U, cU, cL of row r land
+          // in bits 4(7-r)+3 .. 4(7-r).
+          const int fo = f - ge, hgo = hup - go;
+          const uint32_t xcu = (uint32_t)(hgo - fo - 1);
+          f = max(fo, hgo);
+          const int eo = E[r] - ge, ego = H[r] - go;
+          const uint32_t xcl = (uint32_t)(ego - eo - 1);
+          const int e = max(eo, ego);
           const int sv = (int)(int8_t)((r < 4 ? pw.x : pw.y) >> (8 * (r & 3)));
-          const int t2 = __vibmax_s32(f, e, &pf);
-          const int h = __vibmax_s32(diag + sv, t2, &psim);
-          const uint32_t dir = psim ? 12u : (pf ? 4u : 8u);
-          word |= (dir | (cu ? 2u : 0u) | (cl ? 1u : 0u)) << (4 * r);
+          const int sim = diag + sv;
+          const uint32_t xpf = (uint32_t)(e - f - 1);
+          const int t2 = max(f, e);
+          const uint32_t xps = (uint32_t)(t2 - sim - 1);
+          const int h = max(sim, t2);
+          word = __funnelshift_l(xps | ~xpf, word, 1);   // L
+          word = __funnelshift_l(xps | xpf, word, 1);    // U
+          word = __funnelshift_l(xcu, word, 1);          // cU
+          word = __funnelshift_l(xcl, word, 1);          // cL
           diag = H[r];
           H[r] = h;
           E[r] = e;
