@@ -441,7 +441,7 @@ def pipeline_leg(cpu_nj_n: int = 2000):
     nj_gbs = nj_bytes / (st["device_ms"] * 1e-3) / 1e9
     L = S.lengths.astype(np.float64)
     tb_cells = float((L[left] * L[right]).sum())
-    tb_s = ast["kernel_ms"] * 1e-3 if ast.get("kernel_ms") else (t4 - t3)   # match + back kernels
+    tb_s = ast["kernel_ms"] * 1e-3 if ast.get("kernel_ms") else (t4 - t3)   # the match kernels (DP + walk)
     tb_gbs = 0.5 * tb_cells / tb_s / 1e9
     # CPU neighbor joining (oracle, one core) and the device on the same leading block
     m = min(cpu_nj_n, n)
@@ -470,7 +470,8 @@ def pipeline_leg(cpu_nj_n: int = 2000):
         "nj_roofline": {"bound": "hbm", "achieved": nj_gbs, "peak": hbm, "unit": "GB/s", "frac": nj_gbs / hbm,
                         "bytes": nj_bytes, "peak_source": src},
         "traceback_roofline": {"bound": "hbm", "achieved": tb_gbs, "peak": hbm, "unit": "GB/s", "frac": tb_gbs / hbm,
-                               "cells": tb_cells, "kernel_s": tb_s, "peak_source": src},
+                               "cells": tb_cells, "kernel_s": tb_s, "gcups": tb_cells / tb_s / 1e9,
+                               "d2h_s": ast.get("d2h_ms", 0.0) * 1e-3, "peak_source": src},
         "cpu_nj": {"n": m, "oracle_one_core_s": t6 - t5, "device_s": t8 - t7, "kind": "port",
                    "note": "the reference's buildTree restated (exact argmin), one core"},
     }
