@@ -82,6 +82,7 @@ struct BatchPlan {
   int64_t rerun_cap = 0, rerun_threads = 0;
   int64_t pairs16 = 0, pairs32 = 0, pairs_checked = 0;
   int scols = 1;
+  int64_t codes_len = 0;   // bytes of the codes buffer the sets reach (one past the last residue)
   // graph
   cudaGraphExec_t exec = nullptr;
   const int8_t* g_codes = nullptr;
@@ -166,6 +167,8 @@ static int get_plan(Ctx* c, const int64_t* xoff, int nx, const int64_t* yoff, in
   }
   const SetView& X = p->X;
   const SetView& Y = p->Y;
+  for (int k = 0; k < X.n; ++k) p->codes_len = std::max<int64_t>(p->codes_len, X.start[k] + X.len[k]);
+  for (int k = 0; k < Y.n; ++k) p->codes_len = std::max<int64_t>(p->codes_len, Y.start[k] + Y.len[k]);
   const bool force32 = mode == NWG_MODE_BATCHED_INT32 ||
                        std::max(X.maxlen, Y.maxlen) > c->i16.max_len;
   // certain int16: the shorter sequence of every pair is short enough that
@@ -301,6 +304,7 @@ static int enqueue_step(Ctx* c, BatchPlan* p, const int8_t* d_codes, float* d_D,
 
   WaveArgs a{};
   a.codes = d_codes;
+  a.codes_end = d_codes + p->codes_len;
   a.xstart = p->X.d_start; a.xlen = p->X.d_len; a.xorig = p->X.d_orig;
   a.ystart = p->Y.d_start; a.ylen = p->Y.d_len; a.yorig = p->Y.d_orig;
   a.group_y = (const int32_t*)p->gy.p;

@@ -67,6 +67,7 @@ struct DevSet {
 
 struct WaveArgs {
   const int8_t* codes;
+  const int8_t* codes_end;    // one past the last byte of the codes buffer (staging never reads past it)
   const int64_t* xstart;
   const int32_t* xlen;
   const int32_t* xorig;
@@ -94,7 +95,7 @@ struct WaveArgs {
   int triangle;
   int go, ge;
   int scratch_cols;
-  const int8_t* sub;          // 24*24 on device
+  const int8_t* sub;          // 24*24 on device, 4-byte aligned (staged by cp.async)
   // overflow guard (optimistic int16 buckets)
   int check_bound;
   int max_h;                  // the context's int16 upper limit of H (checked groups)

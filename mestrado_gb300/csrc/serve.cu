@@ -317,6 +317,7 @@ int Server::launch_batch(Slot& S) {
     return rc;
   WaveArgs a{};
   a.codes = (const int8_t*)S.codes.p;
+  a.codes_end = a.codes + total_codes;
   a.xstart = a.ystart = (const int64_t*)S.start.p;
   a.xlen = a.ylen = (const int32_t*)S.len.p;
   a.xorig = a.yorig = (const int32_t*)S.orig.p;

@@ -510,6 +510,38 @@ __device__ __forceinline__ void wave_band(const WaveArgs& a, int sl, int b, int 
   }
 }
 
+// Copies the bytes [p, p + n) into shared memory at dst + lead, where p - lead
+// is the word at or below p, and returns lead.  The thread takes words w0,
+// w0 + stride, ...: a word that lies inside [begin, end) goes by a 4-byte
+// cp.async (completed by cp_async_wait_all), the partial words at either edge
+// of the buffer by plain byte loads (bytes outside it read as 0); nothing
+// outside [begin, end) is read.
+__device__ __forceinline__ int stage_bytes(int8_t* dst, const int8_t* p, int n, const int8_t* begin,
+                                           const int8_t* end, int w0, int stride) {
+  const uintptr_t base = (uintptr_t)p & ~(uintptr_t)3;
+  const int lead = (int)((uintptr_t)p - base);
+  const int words = (lead + n + 3) >> 2;
+  for (int w = w0; w < words; w += stride) {
+    const uintptr_t src = base + 4 * (uintptr_t)w;
+    if (src >= (uintptr_t)begin && src + 4 <= (uintptr_t)end) {
+      const unsigned d = (unsigned)__cvta_generic_to_shared(dst + 4 * w);
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+    } else {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const uintptr_t q = src + j;
+        dst[4 * w + j] = (q >= (uintptr_t)begin && q < (uintptr_t)end) ? *reinterpret_cast<const int8_t*>(q)
+                                                                       : (int8_t)0;
+      }
+    }
+  }
+  return lead;
+}
+
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
 template <int R, int P, int V>
 struct MinBlocks {
   static constexpr int rows = V == 5 ? 2 * R : R;   // register rows per lane
@@ -525,14 +557,19 @@ __global__ void __launch_bounds__(kWaveThreads, (MinBlocks<R, P, V>::value)) wav
   static_assert(W == 1 || W == 8 || W == 16 || W == 32, "front width");
   static_assert(W > 1 || K == 1, "one pair per thread holds one X per front");
   extern __shared__ __align__(16) uint32_t prof[];   // Profile<R, W>: [letter][Q][front lane][4]
-  __shared__ int8_t s_sub[kLetters * kLetters];
+  __shared__ __align__(16) int8_t s_sub[kLetters * kLetters + 4];
+  // the rows of the band of both Y sequences, staged by cp.async for the profile build
+  constexpr int kTile = (BAND + 8 + 15) / 16 * 16;
+  __shared__ __align__(16) int8_t s_ytile[2][kTile];
   __shared__ long long s_job;
 
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const int sl = lane % W;                 // lane within the front
   const int seg = lane / W;                // front within the warp
-  for (int e = threadIdx.x; e < kLetters * kLetters; e += blockDim.x) s_sub[e] = a.sub[e];
+  // the substitution matrix, staged by cp.async (visible after the job loop's first barrier)
+  stage_bytes(s_sub, a.sub, kLetters * kLetters, a.sub, a.sub + kLetters * kLetters, threadIdx.x, blockDim.x);
+  cp_async_wait_all();
   // band-boundary scratch of the front: its own block of 4 x scratch_cols
   // words per X, or (W = 1) one column of the CTA's interleaved block
   int32_t* scratch =
@@ -603,16 +640,26 @@ __global__ void __launch_bounds__(kWaveThreads, (MinBlocks<R, P, V>::value)) wav
     const int yoB = has_b ? a.yorig[y1] : 0;
 
     for (int b = 0; b < nb; ++b) {
-      if (b > 0) __syncthreads();   // every warp is done with the previous band's profile
+      // the band's rows of YA and YB into the tiles (every warp is done with
+      // the previous band's profile and tiles after the barrier that follows)
+      const int na = min(BAND, LyA - b * BAND), nbr = min(BAND, LyB - b * BAND);
+      const int leadA = na > 0 ? stage_bytes(s_ytile[0], YA + b * BAND, na, a.codes, a.codes_end, threadIdx.x,
+                                             kWaveThreads)
+                               : 0;
+      const int leadB = (P == 2 && nbr > 0) ? stage_bytes(s_ytile[1], YB + b * BAND, nbr, a.codes, a.codes_end,
+                                                          threadIdx.x, kWaveThreads)
+                                            : 0;
+      cp_async_wait_all();
+      __syncthreads();
       for (int e = threadIdx.x; e < kLetters * BAND; e += kWaveThreads) {
         const int x = e / BAND;
         const int row = e - x * BAND;
         const int grow = b * BAND + row;
         const int gsh = Layout<V>::L == 3 ? a.go : 0;   // layout 3 adds the profile to T = H - go
-        const int sa = (grow < LyA ? (int)s_sub[clamp_code(YA[grow]) * kLetters + x] : 0) + gsh;
+        const int sa = (grow < LyA ? (int)s_sub[clamp_code(s_ytile[0][leadA + row]) * kLetters + x] : 0) + gsh;
         uint32_t w;
         if (P == 2) {
-          const int sb = (grow < LyB ? (int)s_sub[clamp_code(YB[grow]) * kLetters + x] : 0) + gsh;
+          const int sb = (grow < LyB ? (int)s_sub[clamp_code(s_ytile[1][leadB + row]) * kLetters + x] : 0) + gsh;
           w = Lanes<2>::arith(sa, sb);
         } else {
           w = (uint32_t)sa;
