@@ -406,6 +406,15 @@ def pipeline_leg(cpu_nj_n: int = 2000):
     ctx = Context(10, 2)
     ctx.autotune()
     ctx.score_all(S)                                   # plan, graph and tuning warm
+    # one untimed pass of the later stages: their kernels' first launches (module
+    # loading) and their buffers stay out of the timed pass
+    Dw = ctx.score_all(S)
+    jw = ctx.nj(Dw)
+    _, lw, rw = cherries(jw["i"], jw["j"], len(S))
+    cw, ow = encode(S)
+    ctx.align_pairs(cw, ow, lw, rw)
+    ctx.msa(codes=cw, offsets=ow, left=jw["i"], right=jw["j"])
+    del Dw
     t0 = time.perf_counter()
     D = ctx.score_all(S)
     t1 = time.perf_counter()
