@@ -90,3 +90,24 @@ def test_trace_lanes_rejects_other_widths(ctx):
     from mestrado_gb300._native import NWGError
     with pytest.raises(NWGError):
         ctx.set_trace_lanes(4)
+
+
+@pytest.mark.parametrize("go,ge", [(3, 5), (10, 10), (0, 0), (15, 1)])
+@pytest.mark.parametrize("lanes", [32, 16])
+def test_gap_models_match_oracle(go, ge, lanes):
+    # go >= ge takes the one-max F chain (F from max(E, diag + S) of the row
+    # above), go < ge the direct recurrence; both give the reference's flags
+    from mestrado_gb300 import Context
+    seqs = _rand_set(60 + go, 24, 1, 500) + _rand_set(61, 4, 1, 12)
+    S = synth.family(10, 200, ps=0.1, pi=0.03, seed=go + 3)
+    seqs += [S[i] for i in range(len(S))]
+    rng = np.random.default_rng(go * 7 + ge)
+    n = len(seqs)
+    px = rng.integers(0, n, 40).astype(np.int32)
+    py = rng.integers(0, n, 40).astype(np.int32)
+    codes, off = encode(seqs)
+    with Context(go, ge) as c:
+        c.set_trace_lanes(lanes)
+        out = c.align_pairs(codes, off, px, py)
+    for (ax, ay, s), i, j in zip(out, px, py):
+        assert (ax, ay, s) == O.traceback(seqs[i], seqs[j], go, ge), (i, j)
