@@ -33,7 +33,7 @@ const char* letter_order();
 
 struct TuneChoice {
   int R;   // rows per lane (4 to 32, even; not a multiple of 4, or 28: layouts 2 to 4 on int16x2 lanes only)
-  int V;   // register layout (0 to 5)
+  int V;   // register layout (0 to 6)
   int W;   // lanes per wavefront (32, 16, 8): band of W*R rows; 1: one pair per thread, bands of R rows
 };
 // Rows a Y of `rows` residues occupies under choice t (whole bands).
@@ -45,6 +45,7 @@ inline int padded_rows(const TuneChoice& t, int rows) {
 // (the narrow fronts and the rows per lane that are not multiples of 4 exist
 // for int16x2 lanes only).
 inline TuneChoice int32_choice(TuneChoice t) {
+  if (t.V == 6) t.V = 3;   // the split strips exist for int16x2 lanes only
   if (t.W == 32 && t.R % 4 == 0 && t.R != 28) return t;
   const int band = t.W * t.R;
   int R = 32;

@@ -176,7 +176,7 @@ int Ctx::autotune(bool force, nwg_tune_result* out) {
     TuneChoice pick = kDefaultTune[k], pick_wave = kDefaultTuneWave[k];
     for (int W : {32, 16, 8, 1})
     for (int R : kCandR) {
-      for (int V = 0; V <= 5; ++V) {
+      for (int V = 0; V <= 6; ++V) {
         const TuneChoice cand{R, V, W};
         const int Lyc = probe_rows(k, cand);
         if (Lyc == 0 || !wave_exists(R, 2, V, W) || (V == 4 && go < ge)) continue;

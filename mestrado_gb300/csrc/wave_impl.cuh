@@ -38,6 +38,12 @@
 // = max(F'[r-1] - ge, F'[r-1] - go, m[r-1]) = max(F'[r-1] - ge, m[r-1]);
 // m does not depend on F, so only the F' update itself stays on the path
 // from one row to the next (and from one lane to the next).
+// V = 6 is layout 3 with the lane's strip split in two halves one column
+// apart: at step t lane k's upper R/2 rows work on column t - 2k and its lower
+// R/2 rows on column t - 2k - 1, fed by the upper half's last row of the step
+// before.  The two halves are independent within a step, so the lane has two
+// dependency chains of R/2 rows instead of one of R, with layout 3's 3 ALU
+// operations per word; the skew between lanes becomes two columns.
 // V = 5 is layout 3 with two X per front: every lane runs the strips of two
 // X (adjacent in length order) against the same band, row by row
 // interleaved, so two independent dependency chains share the lane's issue
@@ -214,8 +220,8 @@ constexpr int scratch_stride() { return W == 1 ? kWaveThreads : 1; }
 
 template <int V>
 struct Layout {
-  static constexpr int K = V == 5 ? 2 : 1;    // X per front
-  static constexpr int L = V == 5 ? 3 : V;    // register layout of each strip
+  static constexpr int K = V == 5 ? 2 : 1;                // X per front
+  static constexpr int L = (V == 5 || V == 6) ? 3 : V;    // register layout of each strip
 };
 
 template <int R, int P, int V>
@@ -353,6 +359,136 @@ __device__ __forceinline__ void strip_column_pair(BandState<R, P, 3> (&s)[2], co
         s[k].E[r] = e;
         tup[k] = s[k].H[r];
       }
+    }
+  }
+}
+
+// Rows [R0, R0 + RH) (RH a multiple of 4) of a layout-3 strip at one column:
+// s.H holds T = H - go; tup is T of the row above, diag T of the row above at
+// the previous column, f the F of the row above; pp the column's profile
+// (S + go).  Returns F of the last row.
+template <int R0, int RH, int R, int P, int W>
+__device__ __forceinline__ uint32_t strip_rows3(BandState<R, P, 3>& s, const uint4* __restrict__ pp, uint32_t diag,
+                                                uint32_t tup, uint32_t f, uint32_t NGE, uint32_t NGO) {
+  using L = Lanes<P>;
+  static_assert(R0 % 4 == 0 && RH % 4 == 0 && R0 + RH <= R, "4-row profile quads");
+#pragma unroll
+  for (int q = R0 / 4; q < (R0 + RH) / 4; ++q) {
+    const uint4 pv = pp[q * W];
+    const uint32_t sv[4] = {pv.x, pv.y, pv.z, pv.w};
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+      const int r = q * 4 + w;
+      f = L::addmax(f, NGE, tup);                                      // F[r][c]
+      const uint32_t e = L::addmax(s.E[r], NGE, s.H[r]);               // E[r][c]
+      const uint32_t h = L::max3(e, f, L::add(diag, sv[w]));           // H[r][c]
+      diag = s.H[r];
+      s.H[r] = L::add(h, NGO);
+      s.E[r] = e;
+      tup = s.H[r];
+    }
+  }
+  return f;
+}
+
+// One band of layout 6 (layout 3, the lane's strip split in two halves one
+// column apart; one X per front, wavefronts of 8 to 32 lanes).  Arguments as
+// wave_band's.
+template <int R, int P, int W>
+__device__ __forceinline__ void wave_band_split(const WaveArgs& a, int sl, int b, int nb, const int8_t* X0, int Lx0,
+                                                int Lmin, int Lmax, const uint32_t* __restrict__ prof,
+                                                int32_t* __restrict__ scratch, int rowA, int rowB, bool wantA0,
+                                                bool wantB0, int xo0, int yoA, int yoB, float* jobD, int64_t jobld) {
+  using L = Lanes<P>;
+  constexpr int BAND = W * R;
+  constexpr int RH = R / 2;
+  static_assert(W >= 8 && RH % 4 == 0, "split strips: wavefronts, halves of whole 4-row quads");
+  const uint32_t NGE = L::packed(-a.ge);
+  const uint32_t NGO = L::arith(-a.go, -a.go);
+  const uint32_t NGEA = L::arith(-a.ge, -a.ge);
+  const uint32_t SENT = L::splat(kShortMin + a.ge);
+  constexpr int LS = Profile<R, W>::kLetterStride;
+  BandState<R, P, 3> s;
+  const int rowbase = b * BAND + sl * R;
+  const int gsh = a.go;   // layout 3 carries T = H - go
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    s.H[r] = L::splat(-a.ge * (rowbase + r + 1) - gsh);   // T[row][-1]
+    s.E[r] = SENT;
+  }
+  const bool work = Lx0 > 0;
+  const int32_t* rd = scratch + ((b + 1) & 1) * 2 * a.scratch_cols;   // band b-1
+  int32_t* wr = scratch + (b & 1) * 2 * a.scratch_cols;
+  uint32_t hprev = L::splat(-a.ge * rowbase - gsh);   // T of the row above the strip at column c-1
+  uint32_t mid_prev = s.H[RH - 1];                    // T of the upper half's last row at column c-2
+  uint32_t fmid = 0;                                   // F of the upper half's last row at column c-1
+  uint32_t hbot = 0, fbot = 0;
+  int xnext = (sl == 0 && work) ? (int)X0[0] : 0;
+  int xcur = 0;                                        // code of the upper half's previous column
+  uint32_t hb = L::splat(-a.ge - gsh);                 // T[-1][c] of the column lane 0 works on (band 0)
+  const bool top = b == 0;
+  const bool last_band = b + 1 >= nb;
+  const uint4* pl = reinterpret_cast<const uint4*>(prof) + sl;
+
+  auto step = [&](int t, auto checked) {
+    constexpr bool kChecked = decltype(checked)::value;
+    const int c = t - 2 * sl;   // the upper half's column; the lower half's is c - 1
+    uint32_t hin = __shfl_up_sync(0xffffffffu, hbot, 1, W);
+    uint32_t fin = __shfl_up_sync(0xffffffffu, fbot, 1, W);
+    const int xl = xnext;
+    if (kChecked) {
+      if (c + 1 >= 0 && c + 1 < Lx0) xnext = X0[c + 1];
+    } else if (W == 32 || work) {
+      xnext = X0[min(c + 1, Lx0 - 1)];
+    }
+    const bool up_on = kChecked ? (c >= 0 && c < Lx0) : (W == 32 || work);
+    const bool lo_on = kChecked ? (c >= 1 && c - 1 < Lx0) : (W == 32 || work);
+    if (up_on && sl == 0) {
+      hin = top ? hb : (uint32_t)rd[2 * c];
+      fin = top ? SENT : (uint32_t)rd[2 * c + 1];
+    }
+    if (!kChecked || c >= 0) hb = L::add(hb, NGEA);
+    const uint32_t mid_cur = s.H[RH - 1];   // the upper half's last row at column c-1
+    if (lo_on) {
+      fbot = strip_rows3<RH, RH, R, P, W>(s, pl + clamp_code(xcur) * LS, mid_prev, mid_cur, fmid, NGE, NGO);
+      hbot = s.H[R - 1];
+    }
+    if (up_on) {
+      const uint32_t diag = hprev;
+      hprev = hin;
+      fmid = strip_rows3<0, RH, R, P, W>(s, pl + clamp_code(xl) * LS, diag, hin, fin, NGE, NGO);
+      mid_prev = mid_cur;
+      xcur = xl;
+    }
+    if (sl == W - 1 && !last_band && lo_on) {
+      wr[2 * (c - 1)] = (int32_t)hbot;
+      wr[2 * (c - 1) + 1] = (int32_t)fbot;
+    }
+  };
+  // ramp-up (lanes before their columns), steady state (both halves of every
+  // lane on a column), ramp-down (lanes past their last column)
+  int t = 0;
+  const int t1 = Lmin < 2 * W - 1 ? Lmin : 2 * W - 1;
+  for (; t < t1; ++t) step(t, std::true_type{});
+#pragma unroll 2
+  for (; t < Lmin; ++t) step(t, std::false_type{});
+  for (; t < Lmax + 2 * W - 1; ++t) step(t, std::true_type{});
+
+  // H[] now holds the last column (T = H - go); the lane owning a pair's last row reports.
+  if (wantA0) {
+    const int rr = rowA - b * BAND;
+    if (rr >= 0 && rr < BAND && sl == rr / R) {
+      const int v = L::lo(pick<R>(s.H, rr % R)) + gsh;
+      if (jobD) put_score_job(a, jobD, jobld, xo0, yoA, v);
+      else put_score(a, xo0, yoA, v);
+    }
+  }
+  if (P == 2 && wantB0) {
+    const int rr = rowB - b * BAND;
+    if (rr >= 0 && rr < BAND && sl == rr / R) {
+      const int v = L::hi(pick<R>(s.H, rr % R)) + gsh;
+      if (jobD) put_score_job(a, jobD, jobld, xo0, yoB, v);
+      else put_score(a, xo0, yoB, v);
     }
   }
 }
@@ -667,9 +803,14 @@ __global__ void __launch_bounds__(kWaveThreads, (MinBlocks<R, P, V>::value)) wav
         prof[Profile<R, W>::index(x, row)] = w;
       }
       __syncthreads();
-      if (Lmax > 0)
-        wave_band<R, P, V, W>(a, sl, b, nb, X, Lx, Lmin, Lmax, prof, scratch, LyA - 1, LyB - 1, wantA, wantB, xo,
-                              yoA, yoB, jobD, jobld);
+      if (Lmax > 0) {
+        if constexpr (V == 6)
+          wave_band_split<R, P, W>(a, sl, b, nb, X[0], Lx[0], Lmin, Lmax, prof, scratch, LyA - 1, LyB - 1, wantA[0],
+                                   wantB[0], xo[0], yoA, yoB, jobD, jobld);
+        else
+          wave_band<R, P, V, W>(a, sl, b, nb, X, Lx, Lmin, Lmax, prof, scratch, LyA - 1, LyB - 1, wantA, wantB, xo,
+                                yoA, yoB, jobD, jobld);
+      }
     }
   }
 }
@@ -707,6 +848,7 @@ constexpr bool extra_rows(int R) { return R % 4 != 0 || R == 28; }
 // lane its own front, bands of R rows) on int16x2 lanes with V = 0, 2, 3 or 4.
 // The other R: int16x2 wavefronts of 32, 16 or 8 lanes with V = 2, 3 or 4.
 inline bool wave_variant_exists(int R, int P, int V, int W) {
+  if (V == 6) return !extra_rows(R) && R % 8 == 0 && P == 2 && (W == 32 || W == 16 || W == 8);
   if (extra_rows(R)) return P == 2 && (W == 32 || W == 16 || W == 8) && V >= 2 && V <= 4;
   if (W == 32) return (P == 1 || P == 2) && V >= 0 && V <= 5;
   if (W == 1) return P == 2 && (V == 0 || V == 2 || V == 3 || V == 4);
@@ -722,6 +864,9 @@ struct Entry {
     using std::integral_constant;
     if constexpr (W > 1 && !kExtra) {
       if (V == 5) return fn(integral_constant<int, P>{}, integral_constant<int, 5>{}, integral_constant<int, W>{});
+    }
+    if constexpr (W > 1 && !kExtra && P == 2 && R % 8 == 0) {
+      if (V == 6) return fn(integral_constant<int, P>{}, integral_constant<int, 6>{}, integral_constant<int, W>{});
     }
     if (V == 4) return fn(integral_constant<int, P>{}, integral_constant<int, 4>{}, integral_constant<int, W>{});
     if (V == 3) return fn(integral_constant<int, P>{}, integral_constant<int, 3>{}, integral_constant<int, W>{});

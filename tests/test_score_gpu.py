@@ -184,6 +184,24 @@ def test_finer_band_templates_match_oracle(R, V, W):
     _check_template(R, V, W)
 
 
+@pytest.mark.parametrize("R", [8, 16, 24, 32])
+@pytest.mark.parametrize("W", [32, 16, 8])
+def test_split_strip_templates_match_oracle(R, W):
+    # layout 6: layout 3 with each lane's strip in two halves one column apart
+    # (two columns of skew between lanes), single- and multi-band
+    _check_template(R, 6, W)
+
+
+@pytest.mark.parametrize("go,ge", [(3, 5), (15, 1), (0, 0), (40, 30)])
+def test_split_strips_under_gap_models(go, ge):
+    from mestrado_gb300 import Context
+    seqs = _gap_case_sets()["short"]
+    ref = O.score_all(seqs, go, ge, threads=os.cpu_count())
+    with Context(go, ge) as c:
+        c.set_tuning(16, 6, 16)
+        assert np.array_equal(c.score_all(seqs), ref)
+
+
 def _check_template(R, V, W):
     from mestrado_gb300 import Context
     seqs = _rand_set(40 + R, 26, 1, 900)
