@@ -272,7 +272,7 @@ typedef struct {
   int64_t pairs;        /* pairs (i<j) this launch computes                    */
   int64_t cells;        /* their L_i*L_j sum                                   */
   double ms;            /* device time (events around this launch alone)       */
-  int32_t variant;      /* register layout of the wave kernel (0..5)          */
+  int32_t variant;      /* register layout of the wave kernel (0..6)          */
   int32_t lanes;        /* lanes per wavefront (32, 16, 8)                    */
 } nwg_launch_rec;
 
