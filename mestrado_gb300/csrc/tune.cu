@@ -68,7 +68,7 @@ int probe_rows(int k, const TuneChoice& t) {
   return whole > lo ? whole : hi;
 }
 
-const char kCacheTag[] = "nwgpu-tune-6";
+const char kCacheTag[] = "nwgpu-tune-7";   // bumped whenever the candidate set changes
 
 }  // namespace
 
