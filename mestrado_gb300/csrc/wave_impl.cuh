@@ -242,24 +242,31 @@ __device__ __forceinline__ uint32_t strip_column(BandState<R, P, V>& s, const ui
   constexpr int Q = (R + 3) / 4;   // 4-row profile quads; rows past R of the last one are skipped
   uint32_t f = fin;
   if (V == 3) {
-    // s.H holds T = H - go; hin is T of the row above; sv is S + go
+    // s.H holds T = H - go; hin is T of the row above; sv is S + go.  The next
+    // row's diag + S is taken from the old T[r] before T[r] is overwritten, so
+    // no value has to outlive its register's new contents (the profile quad
+    // of the next 4 rows is loaded one quad ahead).
     uint32_t tup = hin;
+    uint4 pv = pp[0];
+    uint32_t hd = L::add(diag, pv.x);
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
-      const uint4 pv = pp[q * W];
-      const uint32_t sv[4] = {pv.x, pv.y, pv.z, pv.w};
+      const uint4 pn = (q + 1 < Q) ? pp[(q + 1) * W] : pv;
+      const uint32_t sn[4] = {pv.y, pv.z, pv.w, pn.x};                 // S + go of the row below
 #pragma unroll
       for (int w = 0; w < 4; ++w) {
         const int r = q * 4 + w;
         if (r >= R) continue;
         f = L::addmax(f, NGE, tup);                                      // F[r][c]
         const uint32_t e = L::addmax(s.E[r], NGE, s.H[r]);               // E[r][c]
-        const uint32_t h = L::max3(e, f, L::add(diag, sv[w]));           // H[r][c]
-        diag = s.H[r];
+        const uint32_t hn = L::add(s.H[r], sn[w]);                       // row r + 1: diag + S
+        const uint32_t h = L::max3(e, f, hd);                            // H[r][c]
         s.H[r] = L::add(h, NGO);
         s.E[r] = e;
         tup = s.H[r];
+        hd = hn;
       }
+      pv = pn;
     }
     return f;
   }
@@ -372,21 +379,31 @@ __device__ __forceinline__ uint32_t strip_rows3(BandState<R, P, 3>& s, const uin
                                                 uint32_t tup, uint32_t f, uint32_t NGE, uint32_t NGO) {
   using L = Lanes<P>;
   static_assert(R0 % 4 == 0 && RH % 4 == 0 && R0 + RH <= R, "4-row profile quads");
+  constexpr int Q0 = R0 / 4, Q1 = (R0 + RH) / 4;
+  // The next row's diag + S is taken from the old T[r] before T[r] is
+  // overwritten, so no value has to outlive its register's new contents (the
+  // profile quad of the next 4 rows is loaded one quad ahead).
+  uint4 pv = pp[Q0 * W];
+  uint32_t hd = L::add(diag, pv.x);                                    // row R0: diag + S
 #pragma unroll
-  for (int q = R0 / 4; q < (R0 + RH) / 4; ++q) {
-    const uint4 pv = pp[q * W];
+  for (int q = Q0; q < Q1; ++q) {
+    const uint4 pn = (q + 1 < Q1) ? pp[(q + 1) * W] : pv;
     const uint32_t sv[4] = {pv.x, pv.y, pv.z, pv.w};
+    const uint32_t sn[4] = {pv.y, pv.z, pv.w, pn.x};                   // S + go of the row below
 #pragma unroll
     for (int w = 0; w < 4; ++w) {
       const int r = q * 4 + w;
       f = L::addmax(f, NGE, tup);                                      // F[r][c]
       const uint32_t e = L::addmax(s.E[r], NGE, s.H[r]);               // E[r][c]
-      const uint32_t h = L::max3(e, f, L::add(diag, sv[w]));           // H[r][c]
-      diag = s.H[r];
+      const uint32_t hn = L::add(s.H[r], sn[w]);                       // row r + 1: diag + S
+      const uint32_t h = L::max3(e, f, hd);                            // H[r][c]
       s.H[r] = L::add(h, NGO);
       s.E[r] = e;
       tup = s.H[r];
+      hd = hn;
+      (void)sv;
     }
+    pv = pn;
   }
   return f;
 }
