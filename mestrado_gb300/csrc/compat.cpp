@@ -34,6 +34,9 @@ nwg_ctx* make_ctx(int go, int ge) {
     std::exit(0);
   }
   if (rc != NWG_OK) die(rc, nullptr, "nwg_ctx_create");
+  // the device's tuned kernel table: read from its cache, or measured once
+  // (a few seconds) and cached; on failure the built-in table stays
+  nwg_autotune(c, 0, nullptr);
   return c;
 }
 

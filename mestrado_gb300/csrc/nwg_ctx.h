@@ -57,17 +57,18 @@ constexpr int kTuneClasses = NWG_TUNE_CLASSES;
 // Upper bound of the Y rows of each class; the last class takes every longer Y.
 constexpr int kClassRows[kTuneClasses] = {64,  96,  128, 160, 192, 224, 256,  320,
                                           384, 448, 512, 640, 768, 1024, 1536, 1 << 30};
-// Defaults before tuning (the table measured on a GB300): one pair per
-// thread (W = 1) for the classes up to 96 rows, wavefronts above.
+// Defaults before tuning (the table measured on a GB300): one pair per thread
+// (W = 1) for the classes up to 96 rows, wavefronts above, mostly the
+// layouts with 1.5 ALU operations per cell (3, and 6 where R is a multiple of 8).
 constexpr TuneChoice kDefaultTune[kTuneClasses] = {
-    {32, 4, 1},  {32, 4, 1},  {4, 2, 32},  {8, 0, 32},  {8, 0, 32},  {8, 0, 32},  {8, 0, 32},  {12, 0, 32},
-    {12, 0, 32}, {16, 2, 32}, {16, 2, 32}, {20, 2, 32}, {24, 2, 32}, {32, 2, 32}, {24, 2, 32}, {24, 2, 32}};
+    {32, 4, 1},  {32, 4, 1},  {16, 5, 8},  {20, 3, 8},  {24, 6, 8},  {28, 3, 8},  {32, 6, 8},  {20, 3, 16},
+    {24, 6, 16}, {28, 3, 16}, {32, 6, 16}, {20, 3, 32}, {24, 6, 16}, {32, 3, 32}, {24, 6, 16}, {32, 3, 32}};
 // The best wavefront (W >= 8) per class before tuning, for latency-bound
 // callers: one pair per thread needs 256 X per CTA and streams a Y in bands,
 // so it wins on throughput over many X but lengthens a small job.
 constexpr TuneChoice kDefaultTuneWave[kTuneClasses] = {
-    {8, 5, 8},   {12, 3, 8},  {4, 2, 32},  {8, 0, 32},  {8, 0, 32},  {8, 0, 32},  {8, 0, 32},  {12, 0, 32},
-    {12, 0, 32}, {16, 2, 32}, {16, 2, 32}, {20, 2, 32}, {24, 2, 32}, {32, 2, 32}, {24, 2, 32}, {24, 2, 32}};
+    {8, 5, 8},   {12, 0, 8},  {16, 5, 8},  {20, 3, 8},  {24, 6, 8},  {28, 3, 8},  {32, 6, 8},  {20, 3, 16},
+    {24, 6, 16}, {28, 3, 16}, {32, 6, 16}, {20, 3, 32}, {24, 6, 16}, {32, 3, 32}, {24, 6, 16}, {32, 3, 32}};
 int tune_class(int rows);
 
 struct BatchPlan;
