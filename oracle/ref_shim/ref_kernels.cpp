@@ -25,15 +25,15 @@
  * offset = 1), so thread-local indexing (blockThread = 0) never aliases.
  *
  * Patches, each forced by running the shipped text correctly (the reference's
- * defects, SURVEY numbering):
- *  - defect 4: a 16x16 block loads only entries 0..287 of the 576-entry matrix
+ * defects):
+ *  - a 16x16 block loads only entries 0..287 of the 576-entry matrix
  *    into shmSM (NeedlemanWunsch.cu:26-35, :188-197).  Before the first pair,
  *    each kernel is run once per loader thread idx = 0..559 on an empty pair
  *    (length 0, returns right after the load), which fills all 576 entries of
  *    its static shmSM through the kernel's own load code;
- *  - defect 3: BLOCK_SIZE 16 with 256 threads overflows AE_shared/sharedYSeq
+ *  - BLOCK_SIZE 16 with 256 threads overflows AE_shared/sharedYSeq
  *    (:75-77, :243-245).  One thread per block indexes slot 0 only;
- *  - defects 1, 2, 7 (the host-side parse/copy, AlignmentScore.cu): not part
+ *  - the host-side parse and copy defects (AlignmentScore.cu): not part
  *    of this text; the caller passes correctly encoded, fully reversed codes.
  * Uninitialised locals of the backtrace kernel (tmpMatchX/Y, shifted out
  * before use) are zero-initialised by the compiler flag
