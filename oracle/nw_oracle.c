@@ -1,7 +1,7 @@
 /*
  * nw_oracle.c -- CPU restatement of the ptersnow/mestrado hot path.
  *
- * TEST INFRASTRUCTURE ONLY: this is the checker.  The product library never
+ * TEST INFRASTRUCTURE ONLY: this is the oracle.  The product library never
  * links or calls it.  Every function names the reference file:line it
  * restates; the reference's GPU code itself does not build on CUDA 13 and is
  * defective as shipped, so the contract is the reference's recurrence on

@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product library links, calls or
  * executes this code; only tests/, __graft_entry__.smoke() and bench.py's CPU
- * baseline leg use it, always as the checker and never as the thing measured
+ * baseline leg use it, always as the oracle and never as the thing measured
  * or shipped.
  *
  * Each function cites the reference file:line whose behaviour it restates.
@@ -106,7 +106,7 @@ typedef struct {
  * joins must hold n-1 records. */
 void nwo_nj_model(float* D, int n, nwo_join* joins, nwo_nj_model_stats* stats);
 
-/* Progressive alignment along the guide tree (this build's definition: the
+/* Progressive alignment along the guide tree (this library's definition: the
  * reference's AlignmentMatch::computeMSA, AlignmentMatch.cu:320-434, is an
  * empty loop -- parity unpinned).  Internal node n+k joins left[k] (X,
  * columns) and right[k] (Y, rows), left[k] < right[k].  A profile is its
