@@ -1,4 +1,4 @@
-"""The oracle's progressive alignment (this build's definition; the
+"""The oracle's progressive alignment (this library's definition; the
 reference's computeMSA is an empty loop): two sequences give the pairwise
 traceback exactly, every row is its sequence with gaps, and columns are never
 all gaps."""
