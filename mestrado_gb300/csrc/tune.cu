@@ -194,6 +194,7 @@ int Ctx::autotune(bool force, nwg_tune_result* out) {
           cudaEventElapsedTime(&ms, ev0, ev1);
         }
         if (rc) break;
+        if (!(ms > 0.f)) continue;   // no usable timing: not a candidate
         const double rate = (double)nx * ny * padded_rows(cand, Lyc) * Lx / (ms * 1e-3);
         found[k].push_back({cand, rate});
         const double est = padded_rows(cand, Ly) / rate;
